@@ -1,0 +1,411 @@
+#!/usr/bin/env python3
+"""Benchmark of the batched, graph-captured frame on one GPU per rank.
+
+A step is one frame of the 4096-block configuration (16^3 blocks of octree
+depth 3..7, ~626 M dense vertices, 1920x1080): interpolation of every block
+from its sparse nodes into the HBM-resident brick store, then the front-to-back
+ray cast of the whole block cube, replayed as one CUDA graph.  Inputs are
+seeded synthetic data with the configuration's shapes and distributions.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's CPU implementation of the path -- its
+dense-field generator (DenseFieldInterpolator<3>, restated in oracle/) -- on
+all host cores over a bounded sample of the same blocks.  The reference has no
+CPU ray caster, so that number covers interpolation only (which favours it).
+
+For N > 1 (torchrun), every rank runs the same frame on its own GPU (replicas:
+the path has no exchange step on one node), value = all ranks' vertices / the
+slowest rank's time.  One JSON line is printed by rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "dense Gvertices/s; Gsamples/s & ms/frame @1080p; adjoint/forward time ratio"
+UNIT = "Gvertices/s"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--config", choices=["cfg3", "cfg2"], default="cfg3")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the adjoint and 16-bit measurements")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
+        os.environ.get("LOCAL_RANK", "0"))
+
+
+def make_workload(name):
+    from revise_gb300 import workloads
+    return workloads.cfg3() if name == "cfg3" else workloads.cfg2()
+
+
+# ------------------------------------------------------------------ CPU legs
+
+def _cpu_interp_blocks(args):
+    """Worker: interpolate the listed blocks with the oracle (the reference algorithm), return (vertices, seconds)."""
+    blocks, n2i_list, sp_list = args
+    import oracle
+    t = time.perf_counter()
+    v = 0
+    for d, n2i, sp in zip(blocks, n2i_list, sp_list):
+        oracle.interp_f32(n2i, sp, d)
+        v += ((1 << d) + 1) ** 3
+    return v, time.perf_counter() - t
+
+
+def _sample_blocks(w, seconds_budget, seed=0):
+    """A depth-stratified block sample whose CPU interpolation takes roughly the budget (single core)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    order = rng.permutation(w.nblocks)
+    # ~60 M vertices/s for one core of the restated reference algorithm: size the sample to the budget
+    target = seconds_budget * 60e6
+    picked, tot = [], 0
+    for b in order:
+        d = int(w.blocks[b, 3])
+        picked.append(int(b))
+        tot += ((1 << d) + 1) ** 3
+        if tot >= target:
+            break
+    return picked
+
+
+def cpu_interp_rate(w, blocks, processes=1):
+    """Vertices/s of the oracle interpolator over `blocks` with `processes` workers (spawned)."""
+    jobs = [[] for _ in range(processes)]
+    for i, b in enumerate(blocks):
+        jobs[i % processes].append(b)
+    payload = []
+    for js in jobs:
+        payload.append(([int(w.blocks[b, 3]) for b in js], [w.block_nodes(b)[0] for b in js],
+                        [w.block_nodes(b)[1] for b in js]))
+    if processes == 1:
+        v, t = _cpu_interp_blocks(payload[0])
+        return v / t, t
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(processes) as pool:
+        res = pool.map(_cpu_interp_blocks, payload)
+    wall = time.perf_counter() - t0
+    v = sum(r[0] for r in res)
+    return v / wall, wall
+
+
+def run_reference(a):
+    rank, world, _ = dist_env()
+    if world > 1 and rank != 0:
+        return 0
+    import oracle
+    oracle.port()
+    w = make_workload(a.config)
+    cores = os.cpu_count() or 1
+    budget = max(1.0, a.cpu_seconds / max(1, a.steps + a.warmup)) * cores
+    blocks = _sample_blocks(w, budget, seed=1)
+    rates = []
+    for i in range(a.warmup + a.steps):
+        r, _ = cpu_interp_rate(w, blocks, processes=cores)
+        if i >= a.warmup:
+            rates.append(r)
+    value = statistics.median(rates) / 1e9
+    sample_v = sum(((1 << int(w.blocks[b, 3])) + 1) ** 3 for b in blocks)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": w.vertices / (value * 1e9) * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": f"{a.config}: {w.nblocks} blocks, depths 3-7, {w.vertices} dense vertices",
+                   "what": "dense-field generation only (the reference has no CPU ray caster)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{len(blocks)} blocks ({sample_v} vertices) per step, all cores, "
+                                   "restated DenseFieldInterpolator<3> (oracle/s3r_oracle.c)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------ clocks
+
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.f = None
+
+    def start(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def run_gb300(a):
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        dist = None
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    from revise_gb300 import _lib, host, workloads
+    from revise_gb300.api import Context, FramePlan
+
+    w = make_workload(a.config)
+    ctx = Context(dev)
+    view = host.view_for(w)
+    plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=16)
+    stream = torch.cuda.current_stream()
+    sparse = torch.from_numpy(w.sparse).cuda()
+    tf = torch.from_numpy(np.ascontiguousarray(w.tf)).cuda()
+    W, H = w.W, w.H
+    rgba = torch.zeros(W * H * 4, dtype=torch.float32, device="cuda")
+    argb = torch.zeros(W * H, dtype=torch.int32, device="cuda")
+    samples = torch.zeros(1, dtype=torch.int64, device="cuda")
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
+    if not a.no_autotune:
+        plan.autotune(view, sparse, tf, reps=3)
+    info = plan.info
+    V = int(info.vertices)
+    alg_bytes = 10 * int(info.nodes) + 4 * V  # n2i + values per node, one dense write per vertex
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    def timed(fn, k):
+        """k runs of fn, each bracketed by CUDA events on the stream, L2 flushed between runs."""
+        ts = []
+        for _ in range(k):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            ts.append((e0, e1))
+        torch.cuda.synchronize()
+        return [x.elapsed_time(y) for x, y in ts]
+
+    frame = lambda: plan.run(view, sparse, tf, rgba, argb)  # noqa: E731
+    for _ in range(max(3, a.warmup)):
+        frame()
+    clocks = Clocks(dev)
+    clocks.start()
+    barrier()
+    l0 = ctx.launches
+    step_ms = timed(frame, a.steps)
+    launches = ctx.launches - l0
+    barrier()
+    clk = clocks.stop()
+    ms = sum(step_ms) / len(step_ms)
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # kernel-level figures (same stream, CUDA events): interpolation and render alone
+    interp_ms = timed(lambda: plan.interp(sparse), max(5, a.steps // 2))
+    samples.zero_()
+    render_ms = timed(lambda: plan.render(view, tf, rgba, None, samples), max(5, a.steps // 2))
+    nsamp = int(samples.item()) / max(5, a.steps // 2)
+    t_interp = statistics.median(interp_ms)
+    t_render = statistics.median(render_ms)
+
+    # end to end through the C ABI with host buffers: H2D of the sparse values, frame, D2H of the image
+    sparse_host = torch.from_numpy(w.sparse).pin_memory()
+    img_host = torch.empty(W * H, dtype=torch.int32).pin_memory()
+    sparse_e2e = torch.empty_like(sparse)
+
+    def e2e_step():
+        sparse_e2e.copy_(sparse_host, non_blocking=True)
+        plan.run(view, sparse_e2e, tf, rgba, argb)
+        img_host.copy_(argb, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = timed(e2e_step, max(5, a.steps // 2))
+    t_e2e = sum(e2e_ms) / len(e2e_ms)
+
+    extras = {}
+    if not a.no_extras and rank == 0:
+        extras = measure_extras(ctx, torch, np)
+
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    hbm = peaks.get("hbm_gbs")
+    peak_note = "of measured"
+    if not hbm:
+        hbm, peak_note = 6800.0, "of fallback"
+    achieved = alg_bytes / (t_interp * 1e-3) / 1e9
+    traffic = None
+    tp = ROOT / "profiles" / "interp_tiles_cfg3_traffic.json"
+    if tp.exists():
+        traffic = json.loads(tp.read_text()).get("dram_bytes_per_launch")
+
+    cpu = None
+    if rank == 0:
+        blocks = _sample_blocks(w, a.cpu_seconds, seed=2)
+        rate, secs = cpu_interp_rate(w, blocks, processes=1)
+        sv = sum(((1 << int(w.blocks[b, 3])) + 1) ** 3 for b in blocks)
+        cpu = {"value": rate / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{len(blocks)} of {w.nblocks} blocks ({sv} vertices, {secs:.1f} s), one core, "
+                         "dense-field generation only (restated DenseFieldInterpolator<3>)"}
+
+    if rank == 0:
+        value = world * V / (ms * 1e-3) / 1e9
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator, revise_gb300/workloads.py)",
+            "config": {"workload": f"{a.config}: {w.nblocks} blocks (16^3 at level {w.level}), octree depths 3-7, "
+                                   f"{V} dense vertices, {int(info.nodes)} sparse nodes, {W}x{H}, "
+                                   "interpolate + ray-cast per frame, CUDA graph",
+                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                       "l2": "L2 flushed (2x129 MB write) between timed steps; 2.5 GB brick store per step",
+                       "tile_cells": int(info.tile_cells), "render_tile": int(info.render_tile)},
+            "ms_per_frame": ms, "frames_per_s": 1e3 / ms,
+            "interp": {"ms": t_interp, "gvertices_per_s": V / (t_interp * 1e-3) / 1e9,
+                       "algorithmic_bytes": alg_bytes},
+            "render": {"ms": t_render, "gsamples_per_s": nsamp / (t_render * 1e-3) / 1e9, "samples": nsamp},
+            "roofline": {"bound": "hbm", "kernel": "interp_tiles_kernel (batched tile interpolation)",
+                         "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "peak_source": peak_note, "traffic": traffic},
+            "e2e": {"value": V / (t_e2e * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": t_e2e,
+                    "h2d_bytes_per_step": int(sparse.numel() * 4), "d2h_bytes_per_step": int(W * H * 4)},
+            "gpu_launches": int(launches),
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        line.update(extras)
+        print(json.dumps(line))
+    plan.close()
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def measure_extras(ctx, torch, np):
+    """Adjoint/forward ratio on the 8-block differentiation config and 16-bit-brick frame rates (cfg2)."""
+    from revise_gb300 import _lib, host, workloads
+    from revise_gb300.api import FramePlan
+    out = {}
+    w = workloads.cfg5()
+    view = host.view_for(w)
+    plan = FramePlan(ctx, w)
+    sp = torch.from_numpy(w.sparse).cuda()
+    tf = torch.from_numpy(np.ascontiguousarray(w.tf)).cuda()
+    rgba = torch.zeros(w.W * w.H * 4, device="cuda")
+    plan.interp(sp)
+    dl = torch.rand_like(rgba) * 0.01
+    dtf = torch.zeros(w.tf.size, device="cuda")
+    bricks, _ = plan.bricks()
+    dd = torch.zeros(bricks.numel(), device="cuda")
+
+    def tm(fn, k=10):
+        for _ in range(3):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(k):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k
+
+    fwd = tm(lambda: plan.render(view, tf, rgba))
+    bwd = tm(lambda: plan.backward(view, tf, rgba, dl, dtf, dd))
+    out["adjoint"] = {"workload": "cfg5: 2x2x2 blocks depth 6, 512x512", "forward_render_ms": fwd,
+                      "backward_ms": bwd, "adjoint_forward_ratio": bwd / fwd}
+    plan.close()
+    w2 = workloads.cfg2()
+    v2 = host.view_for(w2)
+    sp2 = torch.from_numpy(w2.sparse).cuda()
+    tf2 = torch.from_numpy(np.ascontiguousarray(w2.tf)).cuda()
+    img = torch.zeros(w2.W * w2.H * 4, device="cuda")
+    prec = {}
+    for name, fmt in (("f32", _lib.BRICK_F32), ("f16", _lib.BRICK_F16), ("bf16", _lib.BRICK_BF16)):
+        p = FramePlan(ctx, w2, fmt)
+        ms = tm(lambda: p.run(v2, sp2, tf2, img))
+        prec[name] = {"ms_per_frame": ms, "frames_per_s": 1e3 / ms}
+        p.close()
+    out["precision_cfg2"] = prec
+    return out
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        return run_reference(a)
+    return run_gb300(a)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,275 @@
+/*
+ * s3r — GB300-native (sm_103a) implementation of the ReVisE block hot path:
+ * sparse-octree -> dense-grid interpolation, the block ray caster and the
+ * blend of per-block image parts.
+ *
+ * C ABI.  Every entry point is extern "C", never throws, and returns an int
+ * status (S3R_OK == 0).  The message of the last failure on a context comes
+ * from s3r_last_error(ctx) (ctx may be NULL for failures before a context
+ * exists).  Pointers documented "device" are device pointers owned by the
+ * caller; pointers documented "host" are host memory.  Each call that touches
+ * the GPU takes the stream to order its work on (a cudaStream_t passed as
+ * void*; NULL = the legacy default stream) and returns without synchronizing
+ * unless documented otherwise.  One context per host thread, as the
+ * reference keeps one renderer per worker thread.
+ *
+ * Reference interfaces replaced (paths relative to the reference project root):
+ *   s3r_interp_dense           DenseFieldInterpolatorArr_cu_3::interpolate
+ *                              (src/s3dmm_cuda/DenseFieldInterpolatorArr_cu_3.cu:197-257) and the static
+ *                              DenseFieldInterpolator<3>::interpolate(dense, sparse, nodes)
+ *                              (include/s3dmm/DenseFieldInterpolator.hpp:198-419)
+ *   s3r_clear_viewport         DenseFieldRenderer_cu::clearViewport (src/s3dmm_cuda/DenseFieldRenderer_cu.cu:268-277)
+ *   s3r_render_block_argb      DenseFieldRenderer_cu::renderDenseField, Argb mode
+ *                              (src/s3dmm_cuda/DenseFieldRenderer_cu.cu:279-486, renderArgb.hpp:30-55)
+ *   s3r_block_cube,
+ *   s3r_block_view_rect,
+ *   s3r_camera_look_at         the host-side parameter set-up of renderDenseField (:317-409, :353-372)
+ *   s3r_b2f_order              BackToFrontOrder<MacroBlock<3>>::range(eye) (include/BackToFrontOrder.hpp:61-359)
+ *   s3r_bound_rect             getBoundRect (src/s3vs_worker/cuda/VsWorker_cu.cpp:51-88)
+ *   s3r_blend_image_part_host,
+ *   s3r_compose_parts          blendImagePart (src/s3vs_lib/BlendImagePart.hpp:61-145)
+ *   s3r_make_color_transfer    makeColorTransferVector (include/s3vs/ColorTransferFunction.hpp:27-69)
+ *   s3r_frame_*                no single counterpart: the batched form of VsWorker_cu::renderScenePart
+ *                              (src/s3vs_worker/cuda/VsWorker_cu.cpp:225-313) over a whole block cube
+ *   s3r_render_argb_backward   none (the reference has no adjoint)
+ */
+#ifndef S3R_H
+#define S3R_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define S3R_ABI_VERSION 1
+
+/* status codes */
+#define S3R_OK 0
+#define S3R_ERR_INVALID 1     /* bad argument (null pointer, size out of range, ...) */
+#define S3R_ERR_CUDA 2        /* a CUDA runtime call failed; see s3r_last_error */
+#define S3R_ERR_NOMEM 3       /* device or host allocation failed */
+#define S3R_ERR_CANCELLED 4   /* the cancel flag was set between blocks */
+#define S3R_ERR_UNSUPPORTED 5 /* valid request this build does not handle */
+
+/* Field value that marks "outside the domain" in sparse input
+ * (BlockTreeFieldProvider<N>::noFieldValue(), include/s3dmm/BlockTreeFieldProvider.hpp:137-139).
+ * Masked sparse nodes must carry this value, never NaN: NaN in a dense grid
+ * means "not computed yet" while the interpolation runs. */
+#define S3R_NO_FIELD_VALUE 1e30f
+
+/* Deepest subtree the kernels accept: 2^9+1 = 513 vertices per edge. */
+#define S3R_MAX_DEPTH 9
+
+typedef struct s3r_ctx s3r_ctx;
+typedef struct s3r_plan s3r_plan;
+
+/* ------------------------------------------------------------------ context */
+
+int s3r_abi_version(void);
+/* Binds the calling thread to `device` (cudaSetDevice, as selectGpu does,
+ * src/s3dmm_cuda/selectGpu.cu:6-9) and creates a context there. */
+int s3r_ctx_create(int device, s3r_ctx** out);
+int s3r_ctx_destroy(s3r_ctx* ctx);
+const char* s3r_last_error(const s3r_ctx* ctx);
+/* Kernel launches this context has issued so far (for launch accounting). */
+uint64_t s3r_ctx_launch_count(const s3r_ctx* ctx);
+
+/* ---------------------------------------------------- dense interpolation */
+
+/* Dense (2^depth+1)^3 float grid of one block-tree subtree from its n sparse
+ * nodes.  n2i_xyz (device): n vertex indices (x, y, z as uint16, 6 bytes per
+ * node, the BlockTreeNodes<3> n2i layout); sparse (device): n values aligned
+ * with n2i, S3R_NO_FIELD_VALUE where masked; dense (device): receives the grid,
+ * x fastest (ordinal (z*e + y)*e + x with e = 2^depth+1), NaN outside the
+ * domain.  Scratch: a (2^depth+1)^3 float grid owned by the context, grown on
+ * demand (the call may allocate device memory the first time it sees a
+ * larger depth).  Bit-identical to the reference CPU interpolator. */
+int s3r_interp_dense(s3r_ctx* ctx, const uint16_t* n2i_xyz, const float* sparse, uint32_t n, uint32_t depth,
+                     float* dense, void* stream);
+
+/* --------------------------------------------------------- camera / view */
+
+/* Renderer eye parameters (RenderKernelEyeParam, src/s3dmm_cuda/RenderKernelParam.hpp:56-65)
+ * plus the world-to-eye rotation rows and translation the view rectangle needs.
+ * ortho != 0 (no reference counterpart): rays start at eye + e1*x + e2*y and run along n. */
+typedef struct s3r_camera {
+    float eye[3];
+    float e1[3];
+    float e2[3];
+    float n[3];
+    float w;
+    float h;
+    int32_t ortho;
+    int32_t reserved;
+    float view_r[9];
+    float view_t[3];
+} s3r_camera;
+
+/* Everything one render needs besides bricks and the transfer function. */
+typedef struct s3r_view {
+    s3r_camera cam;
+    uint32_t W, H;         /* viewport, pixels */
+    uint32_t level;        /* block level: cube half size 5/2^level, world cube [-5,5]^3 */
+    float field_min;       /* global field range (BlockTreeFieldService::fieldRange) */
+    float field_max;
+    float threshold;       /* absolute threshold; opacity factor = (threshold-min)/(max-min) */
+    float quality;         /* sampling quality (renderQuality) */
+    uint32_t tf_n;         /* transfer-function entries, RGBA float each, 2..4096 */
+    float alpha_stop;      /* batched path: stop a ray once its alpha exceeds this (>= 1: never) */
+    uint32_t reserved[3];
+} s3r_view;
+
+/* getLookAt(eye, center, up) + the eye set-up of DenseFieldRenderer_cu.cu:353-372.
+ * Perspective: fovy_deg is the vertical field of view.  Orthographic (ortho != 0):
+ * ortho_height is the world height the viewport covers. */
+int s3r_camera_look_at(const double eye[3], const double center[3], const double up[3], double fovy_deg,
+                       uint32_t W, uint32_t H, int32_t ortho, double ortho_height, s3r_camera* out);
+
+/* Cube of block idx at level (DenseFieldRenderer_cu.cu:337-350). */
+int s3r_block_cube(uint32_t level, const uint32_t idx[3], float center[3], float* half_size);
+
+/* View rectangle {x, y, W, H} (pixels) the reference launches a block's rays over
+ * (DenseFieldRenderer_cu.cu:374-409). */
+int s3r_block_view_rect(const s3r_view* view, const uint32_t idx[3], int32_t rect[4]);
+
+/* ------------------------------------------------------ plain block render */
+
+/* Fills W*H pixels with value (0; NaN bits for the MIP mode). */
+int s3r_clear_viewport(s3r_ctx* ctx, uint32_t* viewport, uint32_t W, uint32_t H, uint32_t value, void* stream);
+
+/* Ray-casts one block into an ARGB32 viewport (device, W*H, top row first) with
+ * the reference's Argb-mode arithmetic: exact FP32 trilinear filtering, linear
+ * transfer-function lookup, opacity correction, front-to-back compositing with
+ * early termination at alpha > 0.996, then blend-above into the pixel with
+ * ARGB8 quantization.  brick (device): (2^depth+1)^3 floats; tf (device): tf_n
+ * RGBA floats; rect: the block's view rectangle (s3r_block_view_rect). */
+int s3r_render_block_argb(s3r_ctx* ctx, const s3r_view* view, const float* brick, uint32_t depth,
+                          const uint32_t idx[3], const int32_t rect[4], const float* tf, uint32_t* viewport,
+                          void* stream);
+
+/* ----------------------------------------------------------- ordering */
+
+/* Back-to-front order of the blocks of index box [bmin, bmax) whose world box
+ * is [cmin, cmax], for the eye point.  out (host): capacity*3 uint32; *count
+ * receives the block count (the full count even when capacity is smaller). */
+int s3r_b2f_order(const uint32_t bmin[3], const uint32_t bmax[3], const double cmin[3], const double cmax[3],
+                  const double eye[3], uint32_t* out, uint32_t capacity, uint32_t* count);
+
+/* World box of an index box at level (s3vs::boundingBoxOfIndexBox, src/s3vs_worker/BlockOrderUtil.hpp:29-52). */
+int s3r_index_box_world(uint32_t level, const uint32_t bmin[3], const uint32_t bmax[3], double cmin[3],
+                        double cmax[3]);
+
+/* ------------------------------------------------------ image parts, blend */
+
+/* Bounding rectangle {x, y, w, h} of the pixels with nonzero alpha byte, in
+ * image rows as stored (getBoundRect).  w == h == 0 when there are none.
+ * Synchronizes the stream (the result lands in host memory). */
+int s3r_bound_rect(s3r_ctx* ctx, const uint32_t* viewport, uint32_t W, uint32_t H, int32_t rect[4], void* stream);
+
+/* Copies the w x h sub-image at (x, y) of a W-wide image into dst (w*h pixels); device pointers. */
+int s3r_crop(s3r_ctx* ctx, const uint32_t* image, uint32_t W, const int32_t rect[4], uint32_t* dst, void* stream);
+
+/* Host restatement of blendImagePart: src (sw x sh at origin ox, oy) over dst (dw x dh). */
+int s3r_blend_image_part_host(uint32_t* dst, int32_t dw, int32_t dh, const uint32_t* src, int32_t sw, int32_t sh,
+                              int32_t ox, int32_t oy, int32_t just_copy, int32_t offx, int32_t offy);
+
+/* One image part for s3r_compose_parts: a device ARGB32 image at an origin. */
+typedef struct s3r_image_part {
+    const uint32_t* pixels;
+    int32_t origin[2];
+    int32_t size[2];
+} s3r_image_part;
+
+/* Blends the parts into dst (device, dw x dh, origin offx, offy) in array order,
+ * each exactly as blendImagePart would (parts[0] first; just_copy_first copies it). */
+int s3r_compose_parts(s3r_ctx* ctx, const s3r_image_part* parts, uint32_t nparts, int32_t just_copy_first,
+                      uint32_t* dst, int32_t dw, int32_t dh, int32_t offx, int32_t offy, void* stream);
+
+/* ------------------------------------------------ transfer-function table */
+
+/* npoints control points sorted by x: xs (host) and rgba (host, 4 per point). */
+int s3r_make_color_transfer(const double* xs, const double* rgba, uint32_t npoints, uint32_t color_count,
+                            float* out);
+
+/* --------------------------------------------------- batched frame (plan) */
+
+#define S3R_BRICK_F32 0
+#define S3R_BRICK_F16 1  /* value = offset + scale * half, per-brick FP32 scale/offset */
+#define S3R_BRICK_BF16 2 /* value = offset + scale * bfloat16 */
+
+/* Static description of a block set: the topology part of a block tree level
+ * (one BlockTreeNodes n2i list per block), fixed across time frames. */
+typedef struct s3r_frame_desc {
+    uint32_t level;            /* blocks are cubes of this level */
+    uint32_t nblocks;
+    const uint32_t* blocks;    /* host: nblocks x {ix, iy, iz, depth} */
+    const uint64_t* node_off;  /* host: nblocks+1 prefix offsets into n2i / sparse values */
+    const uint16_t* n2i;       /* host: node_off[nblocks] x {x, y, z} */
+    uint32_t brick_format;     /* S3R_BRICK_* */
+    uint32_t tile_cells;       /* interpolation tile edge in cells: 8, 16 or 32; 0 = autotuned */
+    uint32_t render_tile;      /* render CTA shape id; 0 = autotuned */
+    uint32_t reserved;
+} s3r_frame_desc;
+
+typedef struct s3r_plan_info {
+    uint64_t nodes;          /* sparse nodes over all blocks */
+    uint64_t vertices;       /* dense vertices over all blocks */
+    uint64_t brick_bytes;    /* bytes of the brick store */
+    uint64_t tiles;          /* interpolation work items */
+    uint64_t tile_entries;   /* binned node entries (nodes on tile boundaries repeat) */
+    uint32_t tile_cells;
+    uint32_t render_tile;
+    uint32_t brick_format;
+    uint32_t nblocks;
+} s3r_plan_info;
+
+/* Bins the nodes by interpolation tile, uploads the plan and allocates the
+ * brick store (device).  Allocates; call before any stream capture. */
+int s3r_frame_plan(s3r_ctx* ctx, const s3r_frame_desc* desc, s3r_plan** out);
+int s3r_plan_destroy(s3r_plan* plan);
+int s3r_plan_info_get(const s3r_plan* plan, s3r_plan_info* out);
+/* Device pointer to the brick store and, per block, its vertex offset (host, nblocks+1 entries). */
+int s3r_plan_bricks(const s3r_plan* plan, void** bricks, const uint64_t** vertex_off);
+/* Per-brick {scale, offset} pairs (device, 2 floats per block; F16/BF16 only, else NULL). */
+int s3r_plan_brick_scales(const s3r_plan* plan, const float** scale_offset);
+
+/* Project-written autotuner: times the interpolation of `sparse` with tiles of
+ * 8, 16 and 32 cells and the frame render with each CTA shape, `reps` runs
+ * each after one warm-up, keeps the fastest of both and re-bins the plan for
+ * the chosen tile.  Synchronizes the stream; allocates; drops captured graphs. */
+int s3r_plan_autotune(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* sparse, const float* tf,
+                      uint32_t reps, void* stream);
+
+/* Interpolates every block of the plan from sparse (device, node_off[nblocks]
+ * values aligned with n2i) into the brick store, in one launch of tile work items. */
+int s3r_frame_interp(s3r_ctx* ctx, s3r_plan* plan, const float* sparse, void* stream);
+
+/* Ray-casts the brick store front to back, block after block along each ray,
+ * each block sampled exactly as s3r_render_block_argb samples it, composited
+ * in FP32 without ARGB8 quantization.  rgba (device, optional): W*H float RGBA,
+ * non-premultiplied colour and alpha, pixel (vx, vy) at (H-1-vy)*W+vx as in the
+ * ARGB viewport; argb (device, optional): the same pixels as ARGB32;
+ * samples (device, optional): one uint64 counter incremented by the samples taken. */
+int s3r_frame_render(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* tf, float* rgba,
+                     uint32_t* argb, unsigned long long* samples, void* stream);
+
+/* s3r_frame_interp + s3r_frame_render as one CUDA graph, captured on the first
+ * call for this (plan, pointers) and replayed afterwards; the view is copied to
+ * the device before each replay.  Allocates on the first call. */
+int s3r_frame_run(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* sparse, const float* tf,
+                  float* rgba, uint32_t* argb, unsigned long long* samples, void* stream);
+
+/* Adjoint of s3r_frame_render (F32 bricks) for L = 1/2 sum (I - target)^2:
+ * given the forward image rgba (device) and dl_drgba = I - target (device,
+ * W*H*4), accumulates dL/dtf (device, tf_n*4 floats) and dL/ddense (device,
+ * one float per brick vertex).  Sample positions are recomputed per ray. */
+int s3r_render_argb_backward(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* tf,
+                             const float* rgba, const float* dl_drgba, float* dtf, float* ddense, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* S3R_H */

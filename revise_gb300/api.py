@@ -1,0 +1,323 @@
+"""GPU-side Python API over the s3r C ABI, with torch providing device memory
+and streams (plumbing only: every computation runs in the s3r CUDA kernels).
+
+Mirrors the reference's interfaces for this path:
+  Context.interp_dense          DenseFieldInterpolatorTpl_cu_3::interpolate(dst, sparse, nodes)
+                                (include/s3dmm_cuda/DenseFieldInterpolatorTpl_cu_3.hpp:103-107)
+  DenseFieldRenderer            DenseFieldRenderer_cu (include/s3dmm_cuda/DenseFieldRenderer_cu.hpp:32-54)
+  VsWorker                      VsWorker_cu / VsWorkerInterface::renderScenePart
+                                (src/s3vs_worker/cuda/VsWorker_cu.cpp:225-313)
+  FramePlan                     the batched frame (no reference counterpart)
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib, host
+from ._lib import FrameDesc, ImagePart, PlanInfo, View, arr, check, ptr
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("revise_gb300 needs a CUDA device (no CPU fallback)")
+    return torch
+
+
+def _stream(stream):
+    torch = _torch()
+    if stream is None:
+        return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if hasattr(stream, "cuda_stream"):
+        return C.c_void_p(stream.cuda_stream)
+    return C.c_void_p(int(stream))
+
+
+class _CudaArray:
+    """Zero-copy view of s3r-owned device memory for torch.as_tensor."""
+
+    def __init__(self, addr: int, shape, typestr: str, owner):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(addr), False),
+                                         "version": 2, "strides": None}
+        self._owner = owner
+
+
+def device_array(addr: int, shape, dtype: str, owner=None):
+    torch = _torch()
+    typestr = {"f4": "<f4", "f2": "<f2", "u2": "<u2", "u4": "<u4"}[dtype]
+    return torch.as_tensor(_CudaArray(addr, shape, typestr, owner), device="cuda")
+
+
+def to_device_n2i(n2i: np.ndarray):
+    """(n, 3) uint16 node indices -> device int16 tensor holding the same bits."""
+    torch = _torch()
+    return torch.from_numpy(np.ascontiguousarray(n2i, dtype=np.uint16).view(np.int16)).cuda()
+
+
+class Context:
+    """One s3r context (one per host thread, bound to one device)."""
+
+    def __init__(self, device: int = 0):
+        _torch()
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        check(self.lib.s3r_ctx_create(device, C.byref(h)))
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if self.h:
+            self.lib.s3r_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc):
+        check(rc, self.h)
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.s3r_ctx_launch_count(self.h))
+
+    # -- dense interpolation ------------------------------------------------
+    def interp_dense(self, n2i_dev, sparse_dev, depth: int, out=None, stream=None):
+        torch = _torch()
+        e = (1 << depth) + 1
+        if out is None:
+            out = torch.empty(e ** 3, dtype=torch.float32, device="cuda")
+        n = int(sparse_dev.numel())
+        self._check(self.lib.s3r_interp_dense(self.h, ptr(n2i_dev), ptr(sparse_dev), n, depth, ptr(out),
+                                              _stream(stream)))
+        return out
+
+    # -- plain render ------------------------------------------------------
+    def clear_viewport(self, viewport, W: int, H: int, value: int = 0, stream=None):
+        self._check(self.lib.s3r_clear_viewport(self.h, ptr(viewport), W, H, value, _stream(stream)))
+
+    def render_block_argb(self, view: View, brick, depth: int, idx, rect, tf_dev, viewport, stream=None):
+        i = (C.c_uint32 * 3)(*[int(x) for x in idx])
+        r = (C.c_int32 * 4)(*[int(x) for x in rect])
+        self._check(self.lib.s3r_render_block_argb(self.h, C.byref(view), ptr(brick), depth, i, r, ptr(tf_dev),
+                                                   ptr(viewport), _stream(stream)))
+
+    def bound_rect(self, viewport, W: int, H: int, stream=None):
+        r = (C.c_int32 * 4)()
+        self._check(self.lib.s3r_bound_rect(self.h, ptr(viewport), W, H, r, _stream(stream)))
+        return tuple(r[:])
+
+    def crop(self, image, W: int, rect, dst, stream=None):
+        r = (C.c_int32 * 4)(*rect)
+        self._check(self.lib.s3r_crop(self.h, ptr(image), W, r, ptr(dst), _stream(stream)))
+
+    def compose_parts(self, parts, dst, dw: int, dh: int, offset=(0, 0), just_copy_first: bool = False,
+                      stream=None):
+        """parts: list of (device uint32 tensor, (ox, oy), (w, h)) blended in order into dst."""
+        arrp = (ImagePart * max(1, len(parts)))()
+        for i, (px, origin, size) in enumerate(parts):
+            arrp[i].pixels = ptr(px).value
+            arrp[i].origin[0], arrp[i].origin[1] = int(origin[0]), int(origin[1])
+            arrp[i].size[0], arrp[i].size[1] = int(size[0]), int(size[1])
+        self._check(self.lib.s3r_compose_parts(self.h, arrp, len(parts), 1 if just_copy_first else 0, ptr(dst), dw,
+                                               dh, int(offset[0]), int(offset[1]), _stream(stream)))
+
+
+@dataclass
+class ImagePartResult:
+    """s3vs::RgbaImagePart (include/s3vs/types.hpp:47-57): ARGB32 pixels at an origin."""
+    origin: tuple
+    size: tuple
+    pixels: np.ndarray  # (h, w) uint32
+
+
+class FramePlan:
+    """A batched block set resident on the GPU: binned nodes, brick store, render table."""
+
+    def __init__(self, ctx: Context, w, brick_format: int = _lib.BRICK_F32, tile_cells: int = 16,
+                 render_tile: int = 0):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        self.blocks = np.ascontiguousarray(w.blocks, dtype=np.uint32)
+        self.node_off = np.ascontiguousarray(w.node_off, dtype=np.uint64)
+        self.n2i = np.ascontiguousarray(w.n2i, dtype=np.uint16)
+        d = FrameDesc()
+        d.level = w.level
+        d.nblocks = self.blocks.shape[0]
+        d.blocks = arr(self.blocks, C.c_uint32)
+        d.node_off = arr(self.node_off, C.c_uint64)
+        d.n2i = arr(self.n2i, C.c_uint16)
+        d.brick_format = brick_format
+        d.tile_cells = tile_cells
+        d.render_tile = render_tile
+        h = C.c_void_p()
+        ctx._check(self.lib.s3r_frame_plan(ctx.h, C.byref(d), C.byref(h)))
+        self.h = h
+        self.fmt = brick_format
+        self.level = w.level
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.s3r_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def info(self) -> PlanInfo:
+        i = PlanInfo()
+        check(self.lib.s3r_plan_info_get(self.h, C.byref(i)))
+        return i
+
+    def bricks(self):
+        """Zero-copy device tensor of the brick store and the per-block vertex offsets."""
+        p = C.c_void_p()
+        off = _lib.u64p()
+        check(self.lib.s3r_plan_bricks(self.h, C.byref(p), C.byref(off)))
+        nb = self.blocks.shape[0]
+        offs = np.ctypeslib.as_array(off, shape=(nb + 1,)).copy()
+        dt = "f4" if self.fmt == _lib.BRICK_F32 else ("f2" if self.fmt == _lib.BRICK_F16 else "u2")
+        return device_array(p.value, (int(offs[-1]),), dt, self), offs
+
+    def brick_scales(self):
+        p = C.c_void_p()
+        check(self.lib.s3r_plan_brick_scales(self.h, C.byref(p)))
+        if not p.value:
+            return None
+        return device_array(p.value, (self.blocks.shape[0], 2), "f4", self)
+
+    def interp(self, sparse_dev, stream=None):
+        self.ctx._check(self.lib.s3r_frame_interp(self.ctx.h, self.h, ptr(sparse_dev), _stream(stream)))
+
+    def render(self, view: View, tf_dev, rgba=None, argb=None, samples=None, stream=None):
+        self.ctx._check(self.lib.s3r_frame_render(self.ctx.h, self.h, C.byref(view), ptr(tf_dev), ptr(rgba),
+                                                  ptr(argb), ptr(samples), _stream(stream)))
+
+    def run(self, view: View, sparse_dev, tf_dev, rgba=None, argb=None, samples=None, stream=None):
+        self.ctx._check(self.lib.s3r_frame_run(self.ctx.h, self.h, C.byref(view), ptr(sparse_dev), ptr(tf_dev),
+                                               ptr(rgba), ptr(argb), ptr(samples), _stream(stream)))
+
+    def autotune(self, view: View, sparse_dev, tf_dev, reps: int = 3, stream=None):
+        self.ctx._check(self.lib.s3r_plan_autotune(self.ctx.h, self.h, C.byref(view), ptr(sparse_dev), ptr(tf_dev),
+                                                   reps, _stream(stream)))
+
+    def backward(self, view: View, tf_dev, rgba, dl_drgba, dtf, ddense, stream=None):
+        self.ctx._check(self.lib.s3r_render_argb_backward(self.ctx.h, self.h, C.byref(view), ptr(tf_dev),
+                                                          ptr(rgba), ptr(dl_drgba), ptr(dtf), ptr(ddense),
+                                                          _stream(stream)))
+
+
+class DenseFieldRenderer:
+    """DenseFieldRenderer_cu for the Argb mode: interpolates one block's dense
+    field (DeviceField::makeField, DenseFieldRenderer_cu.cu:504-545) and ray-casts
+    it into a device ARGB32 viewport (renderDenseField, :279-486)."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.state = None
+        self._dense = None
+        self._tf = None
+
+    def set_render_shared_state(self, state: "RenderSharedState"):
+        self.state = state
+        self._tf = None
+
+    def clear_viewport(self, viewport):
+        s = self.state
+        self.ctx.clear_viewport(viewport, s.view.W, s.view.H, 0)
+
+    def render_dense_field(self, viewport, level: int, index, cancelled=lambda: False):
+        torch = _torch()
+        s = self.state
+        b = s.block_index[(int(index[0]), int(index[1]), int(index[2]))]
+        depth = int(s.blocks[b, 3])
+        n2i_dev, sparse_dev = s.device_nodes(b)
+        self._dense = self.ctx.interp_dense(n2i_dev, sparse_dev, depth, out=None)
+        if self._tf is None:
+            self._tf = torch.from_numpy(np.ascontiguousarray(s.tf, dtype=np.float32)).cuda()
+        if cancelled():
+            return
+        rect = host.block_view_rect(s.view, index)
+        if rect[2] == 0 or rect[3] == 0:
+            return
+        self.ctx.render_block_argb(s.view, self._dense, depth, index, rect, self._tf, viewport)
+
+
+class RenderSharedState:
+    """The parts of s3vs::VsRenderSharedState (include/s3vs/VsRenderSharedState.hpp:29-46)
+    the Argb path reads: field service (block nodes and values), camera/view and
+    transfer function."""
+
+    def __init__(self, workload, alpha_stop: float = 2.0):
+        self.w = workload
+        self.view = host.view_for(workload, alpha_stop)
+        self.tf = workload.tf
+        self.blocks = workload.blocks
+        self.block_index = {(int(b[0]), int(b[1]), int(b[2])): i for i, b in enumerate(workload.blocks)}
+        self._dev = {}
+
+    def device_nodes(self, b: int):
+        if b not in self._dev:
+            torch = _torch()
+            n2i, vals = self.w.block_nodes(b)
+            self._dev[b] = (to_device_n2i(n2i), torch.from_numpy(np.ascontiguousarray(vals)).cuda())
+        return self._dev[b]
+
+
+class VsWorker:
+    """VsWorkerInterface with the CUDA worker's renderScenePart: clear, order the
+    index box back to front, render every block, read back, crop."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.renderer = DenseFieldRenderer(ctx)
+        self.state = None
+        self.viewport = None
+
+    def initialize(self, shader_path: str = "", log_info: bool = False, log_file: str = "", thread_id: int = 0):
+        pass  # the context already bound the device (selectGpu)
+
+    def set_render_shared_state(self, state: RenderSharedState):
+        self.state = state
+        self.renderer.set_render_shared_state(state)
+
+    def update_state(self, flags: int = ~0):
+        pass
+
+    def render_scene_part(self, level: int, index_box_min, index_box_max, cancelled=lambda: False):
+        torch = _torch()
+        s = self.state
+        W, H = s.view.W, s.view.H
+        if self.viewport is None or self.viewport.numel() != W * H:
+            self.viewport = torch.empty(W * H, dtype=torch.int32, device="cuda")
+        self.renderer.clear_viewport(self.viewport)
+        cmin, cmax = host.index_box_world(level, index_box_min, index_box_max)
+        order = host.b2f_order(index_box_min, index_box_max, cmin, cmax, s.w.eye)
+        for idx in order:
+            if cancelled():
+                return None
+            if tuple(int(x) for x in idx) not in s.block_index:
+                continue
+            self.renderer.render_dense_field(self.viewport, level, idx, cancelled)
+        rect = self.ctx.bound_rect(self.viewport, W, H)
+        if rect[2] == 0:
+            return ImagePartResult((0, 0), (0, 0), np.zeros((0, 0), dtype=np.uint32))
+        crop = torch.empty(rect[2] * rect[3], dtype=torch.int32, device="cuda")
+        self.ctx.crop(self.viewport, W, rect, crop)
+        pix = crop.cpu().numpy().view(np.uint32).reshape(rect[3], rect[2])
+        return ImagePartResult((rect[0], rect[1]), (rect[2], rect[3]), pix)

@@ -1,0 +1,1165 @@
+// Host side of the s3r C ABI (include/s3r.h): contexts, argument checks,
+// parameter set-up restated from the reference's host code, the batched
+// plan (tile binning of the octree nodes), CUDA-graph capture of a frame and
+// the tile-size / CTA-shape autotuner.  Built with -ffp-contract=off so that
+// float set-up code rounds as written.
+#include "s3r_internal.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+using namespace s3r;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+} // namespace
+
+struct s3r_ctx {
+    int device = 0;
+    std::string err;
+    float* grid = nullptr; // single-block interpolation scratch
+    size_t grid_cap = 0;   // floats
+    int32_t* rect_dev = nullptr;
+    int32_t* rect_host = nullptr; // pinned
+    s3r_image_part* parts_dev = nullptr;
+    size_t parts_cap = 0;
+    cudaStream_t capture = nullptr;
+    uint64_t launches = 0;
+    int sms = 152;
+};
+
+struct s3r_plan {
+    s3r_ctx* ctx = nullptr;
+    s3r_frame_desc desc{};
+    uint32_t nblocks = 0, level = 0, fmt = 0;
+    uint32_t tile_log2 = 4;
+    uint32_t render_tile = 0;
+    std::vector<uint32_t> blocks;      // 4 per block
+    std::vector<uint64_t> node_off;    // nblocks+1
+    std::vector<uint16_t> n2i;         // host copy (re-binning by the autotuner)
+    std::vector<uint64_t> vertex_off;  // nblocks+1
+    uint64_t vertices = 0, nodes = 0, tiles = 0, entries = 0;
+    // device
+    PlanBlock* blocks_dev = nullptr;
+    uint2* items_dev = nullptr;
+    uint64_t* entry_off_dev = nullptr;
+    uint16_t* entry_local_dev = nullptr;
+    uint32_t* entry_node_dev = nullptr;
+    int32_t* coarse_dev = nullptr;
+    uint64_t* node_off_dev = nullptr;
+    float2* scale_offset_dev = nullptr;
+    void* bricks = nullptr;
+    RenderBlock* table_dev = nullptr;
+    s3r_view* view_dev = nullptr;
+    uint32_t grid_ctas = 0;
+    // host render table (rects depend on the view)
+    std::vector<RenderBlock> table_host;
+    RenderBlock* table_pinned = nullptr;
+    s3r_view* view_pinned = nullptr;
+    cudaEvent_t staged = nullptr;
+    bool have_view = false;
+    s3r_view last_view{};
+    // graph of s3r_frame_run
+    cudaGraphExec_t exec = nullptr;
+    const void* g_key[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    uint32_t graph_kernels = 0;
+};
+
+namespace {
+
+int fail(s3r_ctx* ctx, int code, const std::string& msg)
+{
+    g_last_error = msg;
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+int cuda_fail(s3r_ctx* ctx, cudaError_t e, const char* what)
+{
+    return fail(ctx, S3R_ERR_CUDA, std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")");
+}
+
+#define S3R_CUDA(ctx, call)                                   \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+int set_device(s3r_ctx* ctx)
+{
+    int cur = -1;
+    cudaError_t e = cudaGetDevice(&cur);
+    if (e == cudaSuccess && cur == ctx->device) return S3R_OK;
+    e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaSetDevice");
+    return S3R_OK;
+}
+
+// ---------------------------------------------------------------- geometry
+
+void block_cube_f(uint32_t level, const uint32_t idx[3], float c[3], float& h)
+{
+    const float top = 5.f;
+    h = top / (float)(1u << level);
+    for (int d = 0; d < 3; ++d)
+        c[d] = -top + h * (float)(1u + (idx[d] << 1));
+}
+
+int clampi(int x, int lo, int hi) { return x < lo ? lo : (x > hi ? hi : x); }
+
+// DenseFieldRenderer_cu.cu:374-409: bounding box of the projected cube corners,
+// truncated toward zero, clamped to the viewport; {x, y, w, h} with w = max - min.
+void view_rect(const s3r_view& v, const uint32_t idx[3], int32_t rect[4])
+{
+    float c[3], h;
+    block_cube_f(v.level, idx, c, h);
+    const float lcam = 0.01f * 2 * 5.f;
+    const float pixel = v.cam.h / (float)v.H;
+    const float* r = v.cam.view_r;
+    const float* t = v.cam.view_t;
+    bool have = false, full = false;
+    int xmin = 0, xmax = 0, ymin = 0, ymax = 0;
+    for (int i = 0; i < 8; ++i) {
+        float p[3];
+        for (int d = 0; d < 3; ++d)
+            p[d] = c[d] + (float)((int)(((i >> d) & 1) << 1) - 1) * h;
+        float q[3];
+        for (int a = 0; a < 3; ++a)
+            q[a] = r[3 * a] * p[0] + r[3 * a + 1] * p[1] + r[3 * a + 2] * p[2] + t[a];
+        int sx, sy;
+        if (v.cam.ortho) {
+            sx = clampi((int)(q[0] / pixel) + (int)(v.W >> 1), 0, (int)v.W - 1);
+            sy = clampi((int)(q[1] / pixel) + (int)(v.H >> 1), 0, (int)v.H - 1);
+        } else {
+            if (q[2] >= 0) {
+                full = true;
+                break;
+            }
+            sx = clampi((int)(-q[0] / q[2] * lcam / pixel) + (int)(v.W >> 1), 0, (int)v.W - 1);
+            sy = clampi((int)(-q[1] / q[2] * lcam / pixel) + (int)(v.H >> 1), 0, (int)v.H - 1);
+        }
+        if (!have) {
+            xmin = xmax = sx;
+            ymin = ymax = sy;
+            have = true;
+        } else {
+            xmin = std::min(xmin, sx);
+            xmax = std::max(xmax, sx);
+            ymin = std::min(ymin, sy);
+            ymax = std::max(ymax, sy);
+        }
+    }
+    if (full) {
+        // a corner behind the eye: the whole viewport (bb << {0,0} << viewportSize)
+        xmin = ymin = 0;
+        xmax = (int)v.W;
+        ymax = (int)v.H;
+    }
+    rect[0] = xmin;
+    rect[1] = ymin;
+    rect[2] = xmax - xmin;
+    rect[3] = ymax - ymin;
+}
+
+int check_view(s3r_ctx* ctx, const s3r_view* v)
+{
+    if (!v) return fail(ctx, S3R_ERR_INVALID, "view is null");
+    if (v->W == 0 || v->H == 0 || v->W > 32768 || v->H > 32768)
+        return fail(ctx, S3R_ERR_INVALID, "viewport size out of range");
+    if (v->tf_n < 2 || v->tf_n > 4096) return fail(ctx, S3R_ERR_INVALID, "tf_n must be in [2, 4096]");
+    if (v->level > 12) return fail(ctx, S3R_ERR_INVALID, "level out of range");
+    if (!(v->field_max > v->field_min)) return fail(ctx, S3R_ERR_INVALID, "field range is empty");
+    if (!(v->quality > 0.f)) return fail(ctx, S3R_ERR_INVALID, "quality must be positive");
+    return S3R_OK;
+}
+
+// ---------------------------------------------------------------- ordering
+
+// Split of one index range by one eye coordinate (UniformIndexRangeSplitter,
+// include/UniformIndexRangeSplitter.hpp:27-57), in the reference's float type.
+struct Split {
+    uint32_t before[2];
+    uint32_t at; // ~0u: none
+    uint32_t after[2];
+};
+
+Split split_range(uint32_t lo, uint32_t hi, float c0, float c1, float x)
+{
+    Split s;
+    if (x <= c0) {
+        s.before[0] = s.before[1] = 0;
+        s.at = ~0u;
+        s.after[0] = lo;
+        s.after[1] = hi;
+        return s;
+    }
+    if (x >= c1) {
+        s.before[0] = lo;
+        s.before[1] = hi;
+        s.at = ~0u;
+        s.after[0] = s.after[1] = 0;
+        return s;
+    }
+    const float factor = (float)(hi - lo) / (c1 - c0);
+    const uint32_t at = (uint32_t)((x - c0) * factor) + lo;
+    s.before[0] = lo;
+    s.before[1] = at;
+    s.at = at;
+    s.after[0] = at + 1;
+    s.after[1] = hi;
+    return s;
+}
+
+// Macro-block visiting order: the 27 cells of the 3x3x3 split (0 = before the
+// eye, 1 = at it, 2 = beyond it per axis) taken corners first, then edges,
+// faces and the eye's own cell (include/BackToFrontOrder.hpp:182-209).
+constexpr uint8_t kMacroOrder[27] = {0, 2, 6, 8, 18, 20, 24, 26, 1, 3, 5, 7, 9, 11,
+                                     15, 17, 19, 21, 23, 25, 4, 10, 12, 14, 16, 22, 13};
+
+// Inside one macro block: anti-diagonal sweeps of increasing coordinate sum,
+// the same successor rule as include/BackToFrontOrder.hpp:246-307 (unsigned
+// arithmetic kept), mirrored on axes beyond the eye.
+bool next_in_box(uint32_t p[3], const uint32_t mn[3], const uint32_t mx[3])
+{
+    uint32_t s = p[0] + p[1] + p[2];
+    if (s + 3 == mx[0] + mx[1] + mx[2]) return false;
+    if (p[0] > mn[0] && p[1] + 1 < mx[1]) {
+        --p[0];
+        ++p[1];
+    } else if (p[0] + p[1] > mn[0] + mn[1] && p[2] + 1 < mx[2]) {
+        if (s - mn[1] - p[2] < mx[0] + 1) {
+            p[0] = s - mn[1] - p[2] - 1;
+            p[1] = mn[1];
+            p[2] = p[2] + 1;
+        } else {
+            p[0] = mx[0] - 1;
+            p[1] = s - mx[0] - p[2];
+            p[2] = p[2] + 1;
+        }
+    } else {
+        ++s;
+        const uint32_t x0 = s - mn[1] - mn[2];
+        if (x0 < mx[0]) {
+            p[0] = x0;
+            p[1] = mn[1];
+            p[2] = mn[2];
+        } else {
+            const uint32_t x1 = s - mx[0] + 1 - mn[2];
+            if (x1 < mx[1]) {
+                p[0] = mx[0] - 1;
+                p[1] = x1;
+                p[2] = mn[2];
+            } else {
+                p[0] = mx[0] - 1;
+                p[1] = mx[1] - 1;
+                p[2] = s + 2 - mx[0] - mx[1];
+            }
+        }
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------- plan
+
+void plan_free_device(s3r_plan* p)
+{
+    auto f = [](void* q) {
+        if (q) cudaFree(q);
+    };
+    f(p->blocks_dev);
+    f(p->items_dev);
+    f(p->entry_off_dev);
+    f(p->entry_local_dev);
+    f(p->entry_node_dev);
+    f(p->coarse_dev);
+    p->blocks_dev = nullptr;
+    p->items_dev = nullptr;
+    p->entry_off_dev = nullptr;
+    p->entry_local_dev = nullptr;
+    p->entry_node_dev = nullptr;
+    p->coarse_dev = nullptr;
+}
+
+void plan_drop_graph(s3r_plan* p)
+{
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    p->exec = nullptr;
+    for (auto& k : p->g_key) k = nullptr;
+}
+
+template <class T> int upload(s3r_ctx* ctx, T** dst, const std::vector<T>& src)
+{
+    const size_t bytes = std::max<size_t>(src.size(), 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(dst, bytes);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(plan)");
+    if (!src.empty()) {
+        e = cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMemcpy(plan)");
+    }
+    return S3R_OK;
+}
+
+// Bins every block's nodes by tile of 2^tile_log2 cells (closed tiles: nodes on
+// shared faces, edges and corners go to every tile containing them; lattice
+// points of the tile grid are left to the coarse descent), builds the coarse
+// index grids and the work-item list (largest tiles first), and uploads them.
+int plan_bin(s3r_plan* p, uint32_t tile_log2)
+{
+    s3r_ctx* ctx = p->ctx;
+    const uint32_t nb = p->nblocks;
+    std::vector<PlanBlock> pb(nb);
+    std::vector<uint64_t> tiles_off(nb + 1, 0), coarse_off(nb + 1, 0);
+    for (uint32_t b = 0; b < nb; ++b) {
+        const uint32_t d = p->blocks[4 * b + 3];
+        const uint32_t k = std::min(tile_log2, d);
+        const uint32_t L = d - k;
+        pb[b].depth = d;
+        pb[b].tile_log2 = k;
+        pb[b].coarse_log2 = L;
+        pb[b].node_base = p->node_off[b];
+        pb[b].dense_off = p->vertex_off[b];
+        const uint64_t m = 1ull << L;
+        tiles_off[b + 1] = tiles_off[b] + m * m * m;
+        coarse_off[b + 1] = coarse_off[b] + (m + 1) * (m + 1) * (m + 1);
+    }
+    if (coarse_off[nb] > 0xffffffffull) return fail(ctx, S3R_ERR_INVALID, "coarse grids too large");
+    for (uint32_t b = 0; b < nb; ++b) pb[b].coarse_off = (uint32_t)coarse_off[b];
+    const uint64_t ntiles = tiles_off[nb];
+    std::vector<int32_t> coarse(coarse_off[nb], -1);
+    std::vector<uint64_t> count(ntiles + 1, 0);
+
+    const unsigned nthreads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    auto parallel = [&](auto&& fn) {
+        std::vector<std::thread> th;
+        for (unsigned t = 0; t < nthreads; ++t)
+            th.emplace_back([&, t] {
+                for (uint32_t b = t; b < nb; b += nthreads) fn(b);
+            });
+        for (auto& x : th) x.join();
+    };
+    auto tile_span = [](uint32_t x, uint32_t T, uint32_t m, uint32_t& lo, uint32_t& hi) {
+        lo = x == 0 ? 0 : (x - 1) / T;
+        hi = std::min(x / T, m - 1);
+    };
+    // pass 1: counts and coarse grids
+    parallel([&](uint32_t b) {
+        const PlanBlock& B = pb[b];
+        const uint32_t T = 1u << B.tile_log2, m = 1u << B.coarse_log2, m1 = m + 1;
+        for (uint64_t i = p->node_off[b]; i < p->node_off[b + 1]; ++i) {
+            const uint32_t x = p->n2i[3 * i], y = p->n2i[3 * i + 1], z = p->n2i[3 * i + 2];
+            const bool lattice = (x % T == 0) && (y % T == 0) && (z % T == 0);
+            if (lattice) coarse[B.coarse_off + (x / T) + m1 * ((y / T) + m1 * (z / T))] = (int32_t)(i - p->node_off[b]);
+            if (lattice && B.coarse_log2 > 0) continue;
+            uint32_t xl, xh, yl, yh, zl, zh;
+            tile_span(x, T, m, xl, xh);
+            tile_span(y, T, m, yl, yh);
+            tile_span(z, T, m, zl, zh);
+            for (uint32_t tz = zl; tz <= zh; ++tz)
+                for (uint32_t ty = yl; ty <= yh; ++ty)
+                    for (uint32_t tx = xl; tx <= xh; ++tx)
+                        ++count[tiles_off[b] + tx + m * (ty + m * tz)];
+        }
+    });
+    // items: largest tiles first, then block order
+    std::vector<uint64_t> order(ntiles);
+    {
+        std::vector<uint32_t> bord(nb);
+        for (uint32_t b = 0; b < nb; ++b) bord[b] = b;
+        std::stable_sort(bord.begin(), bord.end(),
+                         [&](uint32_t a, uint32_t c) { return pb[a].tile_log2 > pb[c].tile_log2; });
+        uint64_t o = 0;
+        for (uint32_t b : bord)
+            for (uint64_t t = tiles_off[b]; t < tiles_off[b + 1]; ++t) order[o++] = t;
+    }
+    std::vector<uint2> items(ntiles);
+    std::vector<uint64_t> entry_off(ntiles + 1, 0);
+    std::vector<uint64_t> slot(ntiles); // tile (block-major) -> item position
+    std::vector<uint32_t> tile_block(ntiles);
+    for (uint32_t b = 0; b < nb; ++b)
+        for (uint64_t t = tiles_off[b]; t < tiles_off[b + 1]; ++t) tile_block[t] = b;
+    for (uint64_t it = 0; it < ntiles; ++it) {
+        const uint64_t t = order[it];
+        slot[t] = it;
+        const uint32_t b = tile_block[t];
+        items[it] = make_uint2(b, (uint32_t)(t - tiles_off[b]));
+        entry_off[it + 1] = entry_off[it] + count[t];
+    }
+    const uint64_t nentries = entry_off[ntiles];
+    std::vector<uint16_t> local(nentries);
+    std::vector<uint32_t> node(nentries);
+    std::vector<uint64_t> cursor(ntiles);
+    for (uint64_t t = 0; t < ntiles; ++t) cursor[t] = entry_off[slot[t]];
+    // pass 2: fill (tiles of one block are only touched by that block's thread)
+    parallel([&](uint32_t b) {
+        const PlanBlock& B = pb[b];
+        const uint32_t T = 1u << B.tile_log2, m = 1u << B.coarse_log2, E = T + 1;
+        for (uint64_t i = p->node_off[b]; i < p->node_off[b + 1]; ++i) {
+            const uint32_t x = p->n2i[3 * i], y = p->n2i[3 * i + 1], z = p->n2i[3 * i + 2];
+            const bool lattice = (x % T == 0) && (y % T == 0) && (z % T == 0);
+            if (lattice && B.coarse_log2 > 0) continue;
+            uint32_t xl, xh, yl, yh, zl, zh;
+            tile_span(x, T, m, xl, xh);
+            tile_span(y, T, m, yl, yh);
+            tile_span(z, T, m, zl, zh);
+            for (uint32_t tz = zl; tz <= zh; ++tz)
+                for (uint32_t ty = yl; ty <= yh; ++ty)
+                    for (uint32_t tx = xl; tx <= xh; ++tx) {
+                        const uint64_t t = tiles_off[b] + tx + m * (ty + m * tz);
+                        const uint64_t e = cursor[t]++;
+                        local[e] = (uint16_t)((x - tx * T) + E * ((y - ty * T) + E * (z - tz * T)));
+                        node[e] = (uint32_t)(i - p->node_off[b]);
+                    }
+        }
+    });
+    plan_free_device(p);
+    int rc;
+    if ((rc = upload(ctx, &p->blocks_dev, pb))) return rc;
+    if ((rc = upload(ctx, &p->items_dev, items))) return rc;
+    if ((rc = upload(ctx, &p->entry_off_dev, entry_off))) return rc;
+    if ((rc = upload(ctx, &p->entry_local_dev, local))) return rc;
+    if ((rc = upload(ctx, &p->entry_node_dev, node))) return rc;
+    if ((rc = upload(ctx, &p->coarse_dev, coarse))) return rc;
+    p->tile_log2 = tile_log2;
+    p->tiles = ntiles;
+    p->entries = nentries;
+    // persistent grid: resident CTAs on every SM
+    const uint32_t E = (1u << tile_log2) + 1u;
+    const size_t smem = (size_t)E * E * E * sizeof(float);
+    const uint32_t per_sm = std::max<uint32_t>(1, std::min<uint32_t>(8, (uint32_t)((227u * 1024u) / (smem + 1024))));
+    p->grid_ctas = (uint32_t)std::min<uint64_t>(ntiles, (uint64_t)ctx->sms * per_sm);
+    plan_drop_graph(p);
+    return S3R_OK;
+}
+
+int plan_stage_view(s3r_plan* p, const s3r_view* view, cudaStream_t s)
+{
+    s3r_ctx* ctx = p->ctx;
+    const bool same = p->have_view && std::memcmp(&p->last_view, view, sizeof(s3r_view)) == 0;
+    if (same) return S3R_OK;
+    // the staging buffers may still feed an earlier copy
+    S3R_CUDA(ctx, cudaEventSynchronize(p->staged));
+    const uint32_t m = 1u << p->level;
+    RenderBlock* tb = p->table_pinned;
+    std::memcpy(tb, p->table_host.data(), sizeof(RenderBlock) * p->table_host.size());
+    for (uint32_t b = 0; b < p->nblocks; ++b) {
+        const uint32_t* bl = &p->blocks[4 * b];
+        const uint32_t cell = bl[0] + m * (bl[1] + m * bl[2]);
+        view_rect(*view, bl, tb[cell].rect);
+    }
+    *p->view_pinned = *view;
+    S3R_CUDA(ctx, cudaMemcpyAsync(p->table_dev, tb, sizeof(RenderBlock) * p->table_host.size(),
+                                  cudaMemcpyHostToDevice, s));
+    S3R_CUDA(ctx, cudaMemcpyAsync(p->view_dev, p->view_pinned, sizeof(s3r_view), cudaMemcpyHostToDevice, s));
+    S3R_CUDA(ctx, cudaEventRecord(p->staged, s));
+    p->last_view = *view;
+    p->have_view = true;
+    return S3R_OK;
+}
+
+int plan_launch_interp(s3r_plan* p, const float* sparse, cudaStream_t s, uint32_t* kernels)
+{
+    s3r_ctx* ctx = p->ctx;
+    if (p->fmt != S3R_BRICK_F32) {
+        S3R_CUDA(ctx, launch_block_ranges(p->blocks_dev, p->nblocks, sparse, p->node_off_dev, p->scale_offset_dev, s));
+        ++*kernels;
+    }
+    TileArgs a{};
+    a.blocks = p->blocks_dev;
+    a.items = p->items_dev;
+    a.nitems = (uint32_t)p->tiles;
+    a.entry_off = p->entry_off_dev;
+    a.entry_local = p->entry_local_dev;
+    a.entry_node = p->entry_node_dev;
+    a.coarse_idx = p->coarse_dev;
+    a.sparse = sparse;
+    a.scale_offset = p->fmt == S3R_BRICK_F32 ? nullptr : p->scale_offset_dev;
+    a.out = p->bricks;
+    S3R_CUDA(ctx, launch_interp_plan(a, p->fmt, p->tile_log2, p->grid_ctas, s));
+    ++*kernels;
+    return S3R_OK;
+}
+
+int plan_launch_render(s3r_plan* p, const float* tf, float* rgba, uint32_t* argb, unsigned long long* samples,
+                       cudaStream_t s, uint32_t* kernels)
+{
+    FrameArgs fa{};
+    fa.view = p->view_dev;
+    fa.table = p->table_dev;
+    fa.bricks = p->bricks;
+    fa.tf = tf;
+    fa.rgba = rgba;
+    fa.argb = argb;
+    fa.samples = samples;
+    fa.scale_offset = p->fmt == S3R_BRICK_F32 ? nullptr : p->scale_offset_dev;
+    S3R_CUDA(p->ctx, launch_frame_render(fa, p->last_view.W, p->last_view.H, p->last_view.tf_n, p->fmt,
+                                         p->render_tile, s));
+    ++*kernels;
+    return S3R_OK;
+}
+
+} // namespace
+
+// ==================================================================== C ABI
+
+extern "C" {
+
+int s3r_abi_version(void) { return S3R_ABI_VERSION; }
+
+const char* s3r_last_error(const s3r_ctx* ctx) { return ctx ? ctx->err.c_str() : g_last_error.c_str(); }
+
+uint64_t s3r_ctx_launch_count(const s3r_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int s3r_ctx_create(int device, s3r_ctx** out)
+{
+    if (!out) return fail(nullptr, S3R_ERR_INVALID, "out is null");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaGetDeviceCount");
+    if (device < 0 || device >= n) return fail(nullptr, S3R_ERR_INVALID, "no such device");
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "cudaSetDevice");
+    s3r_ctx* c = new (std::nothrow) s3r_ctx;
+    if (!c) return fail(nullptr, S3R_ERR_NOMEM, "out of host memory");
+    c->device = device;
+    cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
+    if ((e = cudaMalloc(&c->rect_dev, 4 * sizeof(int32_t))) != cudaSuccess ||
+        (e = cudaMallocHost(&c->rect_host, 4 * sizeof(int32_t))) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&c->capture, cudaStreamNonBlocking)) != cudaSuccess) {
+        s3r_ctx_destroy(c);
+        return cuda_fail(nullptr, e, "context allocation");
+    }
+    *out = c;
+    return S3R_OK;
+}
+
+int s3r_ctx_destroy(s3r_ctx* ctx)
+{
+    if (!ctx) return S3R_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->grid) cudaFree(ctx->grid);
+    if (ctx->rect_dev) cudaFree(ctx->rect_dev);
+    if (ctx->rect_host) cudaFreeHost(ctx->rect_host);
+    if (ctx->parts_dev) cudaFree(ctx->parts_dev);
+    if (ctx->capture) cudaStreamDestroy(ctx->capture);
+    delete ctx;
+    return S3R_OK;
+}
+
+int s3r_interp_dense(s3r_ctx* ctx, const uint16_t* n2i_xyz, const float* sparse, uint32_t n, uint32_t depth,
+                     float* dense, void* stream)
+{
+    if (!ctx) return fail(nullptr, S3R_ERR_INVALID, "ctx is null");
+    if (depth > S3R_MAX_DEPTH) return fail(ctx, S3R_ERR_INVALID, "depth exceeds S3R_MAX_DEPTH");
+    if (!dense || (n > 0 && (!n2i_xyz || !sparse))) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    int rc = set_device(ctx);
+    if (rc) return rc;
+    const uint64_t e = (1ull << depth) + 1ull;
+    const uint64_t count = e * e * e;
+    if (ctx->grid_cap < count) {
+        if (ctx->grid) cudaFree(ctx->grid);
+        ctx->grid = nullptr;
+        ctx->grid_cap = 0;
+        S3R_CUDA(ctx, cudaMalloc(&ctx->grid, count * sizeof(float)));
+        ctx->grid_cap = count;
+    }
+    cudaStream_t s = as_stream(stream);
+    S3R_CUDA(ctx, launch_fill_f32(ctx->grid, count, __builtin_nanf(""), s));
+    S3R_CUDA(ctx, launch_scatter_nodes(ctx->grid, depth, n2i_xyz, sparse, n, s));
+    uint32_t launches = 0;
+    S3R_CUDA(ctx, launch_interp_grid(ctx->grid, depth, dense, s, &launches));
+    ctx->launches += 1 + (n > 0 ? 1 : 0) + launches;
+    return S3R_OK;
+}
+
+int s3r_camera_look_at(const double eye[3], const double center[3], const double up[3], double fovy_deg, uint32_t W,
+                       uint32_t H, int32_t ortho, double ortho_height, s3r_camera* out)
+{
+    if (!eye || !center || !up || !out || W == 0 || H == 0) return fail(nullptr, S3R_ERR_INVALID, "bad argument");
+    double z[3] = {eye[0] - center[0], eye[1] - center[1], eye[2] - center[2]};
+    double zl = std::sqrt(z[0] * z[0] + z[1] * z[1] + z[2] * z[2]);
+    if (!(zl > 0)) return fail(nullptr, S3R_ERR_INVALID, "eye equals center");
+    for (double& c : z) c /= zl;
+    double x[3] = {up[1] * z[2] - up[2] * z[1], up[2] * z[0] - up[0] * z[2], up[0] * z[1] - up[1] * z[0]};
+    double xl = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+    if (!(xl > 0)) return fail(nullptr, S3R_ERR_INVALID, "up is parallel to the view direction");
+    for (double& c : x) c /= xl;
+    double y[3] = {z[1] * x[2] - z[2] * x[1], z[2] * x[0] - z[0] * x[2], z[0] * x[1] - z[1] * x[0]};
+    const float lcam = 0.01f * 2 * 5.f;
+    std::memset(out, 0, sizeof(*out));
+    for (int d = 0; d < 3; ++d) {
+        out->eye[d] = (float)eye[d];
+        out->e1[d] = (float)x[d];
+        out->e2[d] = (float)y[d];
+        out->n[d] = (float)z[d] * (-lcam);
+        out->view_r[d] = (float)x[d];
+        out->view_r[3 + d] = (float)y[d];
+        out->view_r[6 + d] = (float)z[d];
+    }
+    const double* rows[3] = {x, y, z};
+    for (int a = 0; a < 3; ++a)
+        out->view_t[a] = (float)-(rows[a][0] * eye[0] + rows[a][1] * eye[1] + rows[a][2] * eye[2]);
+    out->ortho = ortho ? 1 : 0;
+    if (ortho) {
+        out->h = (float)ortho_height;
+    } else {
+        out->h = (float)(2 * lcam * std::tan(0.5 * fovy_deg * M_PI / 180));
+    }
+    const float pixel = out->h / (float)H;
+    out->w = pixel * (float)W;
+    return S3R_OK;
+}
+
+int s3r_block_cube(uint32_t level, const uint32_t idx[3], float center[3], float* half_size)
+{
+    if (!idx || !center || !half_size || level > 12) return fail(nullptr, S3R_ERR_INVALID, "bad argument");
+    block_cube_f(level, idx, center, *half_size);
+    return S3R_OK;
+}
+
+int s3r_block_view_rect(const s3r_view* view, const uint32_t idx[3], int32_t rect[4])
+{
+    if (!idx || !rect) return fail(nullptr, S3R_ERR_INVALID, "bad argument");
+    int rc = check_view(nullptr, view);
+    if (rc) return rc;
+    view_rect(*view, idx, rect);
+    return S3R_OK;
+}
+
+int s3r_clear_viewport(s3r_ctx* ctx, uint32_t* viewport, uint32_t W, uint32_t H, uint32_t value, void* stream)
+{
+    if (!ctx || !viewport) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    int rc = set_device(ctx);
+    if (rc) return rc;
+    S3R_CUDA(ctx, launch_fill_u32(viewport, (uint64_t)W * H, value, as_stream(stream)));
+    ++ctx->launches;
+    return S3R_OK;
+}
+
+int s3r_render_block_argb(s3r_ctx* ctx, const s3r_view* view, const float* brick, uint32_t depth,
+                          const uint32_t idx[3], const int32_t rect[4], const float* tf, uint32_t* viewport,
+                          void* stream)
+{
+    if (!ctx) return fail(nullptr, S3R_ERR_INVALID, "ctx is null");
+    int rc = check_view(ctx, view);
+    if (rc) return rc;
+    if (!brick || !idx || !rect || !tf || !viewport) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (depth > S3R_MAX_DEPTH) return fail(ctx, S3R_ERR_INVALID, "depth exceeds S3R_MAX_DEPTH");
+    const uint32_t m = 1u << view->level;
+    if (idx[0] >= m || idx[1] >= m || idx[2] >= m) return fail(ctx, S3R_ERR_INVALID, "block index outside level");
+    if (rect[2] < 0 || rect[3] < 0) return fail(ctx, S3R_ERR_INVALID, "negative view rectangle");
+    if ((rc = set_device(ctx))) return rc;
+    float c[3], h;
+    block_cube_f(view->level, idx, c, h);
+    S3R_CUDA(ctx, launch_render_block_argb(view, brick, depth, c, h, rect, view->W, view->H, tf, view->tf_n, viewport,
+                                           as_stream(stream)));
+    if (rect[2] > 0 && rect[3] > 0) ++ctx->launches;
+    return S3R_OK;
+}
+
+int s3r_index_box_world(uint32_t level, const uint32_t bmin[3], const uint32_t bmax[3], double cmin[3], double cmax[3])
+{
+    if (!bmin || !bmax || !cmin || !cmax || level > 12) return fail(nullptr, S3R_ERR_INVALID, "bad argument");
+    // s3vs::boundingBoxOfIndexBox (src/s3vs_worker/BlockOrderUtil.hpp:29-52), float arithmetic
+    const float top = 5.f;
+    const float h = top / (float)(1u << level);
+    for (int d = 0; d < 3; ++d) {
+        if (bmax[d] <= bmin[d]) return fail(nullptr, S3R_ERR_INVALID, "empty index box");
+        const float c0 = -top + h * (float)(1u + (bmin[d] << 1));
+        const float c1 = -top + h * (float)(1u + ((bmax[d] - 1) << 1));
+        cmin[d] = (double)c0 - (double)h;
+        cmax[d] = (double)c1 + (double)h;
+    }
+    return S3R_OK;
+}
+
+int s3r_b2f_order(const uint32_t bmin[3], const uint32_t bmax[3], const double cmin[3], const double cmax[3],
+                  const double eye[3], uint32_t* out, uint32_t capacity, uint32_t* count)
+{
+    if (!bmin || !bmax || !cmin || !cmax || !eye || !count || (capacity && !out))
+        return fail(nullptr, S3R_ERR_INVALID, "bad argument");
+    Split sp[3];
+    for (int a = 0; a < 3; ++a) {
+        if (bmax[a] <= bmin[a] || !((float)cmax[a] > (float)cmin[a]))
+            return fail(nullptr, S3R_ERR_INVALID, "index box or world box is empty");
+        sp[a] = split_range(bmin[a], bmax[a], (float)cmin[a], (float)cmax[a], (float)eye[a]);
+    }
+    uint32_t n = 0;
+    for (uint8_t ord : kMacroOrder) {
+        const uint32_t mp[3] = {ord % 3u, (ord / 3u) % 3u, ord / 9u};
+        uint32_t mn[3], mx[3];
+        bool valid = true;
+        for (int a = 0; a < 3; ++a) {
+            const Split& s = sp[a];
+            if (mp[a] == 0) {
+                mn[a] = s.before[0];
+                mx[a] = s.before[1];
+                valid &= s.before[0] != s.before[1];
+            } else if (mp[a] == 1) {
+                mn[a] = s.at;
+                mx[a] = s.at + 1;
+                valid &= s.at != ~0u;
+            } else {
+                mn[a] = s.after[0];
+                mx[a] = s.after[1];
+                valid &= s.after[0] != s.after[1];
+            }
+        }
+        if (!valid) continue;
+        uint32_t p[3] = {mn[0], mn[1], mn[2]};
+        do {
+            if (n < capacity)
+                for (int a = 0; a < 3; ++a) out[3 * n + a] = mp[a] == 2 ? mx[a] - 1 + mn[a] - p[a] : p[a];
+            ++n;
+        } while (next_in_box(p, mn, mx));
+    }
+    *count = n;
+    return S3R_OK;
+}
+
+int s3r_bound_rect(s3r_ctx* ctx, const uint32_t* viewport, uint32_t W, uint32_t H, int32_t rect[4], void* stream)
+{
+    if (!ctx || !viewport || !rect) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    int rc = set_device(ctx);
+    if (rc) return rc;
+    cudaStream_t s = as_stream(stream);
+    int32_t init[4] = {(int32_t)W, (int32_t)H, -1, -1};
+    std::memcpy(ctx->rect_host, init, sizeof(init));
+    S3R_CUDA(ctx, cudaMemcpyAsync(ctx->rect_dev, ctx->rect_host, sizeof(init), cudaMemcpyHostToDevice, s));
+    S3R_CUDA(ctx, launch_bound_rect(viewport, W, H, ctx->rect_dev, s));
+    ++ctx->launches;
+    S3R_CUDA(ctx, cudaMemcpyAsync(ctx->rect_host, ctx->rect_dev, sizeof(init), cudaMemcpyDeviceToHost, s));
+    S3R_CUDA(ctx, cudaStreamSynchronize(s));
+    const int32_t* r = ctx->rect_host;
+    if (r[2] < r[0] || r[3] < r[1]) {
+        rect[0] = rect[1] = rect[2] = rect[3] = 0;
+    } else {
+        rect[0] = r[0];
+        rect[1] = r[1];
+        rect[2] = r[2] - r[0] + 1;
+        rect[3] = r[3] - r[1] + 1;
+    }
+    return S3R_OK;
+}
+
+int s3r_crop(s3r_ctx* ctx, const uint32_t* image, uint32_t W, const int32_t rect[4], uint32_t* dst, void* stream)
+{
+    if (!ctx || !image || !rect || !dst) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (rect[0] < 0 || rect[1] < 0 || rect[2] < 0 || rect[3] < 0 || (uint32_t)(rect[0] + rect[2]) > W)
+        return fail(ctx, S3R_ERR_INVALID, "crop rectangle outside the image");
+    int rc = set_device(ctx);
+    if (rc) return rc;
+    S3R_CUDA(ctx, launch_crop(image, W, rect, dst, as_stream(stream)));
+    if (rect[2] > 0 && rect[3] > 0) ++ctx->launches;
+    return S3R_OK;
+}
+
+int s3r_blend_image_part_host(uint32_t* dst, int32_t dw, int32_t dh, const uint32_t* src, int32_t sw, int32_t sh,
+                              int32_t ox, int32_t oy, int32_t just_copy, int32_t offx, int32_t offy)
+{
+    if (!dst || (!src && sw * sh > 0)) return fail(nullptr, S3R_ERR_INVALID, "null pointer");
+    const int32_t dx = ox - offx, dy = oy - offy;
+    if (dx < 0 || dy < 0 || dx + sw > dw || dy + sh > dh)
+        return fail(nullptr, S3R_ERR_INVALID, "image part does not fit the destination");
+    for (int32_t y = 0; y < sh; ++y) {
+        const uint32_t* srow = src + (size_t)y * sw;
+        uint32_t* drow = dst + (size_t)dw * (dy + y) + dx;
+        if (just_copy) {
+            std::memcpy(drow, srow, sizeof(uint32_t) * sw);
+            continue;
+        }
+        for (int32_t i = 0; i < sw; ++i) {
+            const uint32_t s = srow[i], as = s >> 24;
+            if (as == 0) continue;
+            const uint32_t d = drow[i], ad = d >> 24;
+            if (as == 255u || ad == 0) {
+                drow[i] = s;
+                continue;
+            }
+            const uint32_t a = as + ad * (255u - as) / 255u;
+            uint32_t o = (a & 0xffu) << 24;
+            for (int b = 0; b < 3; ++b) {
+                const uint32_t cs = (s >> (8 * b)) & 0xffu, cd = (d >> (8 * b)) & 0xffu;
+                o |= (((cs * as + cd * (a - as)) / a) & 0xffu) << (8 * b);
+            }
+            drow[i] = o;
+        }
+    }
+    return S3R_OK;
+}
+
+int s3r_compose_parts(s3r_ctx* ctx, const s3r_image_part* parts, uint32_t nparts, int32_t just_copy_first,
+                      uint32_t* dst, int32_t dw, int32_t dh, int32_t offx, int32_t offy, void* stream)
+{
+    if (!ctx || !dst || (nparts && !parts)) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    int rc = set_device(ctx);
+    if (rc) return rc;
+    if (nparts == 0) return S3R_OK;
+    if (ctx->parts_cap < nparts) {
+        if (ctx->parts_dev) cudaFree(ctx->parts_dev);
+        ctx->parts_dev = nullptr;
+        ctx->parts_cap = 0;
+        S3R_CUDA(ctx, cudaMalloc(&ctx->parts_dev, sizeof(s3r_image_part) * nparts));
+        ctx->parts_cap = nparts;
+    }
+    cudaStream_t s = as_stream(stream);
+    S3R_CUDA(ctx, cudaMemcpyAsync(ctx->parts_dev, parts, sizeof(s3r_image_part) * nparts, cudaMemcpyHostToDevice, s));
+    S3R_CUDA(ctx, launch_compose(ctx->parts_dev, nparts, just_copy_first, dst, dw, dh, offx, offy, s));
+    // the parts array is pageable host memory copied asynchronously: finish before returning
+    S3R_CUDA(ctx, cudaStreamSynchronize(s));
+    ++ctx->launches;
+    return S3R_OK;
+}
+
+int s3r_make_color_transfer(const double* xs, const double* rgba, uint32_t npoints, uint32_t color_count, float* out)
+{
+    if (!out || color_count == 0 || (npoints && (!xs || !rgba))) return fail(nullptr, S3R_ERR_INVALID, "bad argument");
+    // makeColorTransferVector (include/s3vs/ColorTransferFunction.hpp:27-69); real_type is float
+    if (npoints == 0) {
+        for (uint32_t i = 0; i < 4 * color_count; ++i) out[i] = 1.f;
+        return S3R_OK;
+    }
+    if (npoints == 1) {
+        for (uint32_t i = 0; i < color_count; ++i)
+            for (int c = 0; c < 4; ++c) out[4 * i + c] = (float)rgba[c];
+        return S3R_OK;
+    }
+    for (uint32_t i = 1; i < npoints; ++i)
+        if (!((float)xs[i] > (float)xs[i - 1])) return fail(nullptr, S3R_ERR_INVALID, "control points not increasing");
+    std::fill(out, out + 4 * color_count, 0.f);
+    const float xmin = (float)xs[0], xmax = (float)xs[npoints - 1];
+    float c1[4];
+    for (int c = 0; c < 4; ++c) out[c] = c1[c] = (float)rgba[c];
+    uint32_t i1 = 0;
+    for (uint32_t ip = 1; ip < npoints; ++ip) {
+        float c2[4];
+        for (int c = 0; c < 4; ++c) c2[c] = (float)rgba[4 * ip + c];
+        const uint32_t i2 = ip + 1 == npoints ? color_count - 1u
+                                              : (uint32_t)(((float)xs[ip] - xmin) / (xmax - xmin) * (float)color_count);
+        for (uint32_t i = i1 + 1; i2 > i1 && i <= i2 && i < color_count; ++i) {
+            const float t = (float)(i - i1) / (float)(i2 - i1);
+            for (int c = 0; c < 4; ++c) out[4 * i + c] = c1[c] * (1 - t) + c2[c] * t;
+        }
+        for (int c = 0; c < 4; ++c) c1[c] = c2[c];
+        i1 = i2;
+    }
+    return S3R_OK;
+}
+
+// ------------------------------------------------------------------ plans
+
+int s3r_frame_plan(s3r_ctx* ctx, const s3r_frame_desc* desc, s3r_plan** out)
+{
+    if (!ctx || !desc || !out) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    *out = nullptr;
+    if (desc->level > 8) return fail(ctx, S3R_ERR_INVALID, "level out of range (max 8)");
+    if (desc->nblocks == 0 || !desc->blocks || !desc->node_off || (!desc->n2i && desc->node_off[desc->nblocks]))
+        return fail(ctx, S3R_ERR_INVALID, "empty or null block description");
+    if (desc->brick_format > S3R_BRICK_BF16) return fail(ctx, S3R_ERR_INVALID, "unknown brick format");
+    uint32_t tl = 4;
+    if (desc->tile_cells) {
+        if (desc->tile_cells == 8) tl = 3;
+        else if (desc->tile_cells == 16) tl = 4;
+        else if (desc->tile_cells == 32) tl = 5;
+        else return fail(ctx, S3R_ERR_INVALID, "tile_cells must be 0, 8, 16 or 32");
+    }
+    int rc = set_device(ctx);
+    if (rc) return rc;
+    const uint32_t m = 1u << desc->level;
+    auto p = new (std::nothrow) s3r_plan;
+    if (!p) return fail(ctx, S3R_ERR_NOMEM, "out of host memory");
+    p->ctx = ctx;
+    p->desc = *desc;
+    p->nblocks = desc->nblocks;
+    p->level = desc->level;
+    p->fmt = desc->brick_format;
+    p->render_tile = desc->render_tile % kRenderShapes;
+    p->blocks.assign(desc->blocks, desc->blocks + 4 * (size_t)desc->nblocks);
+    p->node_off.assign(desc->node_off, desc->node_off + desc->nblocks + 1);
+    p->nodes = p->node_off[desc->nblocks];
+    p->n2i.assign(desc->n2i, desc->n2i + 3 * p->nodes);
+    p->vertex_off.assign(desc->nblocks + 1, 0);
+    p->table_host.assign((size_t)m * m * m, RenderBlock{});
+    for (auto& t : p->table_host) {
+        t.depth = 0xffffffffu;
+        t.fmt = p->fmt;
+    }
+    auto bail = [&](int code) {
+        s3r_plan_destroy(p);
+        return code;
+    };
+    for (uint32_t b = 0; b < desc->nblocks; ++b) {
+        const uint32_t* bl = &p->blocks[4 * b];
+        if (bl[0] >= m || bl[1] >= m || bl[2] >= m)
+            return bail(fail(ctx, S3R_ERR_INVALID, "block index outside the level"));
+        if (bl[3] > S3R_MAX_DEPTH) return bail(fail(ctx, S3R_ERR_INVALID, "block depth exceeds S3R_MAX_DEPTH"));
+        if (p->node_off[b + 1] < p->node_off[b]) return bail(fail(ctx, S3R_ERR_INVALID, "node offsets decrease"));
+        if (p->node_off[b + 1] - p->node_off[b] > 0xffffffffull)
+            return bail(fail(ctx, S3R_ERR_INVALID, "too many nodes in one block"));
+        const uint64_t e = (1ull << bl[3]) + 1;
+        p->vertex_off[b + 1] = p->vertex_off[b] + e * e * e;
+        RenderBlock& t = p->table_host[bl[0] + m * (bl[1] + m * bl[2])];
+        if (t.depth != 0xffffffffu) return bail(fail(ctx, S3R_ERR_INVALID, "duplicate block index"));
+        t.depth = bl[3];
+        t.brick_off = p->vertex_off[b];
+        t.block = b;
+        const uint32_t lim = (uint32_t)(e - 1);
+        for (uint64_t i = p->node_off[b]; i < p->node_off[b + 1]; ++i)
+            if (p->n2i[3 * i] > lim || p->n2i[3 * i + 1] > lim || p->n2i[3 * i + 2] > lim)
+                return bail(fail(ctx, S3R_ERR_INVALID, "node index outside its block"));
+    }
+    p->vertices = p->vertex_off[desc->nblocks];
+    const size_t esz = p->fmt == S3R_BRICK_F32 ? 4 : 2;
+    cudaError_t e;
+    if ((e = cudaMalloc(&p->bricks, std::max<uint64_t>(p->vertices, 1) * esz)) != cudaSuccess)
+        return bail(cuda_fail(ctx, e, "cudaMalloc(bricks)"));
+    if ((rc = upload(ctx, &p->node_off_dev, p->node_off))) return bail(rc);
+    if ((e = cudaMalloc(&p->scale_offset_dev, sizeof(float2) * p->nblocks)) != cudaSuccess)
+        return bail(cuda_fail(ctx, e, "cudaMalloc(scales)"));
+    if ((e = cudaMalloc(&p->table_dev, sizeof(RenderBlock) * p->table_host.size())) != cudaSuccess)
+        return bail(cuda_fail(ctx, e, "cudaMalloc(table)"));
+    if ((e = cudaMalloc(&p->view_dev, sizeof(s3r_view))) != cudaSuccess)
+        return bail(cuda_fail(ctx, e, "cudaMalloc(view)"));
+    if ((e = cudaMallocHost(&p->table_pinned, sizeof(RenderBlock) * p->table_host.size())) != cudaSuccess)
+        return bail(cuda_fail(ctx, e, "cudaMallocHost(table)"));
+    if ((e = cudaMallocHost(&p->view_pinned, sizeof(s3r_view))) != cudaSuccess)
+        return bail(cuda_fail(ctx, e, "cudaMallocHost(view)"));
+    if ((e = cudaEventCreateWithFlags(&p->staged, cudaEventDisableTiming)) != cudaSuccess)
+        return bail(cuda_fail(ctx, e, "cudaEventCreate"));
+    if ((rc = plan_bin(p, tl))) return bail(rc);
+    *out = p;
+    return S3R_OK;
+}
+
+int s3r_plan_destroy(s3r_plan* p)
+{
+    if (!p) return S3R_OK;
+    if (p->ctx) cudaSetDevice(p->ctx->device);
+    plan_drop_graph(p);
+    plan_free_device(p);
+    auto f = [](void* q) {
+        if (q) cudaFree(q);
+    };
+    f(p->bricks);
+    f(p->node_off_dev);
+    f(p->scale_offset_dev);
+    f(p->table_dev);
+    f(p->view_dev);
+    if (p->table_pinned) cudaFreeHost(p->table_pinned);
+    if (p->view_pinned) cudaFreeHost(p->view_pinned);
+    if (p->staged) cudaEventDestroy(p->staged);
+    delete p;
+    return S3R_OK;
+}
+
+int s3r_plan_info_get(const s3r_plan* p, s3r_plan_info* out)
+{
+    if (!p || !out) return fail(nullptr, S3R_ERR_INVALID, "null pointer");
+    out->nodes = p->nodes;
+    out->vertices = p->vertices;
+    out->brick_bytes = p->vertices * (p->fmt == S3R_BRICK_F32 ? 4 : 2);
+    out->tiles = p->tiles;
+    out->tile_entries = p->entries;
+    out->tile_cells = 1u << p->tile_log2;
+    out->render_tile = p->render_tile;
+    out->brick_format = p->fmt;
+    out->nblocks = p->nblocks;
+    return S3R_OK;
+}
+
+int s3r_plan_bricks(const s3r_plan* p, void** bricks, const uint64_t** vertex_off)
+{
+    if (!p || !bricks || !vertex_off) return fail(nullptr, S3R_ERR_INVALID, "null pointer");
+    *bricks = p->bricks;
+    *vertex_off = p->vertex_off.data();
+    return S3R_OK;
+}
+
+int s3r_plan_brick_scales(const s3r_plan* p, const float** scale_offset)
+{
+    if (!p || !scale_offset) return fail(nullptr, S3R_ERR_INVALID, "null pointer");
+    *scale_offset = p->fmt == S3R_BRICK_F32 ? nullptr : reinterpret_cast<const float*>(p->scale_offset_dev);
+    return S3R_OK;
+}
+
+int s3r_frame_interp(s3r_ctx* ctx, s3r_plan* plan, const float* sparse, void* stream)
+{
+    if (!ctx || !plan || (!sparse && plan->nodes)) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (plan->ctx != ctx) return fail(ctx, S3R_ERR_INVALID, "plan belongs to another context");
+    int rc = set_device(ctx);
+    if (rc) return rc;
+    uint32_t k = 0;
+    rc = plan_launch_interp(plan, sparse, as_stream(stream), &k);
+    ctx->launches += k;
+    return rc;
+}
+
+int s3r_frame_render(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* tf, float* rgba, uint32_t* argb,
+                     unsigned long long* samples, void* stream)
+{
+    if (!ctx || !plan || !tf) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (plan->ctx != ctx) return fail(ctx, S3R_ERR_INVALID, "plan belongs to another context");
+    int rc = check_view(ctx, view);
+    if (rc) return rc;
+    if (view->level != plan->level) return fail(ctx, S3R_ERR_INVALID, "view level differs from the plan level");
+    if ((rc = set_device(ctx))) return rc;
+    cudaStream_t s = as_stream(stream);
+    if ((rc = plan_stage_view(plan, view, s))) return rc;
+    uint32_t k = 0;
+    rc = plan_launch_render(plan, tf, rgba, argb, samples, s, &k);
+    ctx->launches += k;
+    return rc;
+}
+
+int s3r_frame_run(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* sparse, const float* tf,
+                  float* rgba, uint32_t* argb, unsigned long long* samples, void* stream)
+{
+    if (!ctx || !plan || !tf || (!sparse && plan->nodes)) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (plan->ctx != ctx) return fail(ctx, S3R_ERR_INVALID, "plan belongs to another context");
+    int rc = check_view(ctx, view);
+    if (rc) return rc;
+    if (view->level != plan->level) return fail(ctx, S3R_ERR_INVALID, "view level differs from the plan level");
+    if ((rc = set_device(ctx))) return rc;
+    cudaStream_t s = as_stream(stream);
+    if ((rc = plan_stage_view(plan, view, s))) return rc;
+    const void* key[5] = {sparse, tf, rgba, argb, samples};
+    const bool same = plan->exec && std::memcmp(key, plan->g_key, sizeof(key)) == 0 &&
+                      plan->last_view.W == view->W && plan->last_view.H == view->H &&
+                      plan->last_view.tf_n == view->tf_n;
+    if (!same) {
+        plan_drop_graph(plan);
+        cudaStream_t cs = ctx->capture;
+        S3R_CUDA(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        uint32_t k = 0;
+        int r1 = plan_launch_interp(plan, sparse, cs, &k);
+        int r3 = r1 ? r1 : plan_launch_render(plan, tf, rgba, argb, samples, cs, &k);
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(cs, &graph);
+        if (r3) {
+            if (graph) cudaGraphDestroy(graph);
+            return r3;
+        }
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&plan->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            plan->exec = nullptr;
+            return cuda_fail(ctx, e, "cudaGraphInstantiate");
+        }
+        std::memcpy(plan->g_key, key, sizeof(key));
+        plan->graph_kernels = k;
+    }
+    S3R_CUDA(ctx, cudaGraphLaunch(plan->exec, s));
+    ctx->launches += plan->graph_kernels;
+    return S3R_OK;
+}
+
+int s3r_plan_autotune(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* sparse, const float* tf,
+                      uint32_t reps, void* stream)
+{
+    if (!ctx || !plan || !tf || (!sparse && plan->nodes)) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (plan->ctx != ctx) return fail(ctx, S3R_ERR_INVALID, "plan belongs to another context");
+    int rc = check_view(ctx, view);
+    if (rc) return rc;
+    if (view->level != plan->level) return fail(ctx, S3R_ERR_INVALID, "view level differs from the plan level");
+    if ((rc = set_device(ctx))) return rc;
+    if (reps == 0) reps = 3;
+    cudaStream_t s = as_stream(stream);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    float* img = nullptr;
+    auto cleanup = [&](int code) {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (img) cudaFree(img);
+        return code;
+    };
+    cudaError_t e;
+    if ((e = cudaEventCreate(&e0)) != cudaSuccess || (e = cudaEventCreate(&e1)) != cudaSuccess ||
+        (e = cudaMalloc(&img, sizeof(float) * 4 * (size_t)view->W * view->H)) != cudaSuccess)
+        return cleanup(cuda_fail(ctx, e, "autotune set-up"));
+    auto timed = [&](auto&& body, float& ms) -> int {
+        uint32_t k = 0;
+        int r = body(&k); // warm-up
+        if (r) return r;
+        if ((e = cudaEventRecord(e0, s)) != cudaSuccess) return cuda_fail(ctx, e, "cudaEventRecord");
+        for (uint32_t i = 0; i < reps; ++i)
+            if ((r = body(&k))) return r;
+        if ((e = cudaEventRecord(e1, s)) != cudaSuccess) return cuda_fail(ctx, e, "cudaEventRecord");
+        if ((e = cudaEventSynchronize(e1)) != cudaSuccess) return cuda_fail(ctx, e, "cudaEventSynchronize");
+        cudaEventElapsedTime(&ms, e0, e1);
+        ctx->launches += k;
+        return S3R_OK;
+    };
+    uint32_t best_tl = plan->tile_log2;
+    float best = 3.4e38f;
+    for (uint32_t tl = 3; tl <= 5; ++tl) {
+        if ((rc = plan_bin(plan, tl))) return cleanup(rc);
+        float ms = 0;
+        rc = timed([&](uint32_t* k) { return plan_launch_interp(plan, sparse, s, k); }, ms);
+        if (rc) return cleanup(rc);
+        if (ms < best) {
+            best = ms;
+            best_tl = tl;
+        }
+    }
+    if ((rc = plan_bin(plan, best_tl))) return cleanup(rc);
+    uint32_t k = 0;
+    if ((rc = plan_launch_interp(plan, sparse, s, &k))) return cleanup(rc);
+    ctx->launches += k;
+    if ((rc = plan_stage_view(plan, view, s))) return cleanup(rc);
+    uint32_t best_shape = plan->render_tile;
+    best = 3.4e38f;
+    for (uint32_t shape = 0; shape < (uint32_t)kRenderShapes; ++shape) {
+        plan->render_tile = shape;
+        float ms = 0;
+        rc = timed([&](uint32_t* kk) { return plan_launch_render(plan, tf, img, nullptr, nullptr, s, kk); }, ms);
+        if (rc) return cleanup(rc);
+        if (ms < best) {
+            best = ms;
+            best_shape = shape;
+        }
+    }
+    plan->render_tile = best_shape;
+    plan_drop_graph(plan);
+    return cleanup(S3R_OK);
+}
+
+int s3r_render_argb_backward(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* tf, const float* rgba,
+                             const float* dl_drgba, float* dtf, float* ddense, void* stream)
+{
+    if (!ctx || !plan || !tf || !rgba || !dl_drgba || !dtf || !ddense)
+        return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (plan->fmt != S3R_BRICK_F32) return fail(ctx, S3R_ERR_UNSUPPORTED, "the adjoint needs FP32 bricks");
+    int rc = check_view(ctx, view);
+    if (rc) return rc;
+    if (view->level != plan->level) return fail(ctx, S3R_ERR_INVALID, "view level differs from the plan level");
+    if ((rc = set_device(ctx))) return rc;
+    cudaStream_t s = as_stream(stream);
+    if ((rc = plan_stage_view(plan, view, s))) return rc;
+    FrameArgs fa{};
+    fa.view = plan->view_dev;
+    fa.table = plan->table_dev;
+    fa.bricks = plan->bricks;
+    fa.tf = tf;
+    fa.fwd_rgba = rgba;
+    fa.dl_drgba = dl_drgba;
+    fa.dtf = dtf;
+    fa.ddense = ddense;
+    S3R_CUDA(ctx, launch_frame_backward(fa, view->W, view->H, view->tf_n, s));
+    ++ctx->launches;
+    return S3R_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,641 @@
+// Block ray casting for sm_103a.
+//
+// Restates renderKernel<FieldMode::Argb> + renderArgb of the reference
+// (src/s3dmm_cuda/DenseFieldRenderer_cu.cu:62-215, src/s3dmm_cuda/renderArgb.hpp:30-55,
+// cuda_blend.hpp:24-44, cuda_argb_transform.hpp:26-43) without texture
+// hardware: bricks are linear arrays in HBM read through the read-only path,
+// filtered in FP32 by software trilinear interpolation with clamp addressing
+// (a sample whose 8 texels hold a NaN is skipped, as the texture unit's
+// weighted sum would be NaN); the transfer function sits in shared memory.
+//
+// Ray set-up (per-pixel ray, per-block slab test, sample count and positions)
+// is written with explicitly rounded operations (__fadd_rn, __fmul_rn, ...)
+// so that it cannot be contracted and the CPU oracle reproduces the same
+// sample positions bit for bit.  The sample loop keeps the reference's
+// indexing: sample k = i-1 for i = 1 .. sampleCount-1, at entry + k*step,
+// computed directly (fma) rather than by accumulation.
+//
+// Kernels:
+//   render_block_argb_kernel  one block into an ARGB8 viewport (drop-in form):
+//                             reference non-premultiplied blending, ARGB8
+//                             read-modify-write per block;
+//   frame_render_kernel       batched form: each ray walks the block grid front
+//                             to back (3D DDA), marches every block it enters
+//                             exactly as above, composites block results with
+//                             the over operator in FP32 (premultiplied), and
+//                             stops once alpha passes view.alpha_stop;
+//   frame_backward_kernel     adjoint of frame_render_kernel w.r.t. the
+//                             transfer function and the dense values; re-walks
+//                             each ray instead of storing samples.
+#include "s3r_internal.h"
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+namespace s3r {
+namespace {
+
+constexpr float kAlphaThreshold = 0.996f; // renderArgb.hpp:47
+constexpr float kTopHalf = 5.f;           // DenseFieldRenderer_cu.cu:339
+
+struct BlockRay {
+    float tau_enter;
+    float tau_exit;
+    int samples;
+    float p0[3];
+    float step[3];
+    float origin[3];
+    float factor;
+    uint32_t n;
+};
+
+__device__ __forceinline__ void pixel_ray(const s3r_view& v, uint32_t vx, uint32_t vy, float org[3], float dir[3])
+{
+    const float x = __fmul_rn(__fadd_rn(-0.5f, __fdiv_rn(__fadd_rn((float)vx, 0.5f), (float)v.W)), v.cam.w);
+    const float y = __fmul_rn(__fadd_rn(-0.5f, __fdiv_rn(__fadd_rn((float)vy, 0.5f), (float)v.H)), v.cam.h);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float ex = __fmul_rn(v.cam.e1[d], x);
+        const float ey = __fmul_rn(v.cam.e2[d], y);
+        if (v.cam.ortho) {
+            org[d] = __fadd_rn(__fadd_rn(v.cam.eye[d], ex), ey);
+            dir[d] = v.cam.n[d];
+        } else {
+            org[d] = v.cam.eye[d];
+            dir[d] = __fadd_rn(__fadd_rn(v.cam.n[d], ex), ey);
+        }
+    }
+}
+
+__device__ __forceinline__ void block_cube(uint32_t level, uint32_t ix, uint32_t iy, uint32_t iz, float c[3],
+                                           float& h)
+{
+    h = __fdiv_rn(kTopHalf, (float)(1u << level));
+    c[0] = __fadd_rn(-kTopHalf, __fmul_rn(h, (float)(1u + (ix << 1))));
+    c[1] = __fadd_rn(-kTopHalf, __fmul_rn(h, (float)(1u + (iy << 1))));
+    c[2] = __fadd_rn(-kTopHalf, __fmul_rn(h, (float)(1u + (iz << 1))));
+}
+
+// Slab test and sample set-up (DenseFieldRenderer_cu.cu:81-181). Returns true
+// when the block is rendered for this ray.
+__device__ __forceinline__ bool block_ray(const s3r_view& v, const float org[3], const float dir[3], const float c[3],
+                                          float h, uint32_t depth, BlockRay& r)
+{
+    float te = 1.f, tx = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (!(fabsf(dir[a]) > 1e-10f)) continue;
+        const int b1 = a == 0 ? 1 : 0;
+        const int b2 = a == 2 ? 1 : 2;
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            const float face = side ? __fadd_rn(c[a], h) : __fsub_rn(c[a], h);
+            const float tau = __fdiv_rn(__fsub_rn(face, org[a]), dir[a]);
+            const float p1 = __fadd_rn(org[b1], __fmul_rn(dir[b1], tau));
+            const float p2 = __fadd_rn(org[b2], __fmul_rn(dir[b2], tau));
+            if (fabsf(__fsub_rn(p1, c[b1])) <= h && fabsf(__fsub_rn(p2, c[b2])) <= h) {
+                const bool enter = (dir[a] > 0.f) == (side == 0);
+                if (enter) te = tau;
+                else tx = tau;
+            }
+        }
+    }
+    if (te < 1.f) te = 1.f;
+    r.tau_enter = te;
+    r.tau_exit = tx;
+    if (!(tx > te)) return false;
+    const uint32_t n = (1u << depth) + 1u;
+    const float texel = __fdiv_rn(__fmul_rn(2.f, h), (float)n);
+    const float span = __fsub_rn(tx, te);
+    const float dotr = __fadd_rn(__fadd_rn(__fmul_rn(dir[0], dir[0]), __fmul_rn(dir[1], dir[1])),
+                                 __fmul_rn(dir[2], dir[2]));
+    const float l1 = __fadd_rn(__fadd_rn(fabsf(dir[0]), fabsf(dir[1])), fabsf(dir[2]));
+    const float num = __fmul_rn(__fmul_rn(v.quality, span), dotr);
+    const float den = __fmul_rn(texel, l1);
+    const int s = __float2int_rz(__fdiv_rn(num, den));
+    const float dtau = __fdiv_rn(span, (float)s);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        r.step[d] = __fmul_rn(dir[d], dtau);
+        r.p0[d] = __fadd_rn(org[d], __fmul_rn(dir[d], te));
+    }
+    const double thalf = __dadd_rn((double)h, __dmul_rn(0.5, (double)texel));
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+        r.origin[d] = __fsub_rn(c[d], (float)thalf);
+    r.factor = (float)__ddiv_rn((double)n, __dmul_rn(2.0, thalf));
+    r.n = n;
+    r.samples = s;
+    return true;
+}
+
+struct Cell {
+    uint32_t i0[3], i1[3];
+    float f[3];
+};
+
+__device__ __forceinline__ void sample_cell(const BlockRay& r, int k, Cell& c)
+{
+    const int hi = (int)r.n - 1;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float p = __fmaf_rn(r.step[d], (float)k, r.p0[d]);
+        const float tc = __fmul_rn(__fsub_rn(p, r.origin[d]), r.factor);
+        const float xb = __fsub_rn(tc, 0.5f);
+        const float fl = floorf(xb);
+        c.f[d] = __fsub_rn(xb, fl);
+        const int a = (int)fl, b = a + 1;
+        c.i0[d] = (uint32_t)min(max(a, 0), hi);
+        c.i1[d] = (uint32_t)min(max(b, 0), hi);
+    }
+}
+
+// 8 texels of a cell from a brick of format Fmt, decoded to float.
+template <int Fmt> struct Brick;
+template <> struct Brick<S3R_BRICK_F32> {
+    __device__ static float get(const void* b, uint64_t i) { return __ldg(reinterpret_cast<const float*>(b) + i); }
+};
+template <> struct Brick<S3R_BRICK_F16> {
+    __device__ static float get(const void* b, uint64_t i)
+    {
+        return __half2float(__ldg(reinterpret_cast<const __half*>(b) + i));
+    }
+};
+template <> struct Brick<S3R_BRICK_BF16> {
+    __device__ static float get(const void* b, uint64_t i)
+    {
+        return __bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(b) + i));
+    }
+};
+
+template <int Fmt>
+__device__ __forceinline__ bool trilinear(const void* brick, const Cell& c, uint32_t n, float& val, float t[8],
+                                          uint64_t off[8])
+{
+    const uint64_t n64 = n;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const uint64_t x = (q & 1) ? c.i1[0] : c.i0[0];
+        const uint64_t y = (q & 2) ? c.i1[1] : c.i0[1];
+        const uint64_t z = (q & 4) ? c.i1[2] : c.i0[2];
+        off[q] = (z * n64 + y) * n64 + x;
+        t[q] = Brick<Fmt>::get(brick, off[q]);
+    }
+    bool bad = false;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) bad |= isnan(t[q]);
+    if (bad) return false;
+    const float x00 = __fmaf_rn(c.f[0], t[1] - t[0], t[0]);
+    const float x10 = __fmaf_rn(c.f[0], t[3] - t[2], t[2]);
+    const float x01 = __fmaf_rn(c.f[0], t[5] - t[4], t[4]);
+    const float x11 = __fmaf_rn(c.f[0], t[7] - t[6], t[6]);
+    const float y0 = __fmaf_rn(c.f[1], x10 - x00, x00);
+    const float y1 = __fmaf_rn(c.f[1], x11 - x01, x01);
+    val = __fmaf_rn(c.f[2], y1 - y0, y0);
+    return true;
+}
+
+struct TfSample {
+    float4 c;
+    uint32_t i0, i1;
+    float f;
+    bool clamped;
+};
+
+// tex1D with normalized coordinates, linear filtering, clamp addressing.
+__device__ __forceinline__ TfSample tf_lookup(const float4* tf, uint32_t tfn, float v01)
+{
+    TfSample s;
+    const float u = __fmaf_rn(v01, (float)tfn, -0.5f);
+    const float fl = floorf(u);
+    s.f = u - fl;
+    const int hi = (int)tfn - 1;
+    const int a = (int)fmaxf(fminf(fl, 1e9f), -1e9f), b = a + 1;
+    s.clamped = a < 0 || b > hi;
+    s.i0 = (uint32_t)min(max(a, 0), hi);
+    s.i1 = (uint32_t)min(max(b, 0), hi);
+    const float4 p = tf[s.i0], q = tf[s.i1];
+    s.c.x = __fmaf_rn(s.f, q.x - p.x, p.x);
+    s.c.y = __fmaf_rn(s.f, q.y - p.y, p.y);
+    s.c.z = __fmaf_rn(s.f, q.z - p.z, p.z);
+    s.c.w = __fmaf_rn(s.f, q.w - p.w, p.w);
+    return s;
+}
+
+__device__ __forceinline__ float layer_exponent(uint32_t depth, uint32_t level, float quality)
+{
+    return __fmul_rn(__fdiv_rn(1.f, __fmul_rn((float)(1u << (depth + level)), quality)), 100.f);
+}
+
+__device__ __forceinline__ float4 argb_to_rgba(uint32_t p)
+{
+    return make_float4((float)((p >> 16) & 0xffu) / 255.f, (float)((p >> 8) & 0xffu) / 255.f,
+                       (float)(p & 0xffu) / 255.f, (float)((p >> 24) & 0xffu) / 255.f);
+}
+
+__device__ __forceinline__ uint32_t rgba_to_argb(float4 c)
+{
+    return ((uint32_t)(c.w * 255.999f) << 24) + ((uint32_t)(c.x * 255.999f) << 16) +
+           ((uint32_t)(c.y * 255.999f) << 8) + (uint32_t)(c.z * 255.999f);
+}
+
+// ---------------------------------------------------------------- plain form
+
+__global__ void render_block_argb_kernel(const s3r_view v, const float* __restrict__ brick,
+                                         uint32_t depth, float cx, float cy, float cz, float h, int32_t rx,
+                                         int32_t ry, int32_t rw, int32_t rh, const float4* __restrict__ tf_g,
+                                         uint32_t* __restrict__ viewport)
+{
+    extern __shared__ float4 tf[];
+    for (uint32_t i = threadIdx.y * blockDim.x + threadIdx.x; i < v.tf_n; i += blockDim.x * blockDim.y)
+        tf[i] = tf_g[i];
+    __syncthreads();
+    const int32_t xx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int32_t yy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (xx >= rw || yy >= rh) return;
+    const uint32_t vx = (uint32_t)(rx + xx), vy = (uint32_t)(ry + yy);
+    if (vx >= v.W || vy >= v.H) return;
+    float org[3], dir[3];
+    pixel_ray(v, vx, vy, org, dir);
+    const float c[3] = {cx, cy, cz};
+    BlockRay r;
+    if (!block_ray(v, org, dir, c, h, depth, r)) return;
+    const float span = v.field_max - v.field_min;
+    const float of = (v.threshold - v.field_min) / span;
+    const float il = layer_exponent(depth, v.level, v.quality);
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = 1; i < r.samples; ++i) {
+        Cell cell;
+        sample_cell(r, i - 1, cell);
+        float t[8], val;
+        uint64_t off[8];
+        if (!trilinear<S3R_BRICK_F32>(brick, cell, r.n, val, t, off)) continue;
+        const float v01 = (val - v.field_min) / span;
+        float4 col = tf_lookup(tf, v.tf_n, v01).c;
+        col.w = 1.f - __powf(1.f - col.w * of, il);
+        // blendBehind (cuda_blend.hpp:24-33)
+        const float da = col.w * (1.f - acc.w);
+        const float a = acc.w + da;
+        if (a > 0.f) {
+            const float ka = acc.w / a, kd = da / a;
+            acc.x = acc.x * ka + col.x * kd;
+            acc.y = acc.y * ka + col.y * kd;
+            acc.z = acc.z * ka + col.z * kd;
+        }
+        acc.w = a;
+        if (acc.w > kAlphaThreshold) break;
+    }
+    uint32_t* px = &viewport[(size_t)(v.H - 1 - vy) * v.W + vx];
+    float4 ex = argb_to_rgba(*px);
+    // blendAbove (cuda_blend.hpp:35-44)
+    const float da = ex.w * (1.f - acc.w);
+    const float a = acc.w + da;
+    if (a > 0.f) {
+        const float kd = da / a, ki = acc.w / a;
+        ex.x = ex.x * kd + acc.x * ki;
+        ex.y = ex.y * kd + acc.y * ki;
+        ex.z = ex.z * kd + acc.z * ki;
+    }
+    ex.w = a;
+    *px = rgba_to_argb(ex);
+}
+
+// ---------------------------------------------------------------- batched form
+
+// Front-to-back walk of the (2^level)^3 block grid along one ray
+// (Amanatides-Woo); calls f(block_index, ix, iy, iz) for every block the ray
+// passes, in order; f returns false to stop.
+template <class F>
+__device__ __forceinline__ void walk_blocks(const float org[3], const float dir[3], uint32_t level, F&& f)
+{
+    const int m = 1 << level;
+    const float cell = (2.f * kTopHalf) / (float)m;
+    // entry/exit of the whole cube [-5, 5]^3, restricted to tau >= 1 (the screen plane)
+    float t0 = 1.f, t1 = 3.4e38f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (fabsf(dir[a]) > 1e-10f) {
+            const float inv = 1.f / dir[a];
+            float ta = (-kTopHalf - org[a]) * inv, tb = (kTopHalf - org[a]) * inv;
+            if (ta > tb) { const float t = ta; ta = tb; tb = t; }
+            t0 = fmaxf(t0, ta);
+            t1 = fminf(t1, tb);
+        } else if (org[a] < -kTopHalf || org[a] > kTopHalf) {
+            return;
+        }
+    }
+    if (!(t1 > t0)) return;
+    const float tm = 0.5f * (t0 + fminf(t1, t0 + cell));
+    int ci[3], stp[3];
+    float tmax[3], tdel[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float p = __fmaf_rn(dir[a], t0, org[a]);
+        const float pm = __fmaf_rn(dir[a], tm, org[a]);
+        (void)p;
+        int c = (int)floorf((pm + kTopHalf) / cell);
+        c = min(max(c, 0), m - 1);
+        ci[a] = c;
+        if (dir[a] > 1e-10f) {
+            stp[a] = 1;
+            tmax[a] = ((-kTopHalf + cell * (float)(c + 1)) - org[a]) / dir[a];
+            tdel[a] = cell / dir[a];
+        } else if (dir[a] < -1e-10f) {
+            stp[a] = -1;
+            tmax[a] = ((-kTopHalf + cell * (float)c) - org[a]) / dir[a];
+            tdel[a] = -cell / dir[a];
+        } else {
+            stp[a] = 0;
+            tmax[a] = 3.4e38f;
+            tdel[a] = 3.4e38f;
+        }
+    }
+    for (int guard = 0; guard < 3 * m + 3; ++guard) {
+        const uint32_t b = (uint32_t)ci[0] + (uint32_t)m * ((uint32_t)ci[1] + (uint32_t)m * (uint32_t)ci[2]);
+        if (!f(b, (uint32_t)ci[0], (uint32_t)ci[1], (uint32_t)ci[2])) return;
+        int a = 0;
+        if (tmax[1] < tmax[a]) a = 1;
+        if (tmax[2] < tmax[a]) a = 2;
+        if (tmax[a] >= t1) return;
+        ci[a] += stp[a];
+        if (ci[a] < 0 || ci[a] >= m) return;
+        tmax[a] += tdel[a];
+    }
+}
+
+__device__ __forceinline__ bool pixel_in_rect(const int32_t* rc, uint32_t vx, uint32_t vy)
+{
+    return (int32_t)vx >= rc[0] && (int32_t)vx < rc[0] + rc[2] && (int32_t)vy >= rc[1] && (int32_t)vy < rc[1] + rc[3];
+}
+
+struct Premul {
+    float r, g, b, a;
+};
+
+// March one block along a ray (premultiplied, block-local early termination).
+template <int Fmt>
+__device__ __forceinline__ Premul march_block(const s3r_view& v, const BlockRay& r, const void* brick, float scale,
+                                              float offset, uint32_t depth, const float4* tf, float of,
+                                              uint32_t& taken)
+{
+    const float span = v.field_max - v.field_min;
+    const float il = layer_exponent(depth, v.level, v.quality);
+    Premul acc{0.f, 0.f, 0.f, 0.f};
+    for (int i = 1; i < r.samples; ++i) {
+        ++taken;
+        Cell cell;
+        sample_cell(r, i - 1, cell);
+        float t[8], val;
+        uint64_t off[8];
+        if (!trilinear<Fmt>(brick, cell, r.n, val, t, off)) continue;
+        if (Fmt != S3R_BRICK_F32) val = __fmaf_rn(scale, val, offset);
+        const float v01 = __fdiv_rn(__fsub_rn(val, v.field_min), span);
+        const float4 col = tf_lookup(tf, v.tf_n, v01).c;
+        const float a = __fsub_rn(1.f, __powf(__fmaf_rn(-col.w, of, 1.f), il));
+        const float w = __fmul_rn(__fsub_rn(1.f, acc.a), a);
+        acc.r = __fmaf_rn(w, col.x, acc.r);
+        acc.g = __fmaf_rn(w, col.y, acc.g);
+        acc.b = __fmaf_rn(w, col.z, acc.b);
+        acc.a = __fadd_rn(acc.a, w);
+        if (acc.a > kAlphaThreshold) break;
+    }
+    return acc;
+}
+
+template <int Fmt>
+__global__ void frame_render_kernel(FrameArgs fa)
+{
+    extern __shared__ float4 tf[];
+    const s3r_view v = *fa.view;
+    const uint32_t nthreads = blockDim.x * blockDim.y;
+    const uint32_t tid = threadIdx.y * blockDim.x + threadIdx.x;
+    for (uint32_t i = tid; i < v.tf_n; i += nthreads) tf[i] = reinterpret_cast<const float4*>(fa.tf)[i];
+    __syncthreads();
+    const uint32_t vx = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t vy = blockIdx.y * blockDim.y + threadIdx.y;
+    uint32_t taken = 0;
+    if (vx < v.W && vy < v.H) {
+        float org[3], dir[3];
+        pixel_ray(v, vx, vy, org, dir);
+        const float of = (v.threshold - v.field_min) / (v.field_max - v.field_min);
+        Premul acc{0.f, 0.f, 0.f, 0.f};
+        walk_blocks(org, dir, v.level, [&](uint32_t b, uint32_t ix, uint32_t iy, uint32_t iz) {
+            const RenderBlock* rb = &fa.table[b];
+            const uint32_t depth = rb->depth;
+            if (depth == 0xffffffffu) return true;
+            const int4 rc = *reinterpret_cast<const int4*>(rb->rect);
+            const int32_t rca[4] = {rc.x, rc.y, rc.z, rc.w};
+            if (!pixel_in_rect(rca, vx, vy)) return true;
+            float c[3], h;
+            block_cube(v.level, ix, iy, iz, c, h);
+            BlockRay r;
+            if (!block_ray(v, org, dir, c, h, depth, r)) return true;
+            const char* base = reinterpret_cast<const char*>(fa.bricks);
+            const size_t esz = Fmt == S3R_BRICK_F32 ? 4 : 2;
+            float scale = 1.f, offset = 0.f;
+            if (Fmt != S3R_BRICK_F32) {
+                const float2 so = fa.scale_offset[rb->block];
+                scale = so.x;
+                offset = so.y;
+            }
+            const Premul p = march_block<Fmt>(v, r, base + rb->brick_off * esz, scale, offset, depth, tf, of, taken);
+            const float T = __fsub_rn(1.f, acc.a);
+            acc.r = __fmaf_rn(T, p.r, acc.r);
+            acc.g = __fmaf_rn(T, p.g, acc.g);
+            acc.b = __fmaf_rn(T, p.b, acc.b);
+            acc.a = __fmaf_rn(T, p.a, acc.a);
+            return !(acc.a > v.alpha_stop);
+        });
+        const size_t o = (size_t)(v.H - 1 - vy) * v.W + vx;
+        float4 out = make_float4(0.f, 0.f, 0.f, acc.a);
+        if (acc.a > 0.f) {
+            const float inv = 1.f / acc.a;
+            out.x = acc.r * inv;
+            out.y = acc.g * inv;
+            out.z = acc.b * inv;
+        }
+        if (fa.rgba) reinterpret_cast<float4*>(fa.rgba)[o] = out;
+        if (fa.argb) fa.argb[o] = rgba_to_argb(out);
+    }
+    if (fa.samples) {
+        unsigned long long t = taken;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if ((tid & 31) == 0 && t) atomicAdd(fa.samples, t);
+    }
+}
+
+// ---------------------------------------------------------------- adjoint
+
+// For L = 1/2 sum (I - target)^2 with I = (C/A, A) the premultiplied composite
+// of the kept samples (front to back, T_k = prod_{j<k} (1 - a_k)):
+//   dC/dc_k = T_k a_k,  dC/da_k = T_k c_k - (C - C_{<=k}) / (1 - a_k),
+//   dA/da_k = (1 - A) / (1 - a_k),
+// a_k = 1 - (1 - alpha_tf * of)^il, c_k / alpha_tf linear in the table
+// entries around v01, v01 linear in the trilinear value.
+__global__ void frame_backward_kernel(FrameArgs fa)
+{
+    extern __shared__ float4 sm[];
+    const s3r_view v = *fa.view;
+    float4* tf = sm;
+    float* dtf_s = reinterpret_cast<float*>(sm + v.tf_n);
+    const uint32_t nthreads = blockDim.x * blockDim.y;
+    const uint32_t tid = threadIdx.y * blockDim.x + threadIdx.x;
+    for (uint32_t i = tid; i < v.tf_n; i += nthreads) tf[i] = reinterpret_cast<const float4*>(fa.tf)[i];
+    for (uint32_t i = tid; i < 4 * v.tf_n; i += nthreads) dtf_s[i] = 0.f;
+    __syncthreads();
+    const uint32_t vx = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t vy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (vx < v.W && vy < v.H) {
+        const size_t o = (size_t)(v.H - 1 - vy) * v.W + vx;
+        const float4 I = reinterpret_cast<const float4*>(fa.fwd_rgba)[o];
+        const float4 gI = reinterpret_cast<const float4*>(fa.dl_drgba)[o];
+        const float A = I.w;
+        float gC[3] = {0.f, 0.f, 0.f};
+        float gA = gI.w;
+        const float Ct[3] = {I.x * A, I.y * A, I.z * A};
+        if (A > 0.f) {
+            const float inv = 1.f / A;
+            gC[0] = gI.x * inv;
+            gC[1] = gI.y * inv;
+            gC[2] = gI.z * inv;
+            gA -= (gI.x * I.x + gI.y * I.y + gI.z * I.z) * inv;
+        }
+        const bool active = (gC[0] != 0.f || gC[1] != 0.f || gC[2] != 0.f || gA != 0.f);
+        if (active) {
+            float org[3], dir[3];
+            pixel_ray(v, vx, vy, org, dir);
+            const float span = v.field_max - v.field_min;
+            const float of = (v.threshold - v.field_min) / span;
+            float T = 1.f, Cpre[3] = {0.f, 0.f, 0.f};
+            float accA = 0.f;
+            walk_blocks(org, dir, v.level, [&](uint32_t b, uint32_t ix, uint32_t iy, uint32_t iz) {
+                const RenderBlock* rb = &fa.table[b];
+                const uint32_t depth = rb->depth;
+                if (depth == 0xffffffffu) return true;
+                const int4 rc = *reinterpret_cast<const int4*>(rb->rect);
+                const int32_t rca[4] = {rc.x, rc.y, rc.z, rc.w};
+                if (!pixel_in_rect(rca, vx, vy)) return true;
+                float c[3], h;
+                block_cube(v.level, ix, iy, iz, c, h);
+                BlockRay r;
+                if (!block_ray(v, org, dir, c, h, depth, r)) return true;
+                const float* brick = reinterpret_cast<const float*>(fa.bricks) + rb->brick_off;
+                float* gdense = fa.ddense + rb->brick_off;
+                const float il = layer_exponent(depth, v.level, v.quality);
+                float Ab = 0.f;
+                for (int i = 1; i < r.samples; ++i) {
+                    Cell cell;
+                    sample_cell(r, i - 1, cell);
+                    float t[8], val;
+                    uint64_t off[8];
+                    if (!trilinear<S3R_BRICK_F32>(brick, cell, r.n, val, t, off)) continue;
+                    const float v01 = __fdiv_rn(__fsub_rn(val, v.field_min), span);
+                    const TfSample ts = tf_lookup(tf, v.tf_n, v01);
+                    const float base = __fmaf_rn(-ts.c.w, of, 1.f);
+                    const float pw = __powf(base, il);
+                    const float a = __fsub_rn(1.f, pw);
+                    const float dadc = base > 0.f ? il * pw / base * of : 0.f;
+                    const float wa = T * a;
+                    const float col[3] = {ts.c.x, ts.c.y, ts.c.z};
+                    float g_col[4];
+                    float g_a = 0.f;
+                    const float om = 1.f - a;
+                    const float inv_om = om > 1e-12f ? 1.f / om : 0.f;
+#pragma unroll
+                    for (int ch = 0; ch < 3; ++ch) {
+                        const float cpost = __fmaf_rn(wa, col[ch], Cpre[ch]);
+                        g_col[ch] = gC[ch] * wa;
+                        g_a += gC[ch] * (T * col[ch] - (Ct[ch] - cpost) * inv_om);
+                        Cpre[ch] = cpost;
+                    }
+                    g_a += gA * (1.f - A) * inv_om;
+                    g_col[3] = g_a * dadc;
+                    // transfer-function table
+                    const float f = ts.f;
+#pragma unroll
+                    for (int ch = 0; ch < 4; ++ch) {
+                        atomicAdd(&dtf_s[4 * ts.i0 + ch], g_col[ch] * (1.f - f));
+                        atomicAdd(&dtf_s[4 * ts.i1 + ch], g_col[ch] * f);
+                    }
+                    // dense values
+                    if (!ts.clamped) {
+                        const float4 p = tf[ts.i0], q = tf[ts.i1];
+                        const float g_v01 = (g_col[0] * (q.x - p.x) + g_col[1] * (q.y - p.y) +
+                                             g_col[2] * (q.z - p.z) + g_col[3] * (q.w - p.w)) *
+                                            (float)v.tf_n;
+                        const float g_val = g_v01 / span;
+                        if (g_val != 0.f) {
+                            const float fx = cell.f[0], fy = cell.f[1], fz = cell.f[2];
+#pragma unroll
+                            for (int qn = 0; qn < 8; ++qn) {
+                                const float w = ((qn & 1) ? fx : 1.f - fx) * ((qn & 2) ? fy : 1.f - fy) *
+                                                ((qn & 4) ? fz : 1.f - fz);
+                                atomicAdd(&gdense[off[qn]], g_val * w);
+                            }
+                        }
+                    }
+                    T *= om;
+                    Ab = __fadd_rn(Ab, __fmul_rn(__fsub_rn(1.f, Ab), a));
+                    if (Ab > kAlphaThreshold) break;
+                }
+                // block composite exactly as the forward kernel forms it
+                accA = __fmaf_rn(__fsub_rn(1.f, accA), Ab, accA);
+                return !(accA > v.alpha_stop);
+            });
+        }
+    }
+    __syncthreads();
+    for (uint32_t i = tid; i < 4 * v.tf_n; i += nthreads) {
+        const float g = dtf_s[i];
+        if (g != 0.f) atomicAdd(&fa.dtf[i], g);
+    }
+}
+
+} // namespace
+
+cudaError_t launch_render_block_argb(const s3r_view* view_host, const float* brick, uint32_t depth, const float center[3],
+                                     float half, const int32_t rect[4], uint32_t W, uint32_t H, const float* tf,
+                                     uint32_t tf_n, uint32_t* viewport, cudaStream_t s)
+{
+    (void)W;
+    (void)H;
+    if (rect[2] <= 0 || rect[3] <= 0) return cudaSuccess;
+    dim3 block(16, 8);
+    dim3 grid((rect[2] + 15) / 16, (rect[3] + 7) / 8);
+    render_block_argb_kernel<<<grid, block, tf_n * sizeof(float4), s>>>(
+        *view_host, brick, depth, center[0], center[1], center[2], half, rect[0], rect[1], rect[2], rect[3],
+        reinterpret_cast<const float4*>(tf), viewport);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_frame_render(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, uint32_t fmt,
+                                uint32_t tile_shape, cudaStream_t s)
+{
+    const int sx = kRenderShapeX[tile_shape % kRenderShapes], sy = kRenderShapeY[tile_shape % kRenderShapes];
+    dim3 block(sx, sy);
+    dim3 grid((W + sx - 1) / sx, (H + sy - 1) / sy);
+    const size_t smem = tf_n * sizeof(float4);
+    switch (fmt) {
+    case S3R_BRICK_F32: frame_render_kernel<S3R_BRICK_F32><<<grid, block, smem, s>>>(a); break;
+    case S3R_BRICK_F16: frame_render_kernel<S3R_BRICK_F16><<<grid, block, smem, s>>>(a); break;
+    case S3R_BRICK_BF16: frame_render_kernel<S3R_BRICK_BF16><<<grid, block, smem, s>>>(a); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_frame_backward(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, cudaStream_t s)
+{
+    dim3 block(16, 8);
+    dim3 grid((W + 15) / 16, (H + 7) / 8);
+    const size_t smem = tf_n * sizeof(float4) * 2;
+    if (smem > 48 * 1024) {
+        cudaError_t err =
+            cudaFuncSetAttribute(frame_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) return err;
+    }
+    frame_backward_kernel<<<grid, block, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+} // namespace s3r

@@ -1,0 +1,99 @@
+// Internal types shared by the s3r CUDA kernels and the host side of the C ABI.
+#pragma once
+
+#include "s3r.h"
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace s3r {
+
+constexpr float kNoField = S3R_NO_FIELD_VALUE;
+constexpr int kInterpThreads = 256;
+
+// One block of a batched plan, as the interpolation kernel reads it.
+struct PlanBlock {
+    uint32_t depth;       // subtree depth d: (2^d+1)^3 vertices
+    uint32_t tile_log2;   // k: tile edge 2^k cells (k <= d)
+    uint32_t coarse_log2; // L = d - k: tiles per axis 2^L
+    uint32_t coarse_off;  // first entry of this block's coarse index grid ((2^L+1)^3 int32)
+    uint64_t node_base;   // first node of this block in the sparse value array
+    uint64_t dense_off;   // first vertex of this block's brick
+};
+
+// Arguments of the tile interpolation kernel.  Two node sources:
+//   grid   != nullptr: one block whose sparse values were scattered into a
+//                      NaN-filled (2^d+1)^3 grid (blocks/items unused);
+//   grid   == nullptr: a batched plan whose nodes are binned per tile.
+struct TileArgs {
+    const PlanBlock* blocks;
+    const uint2* items;           // {block, tile} per work item
+    uint32_t nitems;
+    const uint64_t* entry_off;    // nitems+1 prefix offsets into local/node
+    const uint16_t* entry_local;  // node position inside its tile (x + e*(y + e*z), e = 2^k+1)
+    const uint32_t* entry_node;   // node index within its block
+    const int32_t* coarse_idx;    // per block coarse lattice: node index or -1
+    const float* sparse;          // node values
+    const float2* scale_offset;   // per block {scale, offset} for 16-bit bricks
+    void* out;                    // brick store
+    // single-block form
+    const float* grid;
+    uint32_t grid_depth;
+    uint32_t grid_tile_log2;
+};
+
+// Per-block entry of the render block table (dense over the (2^level)^3 block grid).
+struct RenderBlock {
+    uint32_t depth;  // 0xffffffff: no block here
+    uint32_t fmt;    // S3R_BRICK_*
+    uint64_t brick_off;
+    int32_t rect[4]; // view rectangle {x, y, w, h}
+    uint32_t block;  // index into the plan's block list (per-brick scale/offset)
+    uint32_t pad[3];
+};
+
+struct FrameArgs {
+    const s3r_view* view;          // device copy
+    const RenderBlock* table;      // (2^level)^3 entries
+    const void* bricks;
+    const float* tf;               // tf_n RGBA
+    float* rgba;                   // optional
+    uint32_t* argb;                // optional
+    unsigned long long* samples;   // optional
+    const float2* scale_offset;    // per block {scale, offset} (16-bit bricks)
+    // adjoint
+    const float* fwd_rgba;
+    const float* dl_drgba;
+    float* dtf;
+    float* ddense;
+};
+
+// Kernel launchers (defined in the .cu files); all return cudaGetLastError().
+cudaError_t launch_fill_f32(float* p, uint64_t n, float v, cudaStream_t s);
+cudaError_t launch_fill_u32(uint32_t* p, uint64_t n, uint32_t v, cudaStream_t s);
+cudaError_t launch_scatter_nodes(float* grid, uint32_t depth, const uint16_t* n2i, const float* sparse, uint32_t n,
+                                 cudaStream_t s);
+cudaError_t launch_interp_grid(const float* grid, uint32_t depth, float* dense, cudaStream_t s, uint32_t* launches);
+cudaError_t launch_interp_plan(const TileArgs& a, uint32_t fmt, uint32_t tile_log2_max, uint32_t grid_ctas,
+                               cudaStream_t s);
+cudaError_t launch_block_ranges(const PlanBlock* blocks, uint32_t nblocks, const float* sparse,
+                                const uint64_t* node_off_dev, float2* scale_offset, cudaStream_t s);
+
+cudaError_t launch_render_block_argb(const s3r_view* view_host, const float* brick, uint32_t depth, const float center[3],
+                                     float half, const int32_t rect[4], uint32_t W, uint32_t H, const float* tf,
+                                     uint32_t tf_n, uint32_t* viewport, cudaStream_t s);
+cudaError_t launch_frame_render(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, uint32_t fmt,
+                                uint32_t tile_shape, cudaStream_t s);
+cudaError_t launch_frame_backward(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, cudaStream_t s);
+
+cudaError_t launch_bound_rect(const uint32_t* img, uint32_t W, uint32_t H, int32_t* rect_dev, cudaStream_t s);
+cudaError_t launch_crop(const uint32_t* img, uint32_t W, const int32_t rect[4], uint32_t* dst, cudaStream_t s);
+cudaError_t launch_compose(const s3r_image_part* parts_dev, uint32_t nparts, int32_t just_copy_first, uint32_t* dst,
+                           int32_t dw, int32_t dh, int32_t offx, int32_t offy, cudaStream_t s);
+
+// Render CTA shapes the autotuner chooses from: {x, y} threads.
+constexpr int kRenderShapes = 4;
+constexpr int kRenderShapeX[kRenderShapes] = {16, 32, 8, 16};
+constexpr int kRenderShapeY[kRenderShapes] = {8, 4, 8, 16};
+
+} // namespace s3r

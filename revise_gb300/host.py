@@ -1,0 +1,103 @@
+"""Host-only entry points of the s3r C ABI (no GPU needed): camera and view set-up,
+block geometry, back-to-front ordering, the transfer-function table and the
+host image-part blend."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import Camera, View, arr, check
+
+
+def camera_look_at(eye, center, up, fovy_deg: float, W: int, H: int, ortho: bool = False,
+                   ortho_height: float = 0.0) -> Camera:
+    lib = _lib.load()
+    cam = Camera()
+    e = (C.c_double * 3)(*eye)
+    c = (C.c_double * 3)(*center)
+    u = (C.c_double * 3)(*up)
+    check(lib.s3r_camera_look_at(e, c, u, float(fovy_deg), W, H, 1 if ortho else 0, float(ortho_height),
+                                 C.byref(cam)))
+    return cam
+
+
+def make_view(cam: Camera, W: int, H: int, level: int, field_min: float, field_max: float, threshold: float,
+              quality: float, tf_n: int, alpha_stop: float = 2.0) -> View:
+    v = View()
+    v.cam = cam
+    v.W, v.H, v.level = W, H, level
+    v.field_min, v.field_max = field_min, field_max
+    v.threshold, v.quality = threshold, quality
+    v.tf_n = tf_n
+    v.alpha_stop = alpha_stop
+    return v
+
+
+def view_for(w, alpha_stop: float = 2.0) -> View:
+    """The view of a revise_gb300.workloads.Workload."""
+    cam = camera_look_at(w.eye, w.center, w.up, w.fovy, w.W, w.H, w.ortho, w.ortho_height)
+    return make_view(cam, w.W, w.H, w.level, w.field_min, w.field_max, w.threshold, w.quality, w.tf.shape[0],
+                     alpha_stop)
+
+
+def block_cube(level: int, idx):
+    lib = _lib.load()
+    i = (C.c_uint32 * 3)(*idx)
+    c = (C.c_float * 3)()
+    h = C.c_float()
+    check(lib.s3r_block_cube(level, i, c, C.byref(h)))
+    return np.array(c[:], dtype=np.float32), np.float32(h.value)
+
+
+def block_view_rect(view: View, idx) -> np.ndarray:
+    lib = _lib.load()
+    i = (C.c_uint32 * 3)(*idx)
+    r = (C.c_int32 * 4)()
+    check(lib.s3r_block_view_rect(C.byref(view), i, r))
+    return np.array(r[:], dtype=np.int32)
+
+
+def b2f_order(bmin, bmax, cmin, cmax, eye) -> np.ndarray:
+    """BackToFrontOrder<MacroBlock<3>>::range(eye) over index box [bmin, bmax): (n, 3) uint32."""
+    lib = _lib.load()
+    a = (C.c_uint32 * 3)(*bmin)
+    b = (C.c_uint32 * 3)(*bmax)
+    c0 = (C.c_double * 3)(*cmin)
+    c1 = (C.c_double * 3)(*cmax)
+    e = (C.c_double * 3)(*eye)
+    cap = int(np.prod(np.asarray(bmax, dtype=np.int64) - np.asarray(bmin, dtype=np.int64)))
+    out = np.zeros((max(cap, 1), 3), dtype=np.uint32)
+    cnt = C.c_uint32()
+    check(lib.s3r_b2f_order(a, b, c0, c1, e, arr(out, C.c_uint32), cap, C.byref(cnt)))
+    return out[: cnt.value]
+
+
+def index_box_world(level: int, bmin, bmax):
+    lib = _lib.load()
+    a = (C.c_uint32 * 3)(*bmin)
+    b = (C.c_uint32 * 3)(*bmax)
+    c0 = (C.c_double * 3)()
+    c1 = (C.c_double * 3)()
+    check(lib.s3r_index_box_world(level, a, b, c0, c1))
+    return np.array(c0[:]), np.array(c1[:])
+
+
+def make_color_transfer(xs, rgba, color_count: int) -> np.ndarray:
+    lib = _lib.load()
+    xs = np.ascontiguousarray(xs, dtype=np.float64)
+    rgba = np.ascontiguousarray(rgba, dtype=np.float64).reshape(-1, 4)
+    out = np.zeros((color_count, 4), dtype=np.float32)
+    check(lib.s3r_make_color_transfer(arr(xs, C.c_double), arr(rgba, C.c_double), xs.shape[0], color_count,
+                                      arr(out, C.c_float)))
+    return out
+
+
+def blend_image_part(dst: np.ndarray, src: np.ndarray, origin, just_copy: bool = False, offset=(0, 0)) -> None:
+    """blendImagePart on host ARGB32 images (uint32 arrays of shape (h, w)), in place on dst."""
+    lib = _lib.load()
+    assert dst.dtype == np.uint32 and src.dtype == np.uint32 and dst.flags.c_contiguous and src.flags.c_contiguous
+    check(lib.s3r_blend_image_part_host(arr(dst, C.c_uint32), dst.shape[1], dst.shape[0], arr(src, C.c_uint32),
+                                        src.shape[1], src.shape[0], int(origin[0]), int(origin[1]),
+                                        1 if just_copy else 0, int(offset[0]), int(offset[1])))

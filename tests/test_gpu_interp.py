@@ -1,0 +1,134 @@
+"""GPU dense interpolation through the C ABI vs the reference (golden) and the oracle."""
+import numpy as np
+import pytest
+
+import oracle
+from revise_gb300 import _lib, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _same(a, b):
+    return np.array_equal(np.isnan(a), np.isnan(b)) and np.array_equal(a[~np.isnan(a)], b[~np.isnan(b)])
+
+
+def _interp(ctx, n2i, sp, d):
+    import torch
+    from revise_gb300.api import to_device_n2i
+    out = ctx.interp_dense(to_device_n2i(n2i), torch.from_numpy(np.ascontiguousarray(sp, np.float32)).cuda(), d)
+    return out.cpu().numpy()
+
+
+def test_single_block_bit_exact_with_reference_golden(ctx, golden):
+    for name in golden["interp_names"]:
+        got = _interp(ctx, golden[f"interp_{name}_n2i"], golden[f"interp_{name}_sparse"],
+                      int(golden[f"interp_{name}_depth"]))
+        assert _same(got, golden[f"interp_{name}_dense"]), name
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_single_block_vs_oracle_and_fp64(ctx, seed):
+    w = workloads.small(seed=seed, level=1, depths=(1, 3, 5, 6), mask_fraction=0.2)
+    for b in range(w.nblocks):
+        n2i, sp = w.block_nodes(b)
+        d = int(w.blocks[b, 3])
+        got = _interp(ctx, n2i, sp, d)
+        assert _same(got, oracle.interp_f32(n2i, sp, d)), (seed, b)
+        f64 = oracle.interp_f64(n2i, sp, d)
+        assert np.array_equal(np.isnan(got), np.isnan(f64))
+        m = ~np.isnan(got)
+        # tolerance: 1e-6 relative to the value, floored at 1e-6 of the field scale
+        scale = np.abs(sp[sp != np.float32(1e30)]).max()
+        assert np.all(np.abs(got[m] - f64[m]) <= 1e-6 * np.maximum(np.abs(f64[m]), scale))
+
+
+def test_empty_node_list_gives_all_nan(ctx):
+    import torch
+    out = ctx.interp_dense(torch.zeros(0, dtype=torch.int16, device="cuda"),
+                           torch.zeros(0, dtype=torch.float32, device="cuda"), 3)
+    assert torch.isnan(out).all()
+
+
+def test_max_depth_linear_field_and_masked_corner(ctx):
+    # only the 8 root corners at depth 9 (513^3): a linear field is reproduced exactly
+    # up to rounding, and one masked corner masks the whole block
+    d = 9
+    s = 1 << d
+    n2i = np.array([[(i & 1) * s, ((i >> 1) & 1) * s, ((i >> 2) & 1) * s] for i in range(8)], np.uint16)
+    a, bx, by, bz = 0.25, 1.0, -2.0, 0.5
+    vals = (a + bx * n2i[:, 0] / s + by * n2i[:, 1] / s + bz * n2i[:, 2] / s).astype(np.float32)
+    got = _interp(ctx, n2i, vals, d).reshape(s + 1, s + 1, s + 1)
+    z, y, x = np.meshgrid(*[np.arange(0, s + 1, 64)] * 3, indexing="ij")
+    want = a + bx * x / s + by * y / s + bz * z / s
+    np.testing.assert_allclose(got[::64, ::64, ::64], want, atol=1e-5)
+    vals[3] = np.float32(1e30)
+    assert np.isnan(_interp(ctx, n2i, vals, d)).all()
+
+
+def test_depth_beyond_maximum_is_rejected(ctx, lib):
+    import ctypes as C
+    rc = lib.s3r_interp_dense(ctx.h, C.c_void_p(0), C.c_void_p(0), 0, 10, C.c_void_p(1), C.c_void_p(0))
+    assert rc == _lib.S3R_ERR_INVALID
+
+
+@pytest.mark.parametrize("tile", [8, 16, 32])
+def test_batched_plan_bit_exact_with_oracle(ctx, tile):
+    import torch
+    from revise_gb300.api import FramePlan
+    w = workloads.small(seed=11, level=1, depths=(1, 2, 3, 4, 5, 6), mask_fraction=0.2)
+    plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=tile)
+    plan.interp(torch.from_numpy(w.sparse).cuda())
+    torch.cuda.synchronize()
+    bricks, offs = plan.bricks()
+    got = bricks.cpu().numpy()
+    want = oracle.interp_workload(w)
+    assert _same(got, want)
+    plan.close()
+
+
+@pytest.mark.parametrize("fmt", [_lib.BRICK_F16, _lib.BRICK_BF16])
+def test_batched_16bit_bricks_decode_within_quantization(ctx, fmt):
+    import torch
+    from revise_gb300.api import FramePlan
+    w = workloads.small(seed=4, level=1, depths=(3, 4, 5), mask_fraction=0.1)
+    plan = FramePlan(ctx, w, fmt, tile_cells=16)
+    plan.interp(torch.from_numpy(w.sparse).cuda())
+    torch.cuda.synchronize()
+    bricks, offs = plan.bricks()
+    so = plan.brick_scales().cpu().numpy()
+    if fmt == _lib.BRICK_F16:
+        h = bricks.cpu().numpy().astype(np.float32)
+        rel = 2.0 ** -11
+    else:
+        h = (bricks.cpu().numpy().astype(np.uint32) << 16).view(np.float32)
+        rel = 2.0 ** -8
+    want = oracle.interp_workload(w)
+    for b in range(w.nblocks):
+        a, c = int(offs[b]), int(offs[b + 1])
+        dec = so[b, 1] + so[b, 0] * h[a:c]
+        ref = want[a:c]
+        assert np.array_equal(np.isnan(dec), np.isnan(ref))
+        m = ~np.isnan(ref)
+        assert np.all(np.abs(dec[m] - ref[m]) <= rel * so[b, 0] * 1.01 + 1e-6)
+    plan.close()
+
+
+def test_cfg3_full_size_plan_sampled_blocks(ctx):
+    """4096 blocks of depth 3..7 in one launch; a seeded sample of blocks against the oracle."""
+    import torch
+    from revise_gb300.api import FramePlan
+    w = workloads.cfg3()
+    plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=16)
+    plan.interp(torch.from_numpy(w.sparse).cuda())
+    torch.cuda.synchronize()
+    bricks, offs = plan.bricks()
+    rng = np.random.default_rng(0)
+    deep = np.flatnonzero(w.blocks[:, 3] == 7)[:3]
+    sample = np.concatenate([rng.choice(w.nblocks, 40, replace=False), deep])
+    for b in sample:
+        a, c = int(offs[b]), int(offs[b + 1])
+        n2i, sp = w.block_nodes(int(b))
+        assert _same(bricks[a:c].cpu().numpy(), oracle.interp_f32(n2i, sp, int(w.blocks[b, 3]))), b
+    # every vertex was written: NaN only where the oracle says so (checked above) and none left uninitialised
+    assert plan.info.vertices == w.vertices
+    plan.close()

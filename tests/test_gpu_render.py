@@ -1,0 +1,159 @@
+"""GPU ray casting through the C ABI vs the oracle: the plain per-block ARGB8
+path (reference arithmetic and quantization, <= 1 LSB) and the batched float
+path (vs the FP64 oracle, 2e-3 max abs per channel)."""
+import numpy as np
+import pytest
+
+import oracle
+from revise_gb300 import _lib, host, workloads
+
+pytestmark = pytest.mark.gpu
+
+TOL_IMAGE = 2e-3  # max abs per RGBA channel, float image vs the FP64 oracle
+
+
+def _dev(a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def _rects(w, view):
+    return np.array([host.block_view_rect(view, w.blocks[b, :3]) for b in range(w.nblocks)], np.int32)
+
+
+def _argb_diff(a, b):
+    a = a.view(np.uint8).reshape(-1, 4).astype(int)
+    b = b.view(np.uint8).reshape(-1, 4).astype(int)
+    return np.abs(a - b).max(axis=1)
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_plain_block_render_vs_oracle(ctx, seed):
+    import torch
+    w = workloads.small(seed=seed, level=1, depths=(2, 3, 4), W=80, H=60)
+    view = host.view_for(w)
+    ov = oracle.view_from(view)
+    dense = oracle.interp_workload(w)
+    vo = w.vertex_off
+    tf = _dev(w.tf)
+    vp = torch.zeros(w.W * w.H, dtype=torch.int32, device="cuda")
+    ref = np.zeros(w.W * w.H, np.uint32)
+    order = host.b2f_order([0, 0, 0], [2, 2, 2], [-5.0] * 3, [5.0] * 3, w.eye)
+    idx = {tuple(b[:3]): i for i, b in enumerate(w.blocks.tolist())}
+    for blk in order.tolist():
+        b = idx[tuple(blk)]
+        d = int(w.blocks[b, 3])
+        brick = dense[int(vo[b]):int(vo[b + 1])]
+        rect = host.block_view_rect(view, blk)
+        ctx.render_block_argb(view, _dev(brick), d, blk, rect, tf, vp)
+        oracle.render_block_argb8(ov, brick, d, blk, rect, w.tf, ref)
+    got = vp.cpu().numpy().view(np.uint32)
+    diff = _argb_diff(got, ref)
+    assert (ref >> 24).astype(bool).mean() > 0.05  # the image is not empty
+    assert diff.max() <= 1
+    assert (diff > 0).mean() < 0.02
+
+
+def test_worker_scene_part_vs_oracle(ctx):
+    from revise_gb300.api import RenderSharedState, VsWorker
+    w = workloads.small(seed=2, level=1, depths=(3, 4), W=96, H=72)
+    st = RenderSharedState(w)
+    wk = VsWorker(ctx)
+    wk.initialize()
+    wk.set_render_shared_state(st)
+    part = wk.render_scene_part(w.level, [0, 0, 0], [2, 2, 2])
+    ov = oracle.view_from(st.view)
+    ref = oracle.render_frame_argb8(ov, w, oracle.interp_workload(w), _rects(w, st.view), w.tf)
+    ref = ref.reshape(w.H, w.W)
+    ys, xs = np.nonzero(ref >> 24)
+    assert part.origin == (xs.min(), ys.min())
+    assert part.size == (xs.max() - xs.min() + 1, ys.max() - ys.min() + 1)
+    crop = ref[ys.min():ys.max() + 1, xs.min():xs.max() + 1]
+    diff = _argb_diff(part.pixels.ravel(), crop.ravel())
+    assert diff.max() <= 1 and (diff > 0).mean() < 0.02
+
+
+def _frame(ctx, w, fmt=_lib.BRICK_F32, alpha_stop=2.0, tile=16):
+    import torch
+    from revise_gb300.api import FramePlan
+    view = host.view_for(w, alpha_stop)
+    plan = FramePlan(ctx, w, fmt, tile_cells=tile)
+    sp = _dev(w.sparse)
+    tf = _dev(w.tf)
+    rgba = torch.zeros(w.W * w.H * 4, dtype=torch.float32, device="cuda")
+    argb = torch.zeros(w.W * w.H, dtype=torch.int32, device="cuda")
+    samples = torch.zeros(1, dtype=torch.int64, device="cuda")
+    plan.interp(sp)
+    plan.render(view, tf, rgba, argb, samples)
+    torch.cuda.synchronize()
+    return plan, view, rgba.cpu().numpy().reshape(-1, 4), argb.cpu().numpy().view(np.uint32), int(samples.item())
+
+
+@pytest.mark.parametrize("name", ["small", "cfg1"])
+def test_frame_render_vs_fp64_oracle(ctx, name):
+    w = workloads.small(seed=5, level=1, depths=(2, 3, 4, 5), W=96, H=64) if name == "small" else workloads.cfg1()
+    plan, view, img, argb, samples = _frame(ctx, w)
+    ov = oracle.view_from(view)
+    ref, flags = oracle.render_frame_f64(ov, w, oracle.interp_workload(w), _rects(w, view), w.tf)
+    assert ref[:, 3].max() > 0.1 and samples > 0
+    ok = flags == 0
+    err = np.abs(img - ref).max(axis=1)
+    assert err[ok].max() <= TOL_IMAGE, err[ok].max()
+    assert ok.mean() > 0.99
+    plan.close()
+
+
+def test_frame_render_cfg2_sampled_pixels(ctx):
+    """Full 1920x1080 cfg2 frame; a seeded sample of pixels against the FP64 oracle."""
+    w = workloads.cfg2()
+    plan, view, img, argb, samples = _frame(ctx, w)
+    ov = oracle.view_from(view)
+    hit = np.flatnonzero(img[:, 3] > 0)
+    assert hit.size > 1000
+    rng = np.random.default_rng(1)
+    sel = np.concatenate([rng.choice(hit, 1500, replace=False), rng.choice(img.shape[0], 200, replace=False)])
+    vx = sel % w.W
+    vy = w.H - 1 - sel // w.W
+    ref, flags = oracle.render_frame_f64(ov, w, oracle.interp_workload(w), _rects(w, view), w.tf,
+                                         np.stack([vx, vy], 1))
+    ok = flags == 0
+    err = np.abs(img[sel] - ref).max(axis=1)
+    assert err[ok].max() <= TOL_IMAGE, err[ok].max()
+    plan.close()
+
+
+def test_graph_replay_equals_direct_render(ctx):
+    import torch
+    from revise_gb300.api import FramePlan
+    w = workloads.small(seed=8, level=2, depths=(2, 3), W=64, H=48)
+    view = host.view_for(w)
+    plan = FramePlan(ctx, w)
+    sp, tf = _dev(w.sparse), _dev(w.tf)
+    a = torch.zeros(w.W * w.H * 4, device="cuda")
+    b = torch.zeros_like(a)
+    plan.interp(sp)
+    plan.render(view, tf, a)
+    for _ in range(3):
+        plan.run(view, sp, tf, b)
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)
+    plan.close()
+
+
+def test_alpha_stop_bounded_difference(ctx):
+    w = workloads.small(seed=6, level=2, depths=(2, 3), W=64, H=48)
+    _, _, full, _, s_full = _frame(ctx, w, alpha_stop=2.0)
+    _, _, cut, _, s_cut = _frame(ctx, w, alpha_stop=1.0 - 1e-4)
+    assert np.abs(full - cut).max() <= 2e-4
+    assert s_cut <= s_full
+
+
+@pytest.mark.parametrize("fmt", [_lib.BRICK_F16, _lib.BRICK_BF16])
+def test_16bit_bricks_image_error_is_bounded(ctx, fmt):
+    w = workloads.small(seed=9, level=1, depths=(3, 4, 5), W=96, H=64)
+    plan, view, img, _, _ = _frame(ctx, w, fmt=fmt)
+    ov = oracle.view_from(view)
+    ref, flags = oracle.render_frame_f64(ov, w, oracle.interp_workload(w), _rects(w, view), w.tf)
+    err = np.abs(img - ref)[flags == 0]
+    assert err.max() <= (0.02 if fmt == _lib.BRICK_F16 else 0.06)
+    plan.close()
