@@ -1,0 +1,38 @@
+"""The C++ drop-in adapters compile against the reference's own headers: the
+dense-field generator adapter instantiates BlockTreeFieldService<3>::interpolateWith
+(include/s3dmm/BlockTreeFieldService.hpp:118-145) for both dense containers."""
+import shutil
+import subprocess
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+REFERENCE = Path("/root/reference")
+
+SRC = r'''
+#include "s3dmm/BlockTreeFieldService.hpp"
+#include "DenseFieldInterpolatorGb300.hpp"
+using S = s3dmm::BlockTreeFieldService<3>;
+template void S::interpolateWith<s3dmm::DenseFieldInterpolatorGb300<std::vector<float>&>>(
+    s3dmm::Vec2<s3dmm::dfield_real>&, std::vector<float>&, unsigned int, unsigned int, const BlockId&,
+    s3dmm::FieldTimestamps*) const;
+template void S::interpolateWith<s3dmm::DenseFieldInterpolatorGb300<s3dmm::Gb300DenseField&>>(
+    s3dmm::Vec2<s3dmm::dfield_real>&, s3dmm::Gb300DenseField&, unsigned int, unsigned int, const BlockId&,
+    s3dmm::FieldTimestamps*) const;
+'''
+
+
+def test_dense_field_interpolator_adapter_compiles(tmp_path):
+    if not (REFERENCE / "include" / "s3dmm" / "BlockTreeFieldService.hpp").exists():
+        pytest.skip("reference headers not present")
+    cuda_inc = Path("/usr/local/cuda/include")
+    if not cuda_inc.exists() or not shutil.which("g++"):
+        pytest.skip("no toolchain")
+    src = tmp_path / "adapter_check.cpp"
+    src.write_text(SRC)
+    cmd = ["g++", "-std=c++20", "-fsyntax-only", "-DS3DMM_REAL_TYPE=float", "-DS3DMM_ENABLE_CUDA",
+           "-DS3DMM_PROGRESS_REPORT", f"-I{ROOT / 'oracle' / 'shims'}", f"-I{REFERENCE / 'include'}",
+           f"-I{ROOT / 'include'}", f"-I{ROOT / 'revise_gb300' / 'adapters'}", f"-I{cuda_inc}", str(src)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]

@@ -49,20 +49,35 @@ def test_empty_node_list_gives_all_nan(ctx):
     assert torch.isnan(out).all()
 
 
-def test_max_depth_linear_field_and_masked_corner(ctx):
-    # only the 8 root corners at depth 9 (513^3): a linear field is reproduced exactly
-    # up to rounding, and one masked corner masks the whole block
+def _root_corners(d):
+    s = 1 << d
+    return np.array([[(i & 1) * s, ((i >> 1) & 1) * s, ((i >> 2) & 1) * s] for i in range(8)], np.uint16)
+
+
+def test_max_depth_linear_field(ctx):
+    # only the 8 root corners at depth 9 (513^3 vertices): the midpoint scheme
+    # reproduces a linear field up to rounding
     d = 9
     s = 1 << d
-    n2i = np.array([[(i & 1) * s, ((i >> 1) & 1) * s, ((i >> 2) & 1) * s] for i in range(8)], np.uint16)
+    n2i = _root_corners(d)
     a, bx, by, bz = 0.25, 1.0, -2.0, 0.5
     vals = (a + bx * n2i[:, 0] / s + by * n2i[:, 1] / s + bz * n2i[:, 2] / s).astype(np.float32)
     got = _interp(ctx, n2i, vals, d).reshape(s + 1, s + 1, s + 1)
     z, y, x = np.meshgrid(*[np.arange(0, s + 1, 64)] * 3, indexing="ij")
     want = a + bx * x / s + by * y / s + bz * z / s
     np.testing.assert_allclose(got[::64, ::64, ::64], want, atol=1e-5)
+
+
+def test_masked_root_corner_at_depth_8(ctx):
+    # the no-field value spreads to every midpoint whose stencil reaches it, nowhere else
+    d = 8
+    n2i = _root_corners(d)
+    vals = np.linspace(-1, 1, 8).astype(np.float32)
     vals[3] = np.float32(1e30)
-    assert np.isnan(_interp(ctx, n2i, vals, d)).all()
+    got = _interp(ctx, n2i, vals, d)
+    want = oracle.interp_f32(n2i, vals, d)
+    assert _same(got, want)
+    assert 0 < np.isnan(got).mean() < 1
 
 
 def test_depth_beyond_maximum_is_rejected(ctx, lib):
