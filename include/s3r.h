@@ -89,6 +89,23 @@ uint64_t s3r_ctx_launch_count(const s3r_ctx* ctx);
 int s3r_interp_dense(s3r_ctx* ctx, const uint16_t* n2i_xyz, const float* sparse, uint32_t n, uint32_t depth,
                      float* dense, void* stream);
 
+/* Deepest subtree s3r_interp_dense_noalloc accepts: its scratch holds 129^3 floats (8.6 MB). */
+#define S3R_NOALLOC_MAX_DEPTH 7
+
+/* No counterpart in the reference.  The same interpolation as s3r_interp_dense
+ * (same arguments, bit-identical output) for callers that cannot call
+ * cudaMalloc -- applications whose device memory belongs to their own pool
+ * allocator or is reserved up front, and loops that must not stall on the
+ * device-wide synchronization of cudaMalloc/cudaFree.  It takes no context and
+ * allocates nothing: its scratch is a fixed 8.6 MB __device__ array that every
+ * GPU loading the library holds until exit.  depth > S3R_NOALLOC_MAX_DEPTH is
+ * rejected with S3R_ERR_INVALID.  All calls share the array: calls that overlap
+ * on the GPU race and must be ordered on one stream.  The first call on a device
+ * looks up the array's address there (make it before any stream capture).
+ * Errors: s3r_last_error(NULL). */
+int s3r_interp_dense_noalloc(const uint16_t* n2i_xyz, const float* sparse, uint32_t n, uint32_t depth, float* dense,
+                             void* stream);
+
 /* --------------------------------------------------------- camera / view */
 
 /* Renderer eye parameters (RenderKernelEyeParam, src/s3dmm_cuda/RenderKernelParam.hpp:56-65)

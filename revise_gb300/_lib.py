@@ -69,6 +69,7 @@ _SIGS = {
     "s3r_last_error": (C.c_char_p, [vp]),
     "s3r_ctx_launch_count": (C.c_uint64, [vp]),
     "s3r_interp_dense": (C.c_int, [vp, vp, vp, C.c_uint32, C.c_uint32, vp, vp]),
+    "s3r_interp_dense_noalloc": (C.c_int, [vp, vp, C.c_uint32, C.c_uint32, vp, vp]),
     "s3r_camera_look_at": (C.c_int, [f64p, f64p, f64p, C.c_double, C.c_uint32, C.c_uint32, C.c_int32,
                                      C.c_double, C.POINTER(Camera)]),
     "s3r_block_cube": (C.c_int, [C.c_uint32, u32p, f32p, f32p]),

@@ -511,6 +511,10 @@ int plan_launch_render(s3r_plan* p, const float* tf, float* rgba, uint32_t* argb
 
 } // namespace
 
+int s3r::record_error(int code, const char* msg) { return fail(nullptr, code, msg); }
+
+int s3r::record_cuda_error(cudaError_t e, const char* what) { return cuda_fail(nullptr, e, what); }
+
 // ==================================================================== C ABI
 
 extern "C" {

@@ -68,6 +68,10 @@ struct FrameArgs {
     float* ddense;
 };
 
+// Records a failure for s3r_last_error(NULL) and returns code (host.cpp).
+int record_error(int code, const char* msg);
+int record_cuda_error(cudaError_t e, const char* what);
+
 // Kernel launchers (defined in the .cu files); all return cudaGetLastError().
 cudaError_t launch_fill_f32(float* p, uint64_t n, float v, cudaStream_t s);
 cudaError_t launch_fill_u32(uint32_t* p, uint64_t n, uint32_t v, cudaStream_t s);
