@@ -55,7 +55,7 @@ struct s3r_plan {
     uint64_t* entry_off_dev = nullptr;
     uint16_t* entry_local_dev = nullptr;
     uint32_t* entry_node_dev = nullptr;
-    int32_t* coarse_dev = nullptr;
+    uint32_t* queue_dev = nullptr;
     uint64_t* node_off_dev = nullptr;
     float2* scale_offset_dev = nullptr;
     void* bricks = nullptr;
@@ -283,13 +283,11 @@ void plan_free_device(s3r_plan* p)
     f(p->entry_off_dev);
     f(p->entry_local_dev);
     f(p->entry_node_dev);
-    f(p->coarse_dev);
     p->blocks_dev = nullptr;
     p->items_dev = nullptr;
     p->entry_off_dev = nullptr;
     p->entry_local_dev = nullptr;
     p->entry_node_dev = nullptr;
-    p->coarse_dev = nullptr;
 }
 
 void plan_drop_graph(s3r_plan* p)
@@ -353,6 +351,33 @@ int plan_bin(s3r_plan* p, uint32_t tile_log2)
         lo = x == 0 ? 0 : (x - 1) / T;
         hi = std::min(x / T, m - 1);
     };
+    // Descent entries of every tile of block b: the sparse nodes on the 27
+    // points of each coarse cube containing the tile (level 0: all 27, deeper:
+    // the 19 midpoints), fn(tile, slot 27*level + point, node).  Needs the
+    // block's coarse grid complete.
+    auto for_descent = [&](uint32_t b, auto&& fn) {
+        const PlanBlock& B = pb[b];
+        const uint32_t L = B.coarse_log2;
+        if (L == 0) return;
+        const uint32_t m = 1u << L, m1 = m + 1;
+        for (uint32_t tz = 0; tz < m; ++tz)
+            for (uint32_t ty = 0; ty < m; ++ty)
+                for (uint32_t tx = 0; tx < m; ++tx) {
+                    const uint64_t t = tiles_off[b] + tx + m * (ty + m * tz);
+                    for (uint32_t l = 0; l < L; ++l) {
+                        const uint32_t cube = 1u << (L - l); // cube edge in tiles
+                        const uint32_t bx = tx & ~(cube - 1), by = ty & ~(cube - 1), bz = tz & ~(cube - 1);
+                        const uint32_t hc = cube >> 1;
+                        for (uint32_t q = 0; q < 27; ++q) {
+                            const uint32_t px = q % 3, py = (q / 3) % 3, pz = q / 9;
+                            if (l > 0 && !(px & 1) && !(py & 1) && !(pz & 1)) continue;
+                            const uint32_t gx = bx + hc * px, gy = by + hc * py, gz = bz + hc * pz;
+                            const int32_t node = coarse[B.coarse_off + gx + m1 * (gy + m1 * gz)];
+                            if (node >= 0) fn(t, 27 * l + q, node);
+                        }
+                    }
+                }
+    };
     // pass 1: counts and coarse grids
     parallel([&](uint32_t b) {
         const PlanBlock& B = pb[b];
@@ -371,6 +396,7 @@ int plan_bin(s3r_plan* p, uint32_t tile_log2)
                     for (uint32_t tx = xl; tx <= xh; ++tx)
                         ++count[tiles_off[b] + tx + m * (ty + m * tz)];
         }
+        for_descent(b, [&](uint64_t t, uint32_t, int32_t) { ++count[t]; });
     });
     // items: largest tiles first, then block order
     std::vector<uint64_t> order(ntiles);
@@ -422,6 +448,12 @@ int plan_bin(s3r_plan* p, uint32_t tile_log2)
                         node[e] = (uint32_t)(i - p->node_off[b]);
                     }
         }
+        const uint32_t E3 = E * E * E;
+        for_descent(b, [&](uint64_t t, uint32_t slot, int32_t nd) {
+            const uint64_t e = cursor[t]++;
+            local[e] = (uint16_t)(E3 + slot);
+            node[e] = (uint32_t)nd;
+        });
     });
     plan_free_device(p);
     int rc;
@@ -430,15 +462,12 @@ int plan_bin(s3r_plan* p, uint32_t tile_log2)
     if ((rc = upload(ctx, &p->entry_off_dev, entry_off))) return rc;
     if ((rc = upload(ctx, &p->entry_local_dev, local))) return rc;
     if ((rc = upload(ctx, &p->entry_node_dev, node))) return rc;
-    if ((rc = upload(ctx, &p->coarse_dev, coarse))) return rc;
     p->tile_log2 = tile_log2;
     p->tiles = ntiles;
     p->entries = nentries;
-    // persistent grid: resident CTAs on every SM
-    const uint32_t E = (1u << tile_log2) + 1u;
-    const size_t smem = (size_t)E * E * E * sizeof(float);
-    const uint32_t per_sm = std::max<uint32_t>(1, std::min<uint32_t>(8, (uint32_t)((227u * 1024u) / (smem + 1024))));
-    p->grid_ctas = (uint32_t)std::min<uint64_t>(ntiles, (uint64_t)ctx->sms * per_sm);
+    // persistent grid: the CTAs that fit on every SM at once, fed by the work queue
+    const uint32_t per_sm = interp_plan_ctas_per_sm(p->fmt, tile_log2);
+    p->grid_ctas = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(ntiles, (uint64_t)ctx->sms * per_sm));
     plan_drop_graph(p);
     return S3R_OK;
 }
@@ -482,10 +511,11 @@ int plan_launch_interp(s3r_plan* p, const float* sparse, cudaStream_t s, uint32_
     a.entry_off = p->entry_off_dev;
     a.entry_local = p->entry_local_dev;
     a.entry_node = p->entry_node_dev;
-    a.coarse_idx = p->coarse_dev;
     a.sparse = sparse;
+    a.queue = p->queue_dev;
     a.scale_offset = p->fmt == S3R_BRICK_F32 ? nullptr : p->scale_offset_dev;
     a.out = p->bricks;
+    S3R_CUDA(ctx, cudaMemsetAsync(p->queue_dev, 0, sizeof(uint32_t), s));
     S3R_CUDA(ctx, launch_interp_plan(a, p->fmt, p->tile_log2, p->grid_ctas, s));
     ++*kernels;
     return S3R_OK;
@@ -510,6 +540,17 @@ int plan_launch_render(s3r_plan* p, const float* tf, float* rgba, uint32_t* argb
 }
 
 } // namespace
+
+void s3r::block_sampling(uint32_t level, const uint32_t idx[3], uint32_t depth, RenderBlock& rb)
+{
+    block_cube_f(level, idx, rb.center, rb.half);
+    const uint32_t n = (1u << depth) + 1u;
+    rb.depth = depth;
+    rb.texel = 2 * rb.half / (float)n;
+    const double thalf = (double)rb.half + 0.5 * (double)rb.texel;
+    for (int d = 0; d < 3; ++d) rb.origin[d] = rb.center[d] - (float)thalf;
+    rb.factor = (float)((double)n / (2 * thalf));
+}
 
 int s3r::record_error(int code, const char* msg) { return fail(nullptr, code, msg); }
 
@@ -665,10 +706,10 @@ int s3r_render_block_argb(s3r_ctx* ctx, const s3r_view* view, const float* brick
     if (idx[0] >= m || idx[1] >= m || idx[2] >= m) return fail(ctx, S3R_ERR_INVALID, "block index outside level");
     if (rect[2] < 0 || rect[3] < 0) return fail(ctx, S3R_ERR_INVALID, "negative view rectangle");
     if ((rc = set_device(ctx))) return rc;
-    float c[3], h;
-    block_cube_f(view->level, idx, c, h);
-    S3R_CUDA(ctx, launch_render_block_argb(view, brick, depth, c, h, rect, view->W, view->H, tf, view->tf_n, viewport,
-                                           as_stream(stream)));
+    RenderBlock rb{};
+    block_sampling(view->level, idx, depth, rb);
+    for (int i = 0; i < 4; ++i) rb.rect[i] = rect[i];
+    S3R_CUDA(ctx, launch_render_block_argb(view, brick, rb, tf, viewport, as_stream(stream)));
     if (rect[2] > 0 && rect[3] > 0) ++ctx->launches;
     return S3R_OK;
 }
@@ -916,7 +957,7 @@ int s3r_frame_plan(s3r_ctx* ctx, const s3r_frame_desc* desc, s3r_plan** out)
         p->vertex_off[b + 1] = p->vertex_off[b] + e * e * e;
         RenderBlock& t = p->table_host[bl[0] + m * (bl[1] + m * bl[2])];
         if (t.depth != 0xffffffffu) return bail(fail(ctx, S3R_ERR_INVALID, "duplicate block index"));
-        t.depth = bl[3];
+        block_sampling(p->level, bl, bl[3], t);
         t.brick_off = p->vertex_off[b];
         t.block = b;
         const uint32_t lim = (uint32_t)(e - 1);
@@ -930,6 +971,8 @@ int s3r_frame_plan(s3r_ctx* ctx, const s3r_frame_desc* desc, s3r_plan** out)
     if ((e = cudaMalloc(&p->bricks, std::max<uint64_t>(p->vertices, 1) * esz)) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "cudaMalloc(bricks)"));
     if ((rc = upload(ctx, &p->node_off_dev, p->node_off))) return bail(rc);
+    if ((e = cudaMalloc(&p->queue_dev, sizeof(uint32_t))) != cudaSuccess)
+        return bail(cuda_fail(ctx, e, "cudaMalloc(queue)"));
     if ((e = cudaMalloc(&p->scale_offset_dev, sizeof(float2) * p->nblocks)) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "cudaMalloc(scales)"));
     if ((e = cudaMalloc(&p->table_dev, sizeof(RenderBlock) * p->table_host.size())) != cudaSuccess)
@@ -958,6 +1001,7 @@ int s3r_plan_destroy(s3r_plan* p)
     };
     f(p->bricks);
     f(p->node_off_dev);
+    f(p->queue_dev);
     f(p->scale_offset_dev);
     f(p->table_dev);
     f(p->view_dev);

@@ -62,188 +62,152 @@ template <typename OutT> struct Store;
 template <> struct Store<float> {
     __device__ static void put(float* out, uint64_t i, float v, float, float)
     {
-        out[i] = v == kNoField ? qnan() : v;
+        out[i] = isinf(v) ? qnan() : v;
     }
 };
 template <> struct Store<__half> {
     __device__ static void put(__half* out, uint64_t i, float v, float inv_scale, float offset)
     {
-        out[i] = (v == kNoField || isnan(v)) ? __ushort_as_half((unsigned short)0x7e00)
+        out[i] = (isinf(v) || isnan(v)) ? __ushort_as_half((unsigned short)0x7e00)
                                              : __float2half_rn((v - offset) * inv_scale);
     }
 };
 template <> struct Store<__nv_bfloat16> {
     __device__ static void put(__nv_bfloat16* out, uint64_t i, float v, float inv_scale, float offset)
     {
-        out[i] = (v == kNoField || isnan(v)) ? __ushort_as_bfloat16((unsigned short)0x7fc0)
+        out[i] = (isinf(v) || isnan(v)) ? __ushort_as_bfloat16((unsigned short)0x7fc0)
                                              : __float2bfloat16_rn((v - offset) * inv_scale);
     }
 };
 
-// Value of a coarse-lattice vertex for the descent: the sparse value there, or NaN.
-template <bool kGrid>
-__device__ __forceinline__ float coarse_value(const TileArgs& a, uint32_t gx, uint32_t gy, uint32_t gz, uint32_t e,
-                                              uint32_t k, uint32_t L, uint32_t coarse_off, uint64_t node_base)
-{
-    if constexpr (kGrid) {
-        return a.grid[((uint64_t)gz * e + gy) * e + gx];
-    } else {
-        uint32_t m1 = (1u << L) + 1u;
-        int32_t idx = a.coarse_idx[coarse_off + (gx >> k) + m1 * ((gy >> k) + m1 * (gz >> k))];
-        return idx < 0 ? qnan() : a.sparse[node_base + (uint32_t)idx];
-    }
-}
+// Internally a masked value is +inf: every stencil sum that touches it is
+// +inf, which reproduces the reference's rule "any no-field value in the
+// stencil gives the no-field value" without tests, and finite sums round as
+// before.  NaN keeps its meaning "not computed yet".
+__device__ __forceinline__ float to_internal(float v) { return v == kNoField ? __int_as_float(0x7f800000) : v; }
 
-__device__ __forceinline__ float mid2(float lo, float hi)
-{
-    return (lo == kNoField || hi == kNoField) ? kNoField : kHalf * (lo + hi);
-}
-__device__ __forceinline__ float mid4(float l1, float h1, float l2, float h2)
-{
-    return (l1 == kNoField || h1 == kNoField || l2 == kNoField || h2 == kNoField) ? kNoField
-                                                                                  : kQuarter * (l1 + h1 + l2 + h2);
-}
-__device__ __forceinline__ float mid6(float l1, float h1, float l2, float h2, float l3, float h3)
-{
-    return (l1 == kNoField || h1 == kNoField || l2 == kNoField || h2 == kNoField || l3 == kNoField ||
-            h3 == kNoField)
-               ? kNoField
-               : kSixth * (l1 + h1 + l2 + h2 + l3 + h3);
-}
+// Descent slots: 27 points (3x3x3, x fastest) per coarse level.
+constexpr int kMaxDescentLevels = S3R_MAX_DEPTH;
 
-// Warp 0: walk from the block's root corners down L levels to the 8 corners of
-// the tile at (ox, oy, oz) (vertex coordinates), writing them into the tile.
-template <bool kGrid>
-__device__ void descend(const TileArgs& a, float* s, float* c27, uint32_t d, uint32_t k, uint32_t L,
-                        uint32_t coarse_off, uint64_t node_base, uint32_t ox, uint32_t oy, uint32_t oz)
+// Warp 0: walk from the block's root corners down L levels, using the sparse
+// values already placed in desc[27*l + p] (NaN where no node), and write the
+// tile's 8 corners into the shared tile.
+__device__ void descend(float* s, float* desc, uint32_t d, uint32_t k, uint32_t L, uint32_t ox, uint32_t oy,
+                        uint32_t oz)
 {
     const uint32_t lane = threadIdx.x;
-    const uint32_t e = (1u << d) + 1u;
     const uint32_t T = 1u << k, E = T + 1u;
-    uint32_t size = 1u << d;
-    uint32_t gx0 = 0, gy0 = 0, gz0 = 0;
-    float corner = 0.f;
-    if (lane < 8)
-        corner = coarse_value<kGrid>(a, (lane & 1) ? size : 0, (lane & 2) ? size : 0, (lane & 4) ? size : 0, e, k, L,
-                                     coarse_off, node_base);
     const uint32_t px = lane % 3, py = (lane / 3) % 3, pz = lane / 9;
     const uint32_t nodd = (px & 1) + (py & 1) + (pz & 1);
+    uint32_t size = 1u << d, gx0 = 0, gy0 = 0, gz0 = 0;
+    float corner = 0.f;
     for (uint32_t l = 0; l < L; ++l) {
+        float* c27 = desc + 27 * l;
         const uint32_t hs = size >> 1;
-        const uint32_t src = lane < 27 ? (px >> 1) + 2 * (py >> 1) + 4 * (pz >> 1) : 0;
-        const float cv = __shfl_sync(0xffffffffu, corner, (int)src);
-        if (lane < 27)
-            c27[lane] = nodd == 0 ? cv
-                                  : coarse_value<kGrid>(a, gx0 + hs * px, gy0 + hs * py, gz0 + hs * pz, e, k, L,
-                                                        coarse_off, node_base);
+        if (l > 0) {
+            const uint32_t src = lane < 27 ? (px >> 1) + 2 * (py >> 1) + 4 * (pz >> 1) : 0;
+            const float cv = __shfl_sync(0xffffffffu, corner, (int)src);
+            if (lane < 27 && nodd == 0) c27[lane] = cv;
+        }
         __syncwarp();
         if (lane < 27 && nodd == 1 && isnan(c27[lane])) {
             const uint32_t st = (px & 1) ? 1 : ((py & 1) ? 3 : 9);
-            c27[lane] = mid2(c27[lane - st], c27[lane + st]);
+            c27[lane] = kHalf * (c27[lane - st] + c27[lane + st]);
         }
         __syncwarp();
         if (lane < 27 && nodd == 2 && isnan(c27[lane])) {
-            // the two odd axes, ascending
-            const uint32_t s1 = (px & 1) ? 1 : 3;
+            const uint32_t s1 = (px & 1) ? 1 : 3; // the two odd axes, ascending
             const uint32_t s2 = (pz & 1) ? 9 : 3;
-            c27[lane] = mid4(c27[lane - s1], c27[lane + s1], c27[lane - s2], c27[lane + s2]);
+            c27[lane] = kQuarter * (c27[lane - s1] + c27[lane + s1] + c27[lane - s2] + c27[lane + s2]);
         }
         __syncwarp();
         if (lane == 13 && isnan(c27[13]))
-            c27[13] = mid6(c27[12], c27[14], c27[10], c27[16], c27[4], c27[22]);
+            c27[13] = kSixth * (c27[12] + c27[14] + c27[10] + c27[16] + c27[4] + c27[22]);
         __syncwarp();
         const uint32_t qx = (ox - gx0) >= hs ? 1u : 0u;
         const uint32_t qy = (oy - gy0) >= hs ? 1u : 0u;
         const uint32_t qz = (oz - gz0) >= hs ? 1u : 0u;
-        if (lane < 8)
-            corner = c27[(qx + (lane & 1)) + 3 * (qy + ((lane >> 1) & 1)) + 9 * (qz + (lane >> 2))];
+        if (lane < 8) corner = c27[(qx + (lane & 1)) + 3 * (qy + ((lane >> 1) & 1)) + 9 * (qz + (lane >> 2))];
         gx0 += qx * hs;
         gy0 += qy * hs;
         gz0 += qz * hs;
         size = hs;
         __syncwarp();
     }
-    if (lane < 8)
-        s[(lane & 1) * T + E * (((lane >> 1) & 1) * T + E * ((lane >> 2) * T))] = corner;
+    if (lane < 8) s[(lane & 1) * T + E * (((lane >> 1) & 1) * T + E * ((lane >> 2) * T))] = corner;
 }
 
-// The k fine levels of one tile of 2^k cells held in shared memory (edge E = 2^k+1).
-__device__ void fine_levels(float* s, uint32_t k)
+// One level of one tile: every cube of the level (2^j per axis) is handled by
+// one thread, which reads its 27 points (8 corners known from the coarser
+// levels, 19 midpoints holding a sparse value or NaN), fills the NaN midpoints
+// in registers (edges, then faces, then the centre) and writes back the
+// midpoints it owns: those with every coordinate on the cube's low side or
+// middle, plus the far side where the cube is the last along that axis.
+// Midpoints shared with a neighbour are computed by both from the same values,
+// so a neighbour reading one while it is written reads the same number.
+__device__ __forceinline__ void cube_level(float* s, uint32_t E, uint32_t T, uint32_t j)
 {
-    const uint32_t T = 1u << k, E = T + 1u;
-    const uint32_t stride[3] = {1u, E, E * E};
-    for (uint32_t j = 0; j < k; ++j) {
-        const uint32_t m = 1u << j, sz = T >> j, hs = sz >> 1;
-        const uint32_t m1 = m + 1;
-        // edges: odd along axis a only
-        {
-            const uint32_t per = m * m1 * m1, cnt = 3 * per;
-            for (uint32_t idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
-                const uint32_t a = idx / per;
-                uint32_t r = idx - a * per;
-                const uint32_t i = r & (m - 1);
-                r >>= j;
-                const uint32_t jb = r % m1, jc = r / m1;
-                uint32_t c[3];
-                c[a] = hs + sz * i;
-                c[(a + 1) % 3] = sz * jb;
-                c[(a + 2) % 3] = sz * jc;
-                const uint32_t p = c[0] + E * (c[1] + E * c[2]);
-                if (isnan(s[p])) {
-                    const uint32_t st = hs * stride[a];
-                    s[p] = mid2(s[p - st], s[p + st]);
-                }
+    const uint32_t m = 1u << j, sz = T >> j, hs = sz >> 1;
+    const uint32_t st0 = hs, st1 = E * hs, st2 = E * E * hs;
+    const uint32_t ncubes = 1u << (3 * j);
+    for (uint32_t c = threadIdx.x; c < ncubes; c += blockDim.x) {
+        const uint32_t ci = c & (m - 1), cj = (c >> j) & (m - 1), ck = c >> (2 * j);
+        const uint32_t base = ci * sz + E * (cj * sz + E * (ck * sz));
+        float v[27];
+#pragma unroll
+        for (int p = 0; p < 27; ++p) v[p] = s[base + (p % 3) * st0 + ((p / 3) % 3) * st1 + (p / 9) * st2];
+#pragma unroll
+        for (int p = 0; p < 27; ++p) {
+            const int a = p % 3, b = (p / 3) % 3, cc = p / 9;
+            if ((a & 1) + (b & 1) + (cc & 1) == 1 && isnan(v[p])) {
+                const int st = (a & 1) ? 1 : ((b & 1) ? 3 : 9);
+                v[p] = kHalf * (v[p - st] + v[p + st]);
             }
         }
-        __syncthreads();
-        // faces: even along axis a, odd along the other two
-        {
-            const uint32_t per = m1 * m * m, cnt = 3 * per;
-            for (uint32_t idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
-                const uint32_t a = idx / per;
-                uint32_t r = idx - a * per;
-                const uint32_t ia = r % m1;
-                r /= m1;
-                const uint32_t ib = r & (m - 1), ic = r >> j;
-                const uint32_t b = a == 0 ? 1u : 0u, cax = a == 2 ? 1u : 2u;
-                uint32_t c[3];
-                c[a] = sz * ia;
-                c[b] = hs + sz * ib;
-                c[cax] = hs + sz * ic;
-                const uint32_t p = c[0] + E * (c[1] + E * c[2]);
-                if (isnan(s[p])) {
-                    const uint32_t sb = hs * stride[b], sc = hs * stride[cax];
-                    s[p] = mid4(s[p - sb], s[p + sb], s[p - sc], s[p + sc]);
-                }
+#pragma unroll
+        for (int p = 0; p < 27; ++p) {
+            const int a = p % 3, b = (p / 3) % 3, cc = p / 9;
+            if ((a & 1) + (b & 1) + (cc & 1) == 2 && isnan(v[p])) {
+                const int s1 = (a & 1) ? 1 : 3;
+                const int s2 = (cc & 1) ? 9 : 3;
+                v[p] = kQuarter * (v[p - s1] + v[p + s1] + v[p - s2] + v[p + s2]);
             }
         }
-        __syncthreads();
-        // cells
-        {
-            const uint32_t cnt = m * m * m;
-            for (uint32_t idx = threadIdx.x; idx < cnt; idx += blockDim.x) {
-                const uint32_t x = hs + sz * (idx & (m - 1));
-                const uint32_t y = hs + sz * ((idx >> j) & (m - 1));
-                const uint32_t z = hs + sz * (idx >> (2 * j));
-                const uint32_t p = x + E * (y + E * z);
-                if (isnan(s[p])) {
-                    const uint32_t s0 = hs, s1 = hs * E, s2 = hs * E * E;
-                    s[p] = mid6(s[p - s0], s[p + s0], s[p - s1], s[p + s1], s[p - s2], s[p + s2]);
-                }
-            }
+        if (isnan(v[13])) v[13] = kSixth * (v[12] + v[14] + v[10] + v[16] + v[4] + v[22]);
+        const bool lx = ci == m - 1, ly = cj == m - 1, lz = ck == m - 1;
+#pragma unroll
+        for (int p = 0; p < 27; ++p) {
+            const int a = p % 3, b = (p / 3) % 3, cc = p / 9;
+            if ((a & 1) + (b & 1) + (cc & 1) == 0) continue;
+            if ((a < 2 || lx) && (b < 2 || ly) && (cc < 2 || lz))
+                s[base + a * st0 + b * st1 + cc * st2] = v[p];
         }
-        __syncthreads();
     }
+}
+
+// Shared tile of (2^k+1)^3 floats, rounded up to whole float4s for the vector fill.
+inline size_t tile_smem_bytes(uint32_t tile_log2)
+{
+    const size_t E = (1u << tile_log2) + 1u;
+    return ((E * E * E + 3) / 4) * 16;
 }
 
 template <bool kGrid, typename OutT>
 __global__ void __launch_bounds__(kInterpThreads) interp_tiles_kernel(TileArgs a)
 {
-    extern __shared__ float s[];
-    __shared__ float c27[32];
+    extern __shared__ float4 s_tile[]; // tile_smem_bytes(): (2^k+1)^3 floats rounded up to whole float4s
+    float* s = reinterpret_cast<float*>(s_tile);
+    __shared__ float desc[27 * kMaxDescentLevels];
+    __shared__ uint32_t item_s;
     const uint32_t nitems = a.nitems;
-    for (uint32_t item = blockIdx.x; item < nitems; item += gridDim.x) {
-        uint32_t d, k, L, tile, coarse_off = 0;
+    // Work items come from the queue counter when there is one (zeroed before
+    // the launch), else item blockIdx.x once per CTA.
+    for (uint32_t iter = 0;; ++iter) {
+        if (threadIdx.x == 0) item_s = a.queue ? atomicAdd(a.queue, 1u) : (iter == 0 ? blockIdx.x : nitems);
+        __syncthreads();
+        const uint32_t item = item_s;
+        if (item >= nitems) break;
+        uint32_t d, k, L, tile;
         uint64_t node_base = 0, dense_off = 0;
         uint32_t blk = 0;
         if constexpr (kGrid) {
@@ -259,7 +223,6 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tiles_kernel(TileArgs a
             d = b.depth;
             k = b.tile_log2;
             L = b.coarse_log2;
-            coarse_off = b.coarse_off;
             node_base = b.node_base;
             dense_off = b.dense_off;
         }
@@ -269,31 +232,49 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tiles_kernel(TileArgs a
         const uint32_t ox = tx * T, oy = ty * T, oz = tz * T;
         const uint32_t e = (1u << d) + 1u;
 
-        // 1. nodes into the shared tile
+        // 1. the tile's sparse values (NaN elsewhere) and the descent's
         if constexpr (kGrid) {
             for (uint32_t p = threadIdx.x; p < E3; p += blockDim.x) {
                 const uint32_t lx = p % E, r = p / E, ly = r % E, lz = r / E;
-                s[p] = a.grid[((uint64_t)(oz + lz) * e + (oy + ly)) * e + (ox + lx)];
+                s[p] = to_internal(a.grid[((uint64_t)(oz + lz) * e + (oy + ly)) * e + (ox + lx)]);
+            }
+            // descent points: level l's cube containing the tile, 27 points each
+            for (uint32_t q = threadIdx.x; q < 27 * L; q += blockDim.x) {
+                const uint32_t l = q / 27, p = q % 27;
+                const uint32_t size = 1u << (d - l), hs = size >> 1;
+                const uint32_t bx = ox & ~(size - 1), by = oy & ~(size - 1), bz = oz & ~(size - 1);
+                const uint32_t gx = bx + hs * (p % 3), gy = by + hs * ((p / 3) % 3), gz = bz + hs * (p / 9);
+                desc[q] = to_internal(a.grid[((uint64_t)gz * e + gy) * e + gx]);
             }
         } else {
-            for (uint32_t p = threadIdx.x; p < E3; p += blockDim.x)
-                s[p] = qnan();
+            {
+                const float4 nan4 = make_float4(qnan(), qnan(), qnan(), qnan());
+                float4* s4 = reinterpret_cast<float4*>(s);
+                for (uint32_t p = threadIdx.x; p < (E3 + 3) / 4; p += blockDim.x) s4[p] = nan4;
+            }
+            for (uint32_t q = threadIdx.x; q < 27 * L; q += blockDim.x) desc[q] = __int_as_float(0x7fc00000);
             __syncthreads();
             const uint64_t b0 = a.entry_off[item], b1 = a.entry_off[item + 1];
-            for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x)
-                s[a.entry_local[i]] = a.sparse[node_base + a.entry_node[i]];
+            for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
+                const uint32_t loc = a.entry_local[i];
+                const float v = to_internal(a.sparse[node_base + a.entry_node[i]]);
+                if (loc < E3) s[loc] = v;
+                else desc[loc - E3] = v;
+            }
         }
         __syncthreads();
 
         // 2. tile corners from the coarse levels
         if (L > 0) {
-            if (threadIdx.x < 32)
-                descend<kGrid>(a, s, c27, d, k, L, coarse_off, node_base, ox, oy, oz);
+            if (threadIdx.x < 32) descend(s, desc, d, k, L, ox, oy, oz);
             __syncthreads();
         }
 
-        // 3. fine levels
-        fine_levels(s, k);
+        // 3. fine levels, one barrier each
+        for (uint32_t j = 0; j < k; ++j) {
+            cube_level(s, E, T, j);
+            __syncthreads();
+        }
 
         // 4. owned vertices to HBM: [0, T) per axis, plus the far face on the last tile
         float inv_scale = 1.f, offset = 0.f;
@@ -305,17 +286,21 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tiles_kernel(TileArgs a
             }
         }
         OutT* out = reinterpret_cast<OutT*>(a.out) + dense_off;
-        const uint32_t OX = T + (tx == mL - 1 ? 1u : 0u);
         const uint32_t OY = T + (ty == mL - 1 ? 1u : 0u);
         const uint32_t OZ = T + (tz == mL - 1 ? 1u : 0u);
-        const uint32_t rows = OY * OZ;
-        const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-        for (uint32_t row = warp; row < rows; row += nwarps) {
-            const uint32_t ly = row % OY, lz = row / OY;
-            const uint64_t g = ((uint64_t)(oz + lz) * e + (oy + ly)) * e + ox;
-            const uint32_t sp = E * (ly + E * lz);
-            for (uint32_t lx = lane; lx < OX; lx += 32)
+        const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+        // rows of T values along x: 32/T rows per warp step (T <= 32), no divisions
+        const uint32_t per = T < 32 ? 32u / T : 1u;
+        const uint32_t lx = lane & (T - 1), sub = T < 32 ? lane >> k : 0u;
+        const bool far_x = tx == mL - 1; // the last tile along x also writes its x = T column
+        for (uint32_t lz = 0; lz < OZ; ++lz) {
+            const uint64_t gz = (uint64_t)(oz + lz) * e;
+            for (uint32_t ly = warp * per + sub; ly < OY; ly += nwarps * per) {
+                const uint64_t g = (gz + (oy + ly)) * e + ox;
+                const uint32_t sp = E * (ly + E * lz);
                 Store<OutT>::put(out, g + lx, s[sp + lx], inv_scale, offset);
+                if (far_x && lx == 0) Store<OutT>::put(out, g + T, s[sp + T], inv_scale, offset);
+            }
         }
         __syncthreads();
     }
@@ -369,8 +354,7 @@ inline uint32_t ctas_for(uint64_t n, uint32_t threads)
 template <bool kGrid, typename OutT>
 cudaError_t launch_tiles(const TileArgs& a, uint32_t tile_log2_max, uint32_t grid_ctas, cudaStream_t s)
 {
-    const uint32_t E = (1u << tile_log2_max) + 1u;
-    const size_t smem = (size_t)E * E * E * sizeof(float);
+    const size_t smem = tile_smem_bytes(tile_log2_max);
     auto kern = interp_tiles_kernel<kGrid, OutT>;
     if (smem > 48 * 1024) {
         cudaError_t err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -413,6 +397,24 @@ cudaError_t launch_interp_grid(const float* grid, uint32_t depth, float* dense, 
     a.out = dense;
     if (launches) ++*launches;
     return launch_tiles<true, float>(a, a.grid_tile_log2, a.nitems, s);
+}
+
+uint32_t interp_plan_ctas_per_sm(uint32_t fmt, uint32_t tile_log2)
+{
+    const size_t smem = tile_smem_bytes(tile_log2);
+    int n = 0;
+    cudaError_t e = cudaErrorInvalidValue;
+    auto occ = [&](auto kern) {
+        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, kInterpThreads, smem);
+    };
+    switch (fmt) {
+    case S3R_BRICK_F32: occ(interp_tiles_kernel<false, float>); break;
+    case S3R_BRICK_F16: occ(interp_tiles_kernel<false, __half>); break;
+    case S3R_BRICK_BF16: occ(interp_tiles_kernel<false, __nv_bfloat16>); break;
+    default: break;
+    }
+    return (e == cudaSuccess && n > 0) ? (uint32_t)n : 1u;
 }
 
 cudaError_t launch_interp_plan(const TileArgs& a, uint32_t fmt, uint32_t tile_log2_max, uint32_t grid_ctas,

@@ -67,20 +67,13 @@ __device__ __forceinline__ void pixel_ray(const s3r_view& v, uint32_t vx, uint32
     }
 }
 
-__device__ __forceinline__ void block_cube(uint32_t level, uint32_t ix, uint32_t iy, uint32_t iz, float c[3],
-                                           float& h)
-{
-    h = __fdiv_rn(kTopHalf, (float)(1u << level));
-    c[0] = __fadd_rn(-kTopHalf, __fmul_rn(h, (float)(1u + (ix << 1))));
-    c[1] = __fadd_rn(-kTopHalf, __fmul_rn(h, (float)(1u + (iy << 1))));
-    c[2] = __fadd_rn(-kTopHalf, __fmul_rn(h, (float)(1u + (iz << 1))));
-}
-
 // Slab test and sample set-up (DenseFieldRenderer_cu.cu:81-181). Returns true
 // when the block is rendered for this ray.
-__device__ __forceinline__ bool block_ray(const s3r_view& v, const float org[3], const float dir[3], const float c[3],
-                                          float h, uint32_t depth, BlockRay& r)
+__device__ __forceinline__ bool block_ray(const s3r_view& v, const float org[3], const float dir[3],
+                                          const RenderBlock& rb, BlockRay& r)
 {
+    const float* c = rb.center;
+    const float h = rb.half;
     float te = 1.f, tx = 0.f;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -104,8 +97,8 @@ __device__ __forceinline__ bool block_ray(const s3r_view& v, const float org[3],
     r.tau_enter = te;
     r.tau_exit = tx;
     if (!(tx > te)) return false;
-    const uint32_t n = (1u << depth) + 1u;
-    const float texel = __fdiv_rn(__fmul_rn(2.f, h), (float)n);
+    const uint32_t n = (1u << rb.depth) + 1u;
+    const float texel = rb.texel;
     const float span = __fsub_rn(tx, te);
     const float dotr = __fadd_rn(__fadd_rn(__fmul_rn(dir[0], dir[0]), __fmul_rn(dir[1], dir[1])),
                                  __fmul_rn(dir[2], dir[2]));
@@ -119,11 +112,9 @@ __device__ __forceinline__ bool block_ray(const s3r_view& v, const float org[3],
         r.step[d] = __fmul_rn(dir[d], dtau);
         r.p0[d] = __fadd_rn(org[d], __fmul_rn(dir[d], te));
     }
-    const double thalf = __dadd_rn((double)h, __dmul_rn(0.5, (double)texel));
 #pragma unroll
-    for (int d = 0; d < 3; ++d)
-        r.origin[d] = __fsub_rn(c[d], (float)thalf);
-    r.factor = (float)__ddiv_rn((double)n, __dmul_rn(2.0, thalf));
+    for (int d = 0; d < 3; ++d) r.origin[d] = rb.origin[d];
+    r.factor = rb.factor;
     r.n = n;
     r.samples = s;
     return true;
@@ -241,11 +232,11 @@ __device__ __forceinline__ uint32_t rgba_to_argb(float4 c)
 
 // ---------------------------------------------------------------- plain form
 
-__global__ void render_block_argb_kernel(const s3r_view v, const float* __restrict__ brick,
-                                         uint32_t depth, float cx, float cy, float cz, float h, int32_t rx,
-                                         int32_t ry, int32_t rw, int32_t rh, const float4* __restrict__ tf_g,
-                                         uint32_t* __restrict__ viewport)
+__global__ void render_block_argb_kernel(const s3r_view v, const float* __restrict__ brick, const RenderBlock rb,
+                                         const float4* __restrict__ tf_g, uint32_t* __restrict__ viewport)
 {
+    const uint32_t depth = rb.depth;
+    const int32_t rx = rb.rect[0], ry = rb.rect[1], rw = rb.rect[2], rh = rb.rect[3];
     extern __shared__ float4 tf[];
     for (uint32_t i = threadIdx.y * blockDim.x + threadIdx.x; i < v.tf_n; i += blockDim.x * blockDim.y)
         tf[i] = tf_g[i];
@@ -257,9 +248,8 @@ __global__ void render_block_argb_kernel(const s3r_view v, const float* __restri
     if (vx >= v.W || vy >= v.H) return;
     float org[3], dir[3];
     pixel_ray(v, vx, vy, org, dir);
-    const float c[3] = {cx, cy, cz};
     BlockRay r;
-    if (!block_ray(v, org, dir, c, h, depth, r)) return;
+    if (!block_ray(v, org, dir, rb, r)) return;
     const float span = v.field_max - v.field_min;
     const float of = (v.threshold - v.field_min) / span;
     const float il = layer_exponent(depth, v.level, v.quality);
@@ -325,41 +315,52 @@ __device__ __forceinline__ void walk_blocks(const float org[3], const float dir[
         }
     }
     if (!(t1 > t0)) return;
-    const float tm = 0.5f * (t0 + fminf(t1, t0 + cell));
-    int ci[3], stp[3];
-    float tmax[3], tdel[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const float p = __fmaf_rn(dir[a], t0, org[a]);
+    // start cell: the one holding the entry point itself (clamped onto the grid);
+    // starting any distance inside would skip the first block's segment on rays
+    // that enter close to a block boundary
+    const float tm = t0;
+    // start cell, step direction, next boundary crossing and crossing period per axis
+    int c0, c1, c2, s0, s1, s2;
+    float tx0, tx1, tx2, td0, td1, td2;
+    auto setup = [&](int a, int& c, int& st, float& tmax, float& tdel) {
         const float pm = __fmaf_rn(dir[a], tm, org[a]);
-        (void)p;
-        int c = (int)floorf((pm + kTopHalf) / cell);
-        c = min(max(c, 0), m - 1);
-        ci[a] = c;
+        c = min(max((int)floorf((pm + kTopHalf) / cell), 0), m - 1);
         if (dir[a] > 1e-10f) {
-            stp[a] = 1;
-            tmax[a] = ((-kTopHalf + cell * (float)(c + 1)) - org[a]) / dir[a];
-            tdel[a] = cell / dir[a];
+            st = 1;
+            tmax = ((-kTopHalf + cell * (float)(c + 1)) - org[a]) / dir[a];
+            tdel = cell / dir[a];
         } else if (dir[a] < -1e-10f) {
-            stp[a] = -1;
-            tmax[a] = ((-kTopHalf + cell * (float)c) - org[a]) / dir[a];
-            tdel[a] = -cell / dir[a];
+            st = -1;
+            tmax = ((-kTopHalf + cell * (float)c) - org[a]) / dir[a];
+            tdel = -cell / dir[a];
         } else {
-            stp[a] = 0;
-            tmax[a] = 3.4e38f;
-            tdel[a] = 3.4e38f;
+            st = 0;
+            tmax = 3.4e38f;
+            tdel = 3.4e38f;
         }
-    }
+    };
+    setup(0, c0, s0, tx0, td0);
+    setup(1, c1, s1, tx1, td1);
+    setup(2, c2, s2, tx2, td2);
     for (int guard = 0; guard < 3 * m + 3; ++guard) {
-        const uint32_t b = (uint32_t)ci[0] + (uint32_t)m * ((uint32_t)ci[1] + (uint32_t)m * (uint32_t)ci[2]);
-        if (!f(b, (uint32_t)ci[0], (uint32_t)ci[1], (uint32_t)ci[2])) return;
-        int a = 0;
-        if (tmax[1] < tmax[a]) a = 1;
-        if (tmax[2] < tmax[a]) a = 2;
-        if (tmax[a] >= t1) return;
-        ci[a] += stp[a];
-        if (ci[a] < 0 || ci[a] >= m) return;
-        tmax[a] += tdel[a];
+        const uint32_t b = (uint32_t)c0 + (uint32_t)m * ((uint32_t)c1 + (uint32_t)m * (uint32_t)c2);
+        if (!f(b, (uint32_t)c0, (uint32_t)c1, (uint32_t)c2)) return;
+        if (tx0 <= tx1 && tx0 <= tx2) {
+            if (tx0 >= t1) return;
+            c0 += s0;
+            if (c0 < 0 || c0 >= m) return;
+            tx0 += td0;
+        } else if (tx1 <= tx2) {
+            if (tx1 >= t1) return;
+            c1 += s1;
+            if (c1 < 0 || c1 >= m) return;
+            tx1 += td1;
+        } else {
+            if (tx2 >= t1) return;
+            c2 += s2;
+            if (c2 < 0 || c2 >= m) return;
+            tx2 += td2;
+        }
     }
 }
 
@@ -426,10 +427,8 @@ __global__ void frame_render_kernel(FrameArgs fa)
             const int4 rc = *reinterpret_cast<const int4*>(rb->rect);
             const int32_t rca[4] = {rc.x, rc.y, rc.z, rc.w};
             if (!pixel_in_rect(rca, vx, vy)) return true;
-            float c[3], h;
-            block_cube(v.level, ix, iy, iz, c, h);
             BlockRay r;
-            if (!block_ray(v, org, dir, c, h, depth, r)) return true;
+            if (!block_ray(v, org, dir, *rb, r)) return true;
             const char* base = reinterpret_cast<const char*>(fa.bricks);
             const size_t esz = Fmt == S3R_BRICK_F32 ? 4 : 2;
             float scale = 1.f, offset = 0.f;
@@ -508,6 +507,18 @@ __global__ void frame_backward_kernel(FrameArgs fa)
             const float of = (v.threshold - v.field_min) / span;
             float T = 1.f, Cpre[3] = {0.f, 0.f, 0.f};
             float accA = 0.f;
+            uint32_t tf_i0 = 0xffffffffu, tf_i1 = 0xffffffffu;
+            float tf_a[4] = {0.f, 0.f, 0.f, 0.f}, tf_b[4] = {0.f, 0.f, 0.f, 0.f};
+            auto flush_tf = [&]() {
+                if (tf_i0 == 0xffffffffu) return;
+#pragma unroll
+                for (int ch = 0; ch < 4; ++ch) {
+                    if (tf_a[ch] != 0.f) atomicAdd(&dtf_s[4 * tf_i0 + ch], tf_a[ch]);
+                    if (tf_b[ch] != 0.f) atomicAdd(&dtf_s[4 * tf_i1 + ch], tf_b[ch]);
+                    tf_a[ch] = 0.f;
+                    tf_b[ch] = 0.f;
+                }
+            };
             walk_blocks(org, dir, v.level, [&](uint32_t b, uint32_t ix, uint32_t iy, uint32_t iz) {
                 const RenderBlock* rb = &fa.table[b];
                 const uint32_t depth = rb->depth;
@@ -515,10 +526,8 @@ __global__ void frame_backward_kernel(FrameArgs fa)
                 const int4 rc = *reinterpret_cast<const int4*>(rb->rect);
                 const int32_t rca[4] = {rc.x, rc.y, rc.z, rc.w};
                 if (!pixel_in_rect(rca, vx, vy)) return true;
-                float c[3], h;
-                block_cube(v.level, ix, iy, iz, c, h);
                 BlockRay r;
-                if (!block_ray(v, org, dir, c, h, depth, r)) return true;
+                if (!block_ray(v, org, dir, *rb, r)) return true;
                 const float* brick = reinterpret_cast<const float*>(fa.bricks) + rb->brick_off;
                 float* gdense = fa.ddense + rb->brick_off;
                 const float il = layer_exponent(depth, v.level, v.quality);
@@ -550,12 +559,19 @@ __global__ void frame_backward_kernel(FrameArgs fa)
                     }
                     g_a += gA * (1.f - A) * inv_om;
                     g_col[3] = g_a * dadc;
-                    // transfer-function table
+                    // transfer-function table: consecutive samples of a ray usually fall
+                    // between the same two entries; accumulate them in registers and
+                    // flush to shared memory when the pair changes
                     const float f = ts.f;
+                    if (ts.i0 != tf_i0 || ts.i1 != tf_i1) {
+                        flush_tf();
+                        tf_i0 = ts.i0;
+                        tf_i1 = ts.i1;
+                    }
 #pragma unroll
                     for (int ch = 0; ch < 4; ++ch) {
-                        atomicAdd(&dtf_s[4 * ts.i0 + ch], g_col[ch] * (1.f - f));
-                        atomicAdd(&dtf_s[4 * ts.i1 + ch], g_col[ch] * f);
+                        tf_a[ch] = __fmaf_rn(g_col[ch], 1.f - f, tf_a[ch]);
+                        tf_b[ch] = __fmaf_rn(g_col[ch], f, tf_b[ch]);
                     }
                     // dense values
                     if (!ts.clamped) {
@@ -582,6 +598,7 @@ __global__ void frame_backward_kernel(FrameArgs fa)
                 accA = __fmaf_rn(__fsub_rn(1.f, accA), Ab, accA);
                 return !(accA > v.alpha_stop);
             });
+            flush_tf();
         }
     }
     __syncthreads();
@@ -593,18 +610,14 @@ __global__ void frame_backward_kernel(FrameArgs fa)
 
 } // namespace
 
-cudaError_t launch_render_block_argb(const s3r_view* view_host, const float* brick, uint32_t depth, const float center[3],
-                                     float half, const int32_t rect[4], uint32_t W, uint32_t H, const float* tf,
-                                     uint32_t tf_n, uint32_t* viewport, cudaStream_t s)
+cudaError_t launch_render_block_argb(const s3r_view* view_host, const float* brick, const RenderBlock& rb,
+                                     const float* tf, uint32_t* viewport, cudaStream_t s)
 {
-    (void)W;
-    (void)H;
-    if (rect[2] <= 0 || rect[3] <= 0) return cudaSuccess;
+    if (rb.rect[2] <= 0 || rb.rect[3] <= 0) return cudaSuccess;
     dim3 block(16, 8);
-    dim3 grid((rect[2] + 15) / 16, (rect[3] + 7) / 8);
-    render_block_argb_kernel<<<grid, block, tf_n * sizeof(float4), s>>>(
-        *view_host, brick, depth, center[0], center[1], center[2], half, rect[0], rect[1], rect[2], rect[3],
-        reinterpret_cast<const float4*>(tf), viewport);
+    dim3 grid((rb.rect[2] + 15) / 16, (rb.rect[3] + 7) / 8);
+    render_block_argb_kernel<<<grid, block, view_host->tf_n * sizeof(float4), s>>>(
+        *view_host, brick, rb, reinterpret_cast<const float4*>(tf), viewport);
     return cudaGetLastError();
 }
 

@@ -9,7 +9,7 @@
 namespace s3r {
 
 constexpr float kNoField = S3R_NO_FIELD_VALUE;
-constexpr int kInterpThreads = 256;
+constexpr int kInterpThreads = 128;
 
 // One block of a batched plan, as the interpolation kernel reads it.
 struct PlanBlock {
@@ -32,10 +32,11 @@ struct TileArgs {
     const uint64_t* entry_off;    // nitems+1 prefix offsets into local/node
     const uint16_t* entry_local;  // node position inside its tile (x + e*(y + e*z), e = 2^k+1)
     const uint32_t* entry_node;   // node index within its block
-    const int32_t* coarse_idx;    // per block coarse lattice: node index or -1
+    // entry_local >= (2^k+1)^3 addresses descent slot 27*level + point instead of the tile
     const float* sparse;          // node values
     const float2* scale_offset;   // per block {scale, offset} for 16-bit bricks
     void* out;                    // brick store
+    uint32_t* queue;              // work-queue counter, zeroed before the launch (nullptr: one item per CTA)
     // single-block form
     const float* grid;
     uint32_t grid_depth;
@@ -44,13 +45,22 @@ struct TileArgs {
 
 // Per-block entry of the render block table (dense over the (2^level)^3 block grid).
 struct RenderBlock {
-    uint32_t depth;  // 0xffffffff: no block here
-    uint32_t fmt;    // S3R_BRICK_*
+    uint32_t depth;    // 0xffffffff: no block here
+    uint32_t fmt;      // S3R_BRICK_*
     uint64_t brick_off;
-    int32_t rect[4]; // view rectangle {x, y, w, h}
-    uint32_t block;  // index into the plan's block list (per-brick scale/offset)
-    uint32_t pad[3];
+    int32_t rect[4];   // view rectangle {x, y, w, h}
+    float center[3];   // cube centre and half size (DenseFieldRenderer_cu.cu:337-350)
+    float half;
+    float origin[3];   // texture-space origin: centre - (half + texel/2)  (:176-180)
+    float factor;      // world -> texel scale n / (2 (half + texel/2))     (:181)
+    float texel;       // 2 half / n                                         (:169)
+    uint32_t block;    // index into the plan's block list (per-brick scale/offset)
+    uint32_t pad[2];
 };
+
+// Per-block sampling constants of DenseFieldRenderer_cu.cu:168-181, with the
+// reference's mix of float and double arithmetic (host.cpp).
+void block_sampling(uint32_t level, const uint32_t idx[3], uint32_t depth, RenderBlock& rb);
 
 struct FrameArgs {
     const s3r_view* view;          // device copy
@@ -80,12 +90,12 @@ cudaError_t launch_scatter_nodes(float* grid, uint32_t depth, const uint16_t* n2
 cudaError_t launch_interp_grid(const float* grid, uint32_t depth, float* dense, cudaStream_t s, uint32_t* launches);
 cudaError_t launch_interp_plan(const TileArgs& a, uint32_t fmt, uint32_t tile_log2_max, uint32_t grid_ctas,
                                cudaStream_t s);
+uint32_t interp_plan_ctas_per_sm(uint32_t fmt, uint32_t tile_log2);
 cudaError_t launch_block_ranges(const PlanBlock* blocks, uint32_t nblocks, const float* sparse,
                                 const uint64_t* node_off_dev, float2* scale_offset, cudaStream_t s);
 
-cudaError_t launch_render_block_argb(const s3r_view* view_host, const float* brick, uint32_t depth, const float center[3],
-                                     float half, const int32_t rect[4], uint32_t W, uint32_t H, const float* tf,
-                                     uint32_t tf_n, uint32_t* viewport, cudaStream_t s);
+cudaError_t launch_render_block_argb(const s3r_view* view_host, const float* brick, const RenderBlock& rb,
+                                     const float* tf, uint32_t* viewport, cudaStream_t s);
 cudaError_t launch_frame_render(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, uint32_t fmt,
                                 uint32_t tile_shape, cudaStream_t s);
 cudaError_t launch_frame_backward(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, cudaStream_t s);

@@ -18,7 +18,7 @@ def _setup(W, H):
     return w
 
 
-def _gpu_grad(ctx, w, target_img):
+def _gpu_grad(ctx, w, target_img, keep=None):
     import torch
     from revise_gb300.api import FramePlan
     view = host.view_for(w)
@@ -30,6 +30,8 @@ def _gpu_grad(ctx, w, target_img):
     plan.render(view, tf, rgba)
     tgt = torch.from_numpy(np.ascontiguousarray(target_img, np.float32).ravel()).cuda()
     dl = rgba - tgt
+    if keep is not None:  # pixels whose sample sets float and FP64 arithmetic agree on
+        dl = dl * torch.from_numpy(np.repeat(keep.astype(np.float32), 4)).cuda()
     dtf = torch.zeros(w.tf.size, device="cuda")
     bricks, offs = plan.bricks()
     dd = torch.zeros(bricks.numel(), device="cuda")
@@ -45,14 +47,22 @@ def _rects(w, view):
 
 
 def test_adjoint_matches_fp64_gradient(ctx):
+    """Pixels where a block-local early-termination test lands within 1e-5 of its
+    threshold (the FP64 oracle flags them) are left out of both gradients: there
+    float and FP64 arithmetic may keep different sample sets."""
     w = _setup(160, 160)
     view = host.view_for(w)
     ov = oracle.view_from(view)
     dense = oracle.interp_workload(w)
     rects = _rects(w, view)
     target, _ = oracle.render_frame_f64(ov, w, dense, rects, w.meta["target_tf"])
-    loss64, dtf64, dd64 = oracle.render_frame_grad_f64(ov, w, dense, rects, w.tf, target)
-    view, loss, dtf, dd = _gpu_grad(ctx, w, target)
+    _, flags = oracle.render_frame_f64(ov, w, dense, rects, w.tf)
+    keep = flags == 0
+    assert keep.mean() > 0.97
+    p = np.arange(w.W * w.H)[keep]
+    pixels = np.stack([p % w.W, w.H - 1 - p // w.W], 1)
+    loss64, dtf64, dd64 = oracle.render_frame_grad_f64(ov, w, dense, rects, w.tf, target[keep], pixels)
+    view, loss, dtf, dd = _gpu_grad(ctx, w, target, keep)
     assert abs(loss - loss64) <= 1e-4 * loss64
     e_tf = np.linalg.norm(dtf - dtf64) / np.linalg.norm(dtf64)
     m = ~np.isnan(dense)

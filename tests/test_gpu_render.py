@@ -103,6 +103,21 @@ def test_frame_render_vs_fp64_oracle(ctx, name):
     plan.close()
 
 
+def test_frame_render_opaque_tf_keeps_entry_segments(ctx):
+    """With a nearly opaque transfer function the first samples of a ray decide its
+    colour, so a ray that skipped the short first segment of a block it enters
+    near a block boundary would differ by far more than the tolerance."""
+    w = workloads.small(seed=12, level=2, depths=(2, 3), W=128, H=96, mask_fraction=0.0, eye=(7.0, 9.0, 16.0))
+    t = np.linspace(0, 1, 256)
+    w.tf = np.stack([t, 1 - t, 0.5 + 0 * t, 0.9 + 0.1 * t], 1).astype(np.float32)
+    plan, view, img, _, _ = _frame(ctx, w)
+    ov = oracle.view_from(view)
+    ref, flags = oracle.render_frame_f64(ov, w, oracle.interp_workload(w), _rects(w, view), w.tf)
+    err = np.abs(img - ref).max(axis=1)[flags == 0]
+    assert err.max() <= TOL_IMAGE, err.max()
+    plan.close()
+
+
 def test_frame_render_cfg2_sampled_pixels(ctx):
     """Full 1920x1080 cfg2 frame; a seeded sample of pixels against the FP64 oracle."""
     w = workloads.cfg2()
