@@ -61,6 +61,8 @@ struct s3r_plan {
     void* bricks = nullptr;
     RenderBlock* table_dev = nullptr;
     s3r_view* view_dev = nullptr;
+    int32_t* cover_dev = nullptr;    // union of the present blocks' view rectangles {x0, y0, x1, y1}
+    int32_t* cover_pinned = nullptr;
     uint32_t grid_ctas = 0;
     // host render table (rects depend on the view)
     std::vector<RenderBlock> table_host;
@@ -444,7 +446,7 @@ int plan_bin(s3r_plan* p, uint32_t tile_log2)
                     for (uint32_t tx = xl; tx <= xh; ++tx) {
                         const uint64_t t = tiles_off[b] + tx + m * (ty + m * tz);
                         const uint64_t e = cursor[t]++;
-                        local[e] = (uint16_t)((x - tx * T) + E * ((y - ty * T) + E * (z - tz * T)));
+                        local[e] = (uint16_t)tile_offset(T, x - tx * T, y - ty * T, z - tz * T);
                         node[e] = (uint32_t)(i - p->node_off[b]);
                     }
         }
@@ -482,11 +484,22 @@ int plan_stage_view(s3r_plan* p, const s3r_view* view, cudaStream_t s)
     const uint32_t m = 1u << p->level;
     RenderBlock* tb = p->table_pinned;
     std::memcpy(tb, p->table_host.data(), sizeof(RenderBlock) * p->table_host.size());
+    int32_t cover[4] = {INT32_MAX, INT32_MAX, INT32_MIN, INT32_MIN};
     for (uint32_t b = 0; b < p->nblocks; ++b) {
         const uint32_t* bl = &p->blocks[4 * b];
         const uint32_t cell = bl[0] + m * (bl[1] + m * bl[2]);
-        view_rect(*view, bl, tb[cell].rect);
+        int32_t* r = tb[cell].rect;
+        view_rect(*view, bl, r);
+        if (r[2] > 0 && r[3] > 0) {
+            cover[0] = std::min(cover[0], r[0]);
+            cover[1] = std::min(cover[1], r[1]);
+            cover[2] = std::max(cover[2], r[0] + r[2]);
+            cover[3] = std::max(cover[3], r[1] + r[3]);
+        }
     }
+    if (cover[0] > cover[2]) cover[0] = cover[1] = cover[2] = cover[3] = 0;
+    std::memcpy(p->cover_pinned, cover, sizeof(cover));
+    S3R_CUDA(ctx, cudaMemcpyAsync(p->cover_dev, p->cover_pinned, sizeof(cover), cudaMemcpyHostToDevice, s));
     *p->view_pinned = *view;
     S3R_CUDA(ctx, cudaMemcpyAsync(p->table_dev, tb, sizeof(RenderBlock) * p->table_host.size(),
                                   cudaMemcpyHostToDevice, s));
@@ -533,6 +546,7 @@ int plan_launch_render(s3r_plan* p, const float* tf, float* rgba, uint32_t* argb
     fa.argb = argb;
     fa.samples = samples;
     fa.scale_offset = p->fmt == S3R_BRICK_F32 ? nullptr : p->scale_offset_dev;
+    fa.cover = p->cover_dev;
     S3R_CUDA(p->ctx, launch_frame_render(fa, p->last_view.W, p->last_view.H, p->last_view.tf_n, p->fmt,
                                          p->render_tile, s));
     ++*kernels;
@@ -983,6 +997,10 @@ int s3r_frame_plan(s3r_ctx* ctx, const s3r_frame_desc* desc, s3r_plan** out)
         return bail(cuda_fail(ctx, e, "cudaMallocHost(table)"));
     if ((e = cudaMallocHost(&p->view_pinned, sizeof(s3r_view))) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "cudaMallocHost(view)"));
+    if ((e = cudaMalloc(&p->cover_dev, 4 * sizeof(int32_t))) != cudaSuccess)
+        return bail(cuda_fail(ctx, e, "cudaMalloc(cover)"));
+    if ((e = cudaMallocHost(&p->cover_pinned, 4 * sizeof(int32_t))) != cudaSuccess)
+        return bail(cuda_fail(ctx, e, "cudaMallocHost(cover)"));
     if ((e = cudaEventCreateWithFlags(&p->staged, cudaEventDisableTiming)) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "cudaEventCreate"));
     if ((rc = plan_bin(p, tl))) return bail(rc);
@@ -1007,6 +1025,8 @@ int s3r_plan_destroy(s3r_plan* p)
     f(p->view_dev);
     if (p->table_pinned) cudaFreeHost(p->table_pinned);
     if (p->view_pinned) cudaFreeHost(p->view_pinned);
+    if (p->cover_pinned) cudaFreeHost(p->cover_pinned);
+    f(p->cover_dev);
     if (p->staged) cudaEventDestroy(p->staged);
     delete p;
     return S3R_OK;

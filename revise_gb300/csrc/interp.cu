@@ -90,13 +90,12 @@ __device__ __forceinline__ float to_internal(float v) { return v == kNoField ? _
 constexpr int kMaxDescentLevels = S3R_MAX_DEPTH;
 
 // Warp 0: walk from the block's root corners down L levels, using the sparse
-// values already placed in desc[27*l + p] (NaN where no node), and write the
-// tile's 8 corners into the shared tile.
-__device__ void descend(float* s, float* desc, uint32_t d, uint32_t k, uint32_t L, uint32_t ox, uint32_t oy,
-                        uint32_t oz)
+// values already placed in desc[27*l + p] (NaN where no node); lanes 0-7 return
+// the tile's 8 corners.
+__device__ float descend(float* desc, uint32_t d, uint32_t k, uint32_t L, uint32_t ox, uint32_t oy, uint32_t oz)
 {
+    (void)k;
     const uint32_t lane = threadIdx.x;
-    const uint32_t T = 1u << k, E = T + 1u;
     const uint32_t px = lane % 3, py = (lane / 3) % 3, pz = lane / 9;
     const uint32_t nodd = (px & 1) + (py & 1) + (pz & 1);
     uint32_t size = 1u << d, gx0 = 0, gy0 = 0, gz0 = 0;
@@ -134,7 +133,7 @@ __device__ void descend(float* s, float* desc, uint32_t d, uint32_t k, uint32_t 
         size = hs;
         __syncwarp();
     }
-    if (lane < 8) s[(lane & 1) * T + E * (((lane >> 1) & 1) * T + E * ((lane >> 2) * T))] = corner;
+    return corner; // lanes 0-7: corner (lane&1, lane>>1&1, lane>>2) of the tile
 }
 
 // One level of one tile: every cube of the level (2^j per axis) is handled by
@@ -150,6 +149,7 @@ __device__ __forceinline__ void cube_level(float* s, uint32_t E, uint32_t T, uin
     const uint32_t m = 1u << j, sz = T >> j, hs = sz >> 1;
     const uint32_t st0 = hs, st1 = E * hs, st2 = E * E * hs;
     const uint32_t ncubes = 1u << (3 * j);
+#pragma unroll 1
     for (uint32_t c = threadIdx.x; c < ncubes; c += blockDim.x) {
         const uint32_t ci = c & (m - 1), cj = (c >> j) & (m - 1), ck = c >> (2 * j);
         const uint32_t base = ci * sz + E * (cj * sz + E * (ck * sz));
@@ -192,8 +192,209 @@ inline size_t tile_smem_bytes(uint32_t tile_log2)
     return ((E * E * E + 3) / 4) * 16;
 }
 
+// Parity-split layout of a tile of T cells (T even): vertex (x, y, z) lives in
+// sub-array c = (x&1) | (y&1)<<1 | (z&1)<<2 at (x>>1) + nx*((y>>1) + ny*(z>>1)),
+// with nx = T/2 along an odd axis and T/2+1 along an even one.  At the finest
+// level every class of midpoints then sits in its own dense array, so a warp
+// walking one class touches consecutive words (no bank conflicts), and the
+// even sub-array is the same problem at half resolution for the coarser levels.
+template <uint32_t T> struct SplitTile {
+    static constexpr uint32_t H = T / 2, G = T / 2 + 1;
+    __host__ __device__ static constexpr uint32_t n(uint32_t odd) { return odd ? H : G; }
+    __host__ __device__ static constexpr uint32_t size(uint32_t c) { return n(c & 1) * n((c >> 1) & 1) * n((c >> 2) & 1); }
+    // sum of the sizes of classes 0 .. c-1 (sizes G^3, HG^2, HG^2, H^2G, HG^2, H^2G, H^2G, H^3)
+    __host__ __device__ static constexpr uint32_t base(uint32_t c)
+    {
+        constexpr uint32_t G3 = G * G * G, HG2 = H * G * G, H2G = H * H * G;
+        return (c >= 1 ? G3 : 0) + (c >= 2 ? HG2 : 0) + (c >= 3 ? HG2 : 0) + (c >= 4 ? H2G : 0) +
+               (c >= 5 ? HG2 : 0) + (c >= 6 ? H2G : 0) + (c >= 7 ? H2G : 0);
+    }
+    // element (i, j, k) of class c
+    __host__ __device__ static constexpr uint32_t idx(uint32_t c, uint32_t i, uint32_t j, uint32_t k)
+    {
+        return base(c) + i + n(c & 1) * (j + n((c >> 1) & 1) * k);
+    }
+    __host__ __device__ static constexpr uint32_t at(uint32_t x, uint32_t y, uint32_t z)
+    {
+        return idx((x & 1) | ((y & 1) << 1) | ((z & 1) << 2), x >> 1, y >> 1, z >> 1);
+    }
+};
+
+// The finest level of a tile in the split layout: one thread per 2x2x2 cube
+// (H^3 cubes), reading its 27 points -- corners from the even sub-array, the
+// 19 midpoint slots (a sparse value or NaN) from their class sub-arrays --
+// filling the NaN midpoints in registers (edges, faces, centre; stencil sums in
+// the reference's order) and writing back the ones it owns (low side and
+// middle, plus the far side on the last cube along an axis).  A warp's 32 cubes
+// are consecutive along x within each class row, so every load and store is a
+// run of consecutive words.
+template <uint32_t T> __device__ __forceinline__ void finest_level(float* s)
+{
+    using S = SplitTile<T>;
+    constexpr uint32_t H = S::H;
+    constexpr uint32_t lh = (H >= 2) ? (31 - __builtin_clz(H)) : 0;
+    constexpr uint32_t ncubes = H * H * H;
+#pragma unroll 1
+    for (uint32_t c = threadIdx.x; c < ncubes; c += blockDim.x) {
+        const uint32_t ci = c & (H - 1), cj = (c >> lh) & (H - 1), ck = c >> (2 * lh);
+        float v[27];
+#pragma unroll
+        for (int p = 0; p < 27; ++p) {
+            const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
+            const uint32_t cls = (a & 1) | ((b & 1) << 1) | ((cc & 1) << 2);
+            v[p] = s[S::idx(cls, ci + (a >> 1), cj + (b >> 1), ck + (cc >> 1))];
+        }
+#pragma unroll
+        for (int p = 0; p < 27; ++p) {
+            const int a = p % 3, b = (p / 3) % 3, cc = p / 9;
+            if ((a & 1) + (b & 1) + (cc & 1) == 1 && isnan(v[p])) {
+                const int st = (a & 1) ? 1 : ((b & 1) ? 3 : 9);
+                v[p] = kHalf * (v[p - st] + v[p + st]);
+            }
+        }
+#pragma unroll
+        for (int p = 0; p < 27; ++p) {
+            const int a = p % 3, b = (p / 3) % 3, cc = p / 9;
+            if ((a & 1) + (b & 1) + (cc & 1) == 2 && isnan(v[p])) {
+                const int s1 = (a & 1) ? 1 : 3;
+                const int s2 = (cc & 1) ? 9 : 3;
+                v[p] = kQuarter * (v[p - s1] + v[p + s1] + v[p - s2] + v[p + s2]);
+            }
+        }
+        if (isnan(v[13])) v[13] = kSixth * (v[12] + v[14] + v[10] + v[16] + v[4] + v[22]);
+        const bool lx = ci == H - 1, ly = cj == H - 1, lz = ck == H - 1;
+#pragma unroll
+        for (int p = 0; p < 27; ++p) {
+            const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
+            if ((a & 1) + (b & 1) + (cc & 1) == 0) continue;
+            if ((a < 2 || lx) && (b < 2 || ly) && (cc < 2 || lz)) {
+                const uint32_t cls = (a & 1) | ((b & 1) << 1) | ((cc & 1) << 2);
+                s[S::idx(cls, ci + (a >> 1), cj + (b >> 1), ck + (cc >> 1))] = v[p];
+            }
+        }
+    }
+    __syncthreads();
+}
+
+struct TileItem {
+    uint32_t d, k, L, tx, ty, tz, blk;
+    uint64_t node_base, dense_off;
+    uint32_t item;
+};
+
+// One tile of T = 2^k cells.  Tiles of T >= 2 use the split layout; T = 1
+// (depth-0 blocks) is a plain 2x2x2 copy of the root corners.
+template <uint32_t T, bool kGrid, typename OutT>
+__device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* desc, const TileItem& t)
+{
+    constexpr uint32_t E = T + 1, E3 = E * E * E;
+    using S = SplitTile<T < 2 ? 2 : T>;
+    auto at = [](uint32_t x, uint32_t y, uint32_t z) -> uint32_t {
+        if constexpr (T < 2) return x + 2 * (y + 2 * z);
+        else return S::at(x, y, z);
+    };
+    const uint32_t d = t.d, L = t.L;
+    const uint32_t ox = t.tx * T, oy = t.ty * T, oz = t.tz * T;
+    const uint32_t e = (1u << d) + 1u;
+    // 1. the tile's sparse values (NaN elsewhere) and the descent's
+    if constexpr (kGrid) {
+#pragma unroll 1
+        for (uint32_t p = threadIdx.x; p < E3; p += blockDim.x) {
+            const uint32_t lx = p % E, r = p / E, ly = r % E, lz = r / E;
+            s[at(lx, ly, lz)] = to_internal(a.grid[((uint64_t)(oz + lz) * e + (oy + ly)) * e + (ox + lx)]);
+        }
+        for (uint32_t q = threadIdx.x; q < 27 * L; q += blockDim.x) {
+            const uint32_t l = q / 27, p = q % 27;
+            const uint32_t size = 1u << (d - l), hs = size >> 1;
+            const uint32_t bx = ox & ~(size - 1), by = oy & ~(size - 1), bz = oz & ~(size - 1);
+            const uint32_t gx = bx + hs * (p % 3), gy = by + hs * ((p / 3) % 3), gz = bz + hs * (p / 9);
+            desc[q] = to_internal(a.grid[((uint64_t)gz * e + gy) * e + gx]);
+        }
+    } else {
+        {
+            const float4 nan4 = make_float4(qnan(), qnan(), qnan(), qnan());
+            float4* s4 = reinterpret_cast<float4*>(s);
+#pragma unroll 1
+            for (uint32_t p = threadIdx.x; p < (E3 + 3) / 4; p += blockDim.x) s4[p] = nan4;
+        }
+        for (uint32_t q = threadIdx.x; q < 27 * L; q += blockDim.x) desc[q] = qnan();
+        __syncthreads();
+        const uint64_t b0 = a.entry_off[t.item], b1 = a.entry_off[t.item + 1];
+        for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
+            const uint32_t loc = a.entry_local[i];
+            const float v = to_internal(a.sparse[t.node_base + a.entry_node[i]]);
+            if (loc < E3) s[loc] = v;
+            else desc[loc - E3] = v;
+        }
+    }
+    __syncthreads();
+    // 2. tile corners from the coarse levels
+    if (L > 0) {
+        if (threadIdx.x < 32) {
+            float corner = descend(desc, d, t.k, L, ox, oy, oz);
+            if (threadIdx.x < 8) {
+                const uint32_t c = threadIdx.x;
+                s[at((c & 1) * T, ((c >> 1) & 1) * T, (c >> 2) * T)] = corner;
+            }
+        }
+        __syncthreads();
+    }
+    // 3. levels: the coarser ones on the even sub-array (a tile of T/2 cells), then the finest
+    if constexpr (T >= 2) {
+        constexpr uint32_t kk = (T >= 2) ? (31 - __builtin_clz(T)) : 0;
+        for (uint32_t j = 0; j + 1 < kk; ++j) {
+            cube_level(s, S::G, S::H, j);
+            __syncthreads();
+        }
+        finest_level<T>(s);
+    }
+    // 4. owned vertices to HBM: [0, T) per axis, plus the far side on the last tiles
+    float inv_scale = 1.f, offset = 0.f;
+    if constexpr (!kGrid) {
+        if (a.scale_offset) {
+            const float2 so = a.scale_offset[t.blk];
+            inv_scale = 1.f / so.x;
+            offset = so.y;
+        }
+    }
+    const uint32_t mL = 1u << L;
+    OutT* out = reinterpret_cast<OutT*>(a.out) + t.dense_off;
+    const uint32_t OY = T + (t.ty == mL - 1 ? 1u : 0u);
+    const uint32_t OZ = T + (t.tz == mL - 1 ? 1u : 0u);
+    const bool far_x = t.tx == mL - 1;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    constexpr uint32_t per = T < 32 ? 32u / T : 1u; // rows per warp step
+    const uint32_t lx = lane & (T - 1), sub = T < 32 ? lane / T : 0u;
+    // A lane keeps its x; its rows keep their y parity (the row step is even),
+    // so only z's parity changes: two sub-array bases per lane.
+    const uint32_t y0 = warp * per + sub;
+    static_assert(kInterpThreads % 64 == 0, "the row step must stay even");
+    uint32_t base_z[2] = {0, 0}, nx = 0, nxy = 0;
+    if constexpr (T >= 2) {
+        const uint32_t xo = lx & 1, yo = y0 & 1;
+        nx = xo ? S::H : S::G;
+        nxy = nx * (yo ? S::H : S::G);
+        base_z[0] = S::idx(xo | (yo << 1), lx >> 1, 0, 0);
+        base_z[1] = S::idx(xo | (yo << 1) | 4, lx >> 1, 0, 0);
+    }
+#pragma unroll 1
+    for (uint32_t lz = 0; lz < OZ; ++lz) {
+        const uint64_t gz = (uint64_t)(oz + lz) * e;
+        const uint32_t bz = base_z[lz & 1] + nxy * (lz >> 1);
+#pragma unroll 1
+        for (uint32_t ly = y0; ly < OY; ly += nwarps * per) {
+            const uint64_t g = (gz + (oy + ly)) * e + ox;
+            uint32_t sp;
+            if constexpr (T >= 2) sp = bz + nx * (ly >> 1);
+            else sp = at(lx, ly, lz);
+            Store<OutT>::put(out, g + lx, s[sp], inv_scale, offset);
+            if (far_x && lx == 0) Store<OutT>::put(out, g + T, s[at(T, ly, lz)], inv_scale, offset);
+        }
+    }
+}
+
 template <bool kGrid, typename OutT>
-__global__ void __launch_bounds__(kInterpThreads) interp_tiles_kernel(TileArgs a)
+__global__ void __launch_bounds__(kInterpThreads, 8) interp_tiles_kernel(TileArgs a)
 {
     extern __shared__ float4 s_tile[]; // tile_smem_bytes(): (2^k+1)^3 floats rounded up to whole float4s
     float* s = reinterpret_cast<float*>(s_tile);
@@ -207,100 +408,39 @@ __global__ void __launch_bounds__(kInterpThreads) interp_tiles_kernel(TileArgs a
         __syncthreads();
         const uint32_t item = item_s;
         if (item >= nitems) break;
-        uint32_t d, k, L, tile;
-        uint64_t node_base = 0, dense_off = 0;
-        uint32_t blk = 0;
+        TileItem t;
+        uint32_t tile;
+        t.item = item;
+        t.blk = 0;
+        t.node_base = 0;
+        t.dense_off = 0;
         if constexpr (kGrid) {
-            d = a.grid_depth;
-            k = a.grid_tile_log2 < d ? a.grid_tile_log2 : d;
-            L = d - k;
+            t.d = a.grid_depth;
+            t.k = a.grid_tile_log2 < t.d ? a.grid_tile_log2 : t.d;
+            t.L = t.d - t.k;
             tile = item;
         } else {
             const uint2 it = a.items[item];
-            blk = it.x;
+            t.blk = it.x;
             tile = it.y;
-            const PlanBlock b = a.blocks[blk];
-            d = b.depth;
-            k = b.tile_log2;
-            L = b.coarse_log2;
-            node_base = b.node_base;
-            dense_off = b.dense_off;
+            const PlanBlock b = a.blocks[t.blk];
+            t.d = b.depth;
+            t.k = b.tile_log2;
+            t.L = b.coarse_log2;
+            t.node_base = b.node_base;
+            t.dense_off = b.dense_off;
         }
-        const uint32_t T = 1u << k, E = T + 1u, E3 = E * E * E;
-        const uint32_t mL = 1u << L;
-        const uint32_t tx = tile & (mL - 1), ty = (tile >> L) & (mL - 1), tz = tile >> (2 * L);
-        const uint32_t ox = tx * T, oy = ty * T, oz = tz * T;
-        const uint32_t e = (1u << d) + 1u;
-
-        // 1. the tile's sparse values (NaN elsewhere) and the descent's
-        if constexpr (kGrid) {
-            for (uint32_t p = threadIdx.x; p < E3; p += blockDim.x) {
-                const uint32_t lx = p % E, r = p / E, ly = r % E, lz = r / E;
-                s[p] = to_internal(a.grid[((uint64_t)(oz + lz) * e + (oy + ly)) * e + (ox + lx)]);
-            }
-            // descent points: level l's cube containing the tile, 27 points each
-            for (uint32_t q = threadIdx.x; q < 27 * L; q += blockDim.x) {
-                const uint32_t l = q / 27, p = q % 27;
-                const uint32_t size = 1u << (d - l), hs = size >> 1;
-                const uint32_t bx = ox & ~(size - 1), by = oy & ~(size - 1), bz = oz & ~(size - 1);
-                const uint32_t gx = bx + hs * (p % 3), gy = by + hs * ((p / 3) % 3), gz = bz + hs * (p / 9);
-                desc[q] = to_internal(a.grid[((uint64_t)gz * e + gy) * e + gx]);
-            }
-        } else {
-            {
-                const float4 nan4 = make_float4(qnan(), qnan(), qnan(), qnan());
-                float4* s4 = reinterpret_cast<float4*>(s);
-                for (uint32_t p = threadIdx.x; p < (E3 + 3) / 4; p += blockDim.x) s4[p] = nan4;
-            }
-            for (uint32_t q = threadIdx.x; q < 27 * L; q += blockDim.x) desc[q] = __int_as_float(0x7fc00000);
-            __syncthreads();
-            const uint64_t b0 = a.entry_off[item], b1 = a.entry_off[item + 1];
-            for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
-                const uint32_t loc = a.entry_local[i];
-                const float v = to_internal(a.sparse[node_base + a.entry_node[i]]);
-                if (loc < E3) s[loc] = v;
-                else desc[loc - E3] = v;
-            }
-        }
-        __syncthreads();
-
-        // 2. tile corners from the coarse levels
-        if (L > 0) {
-            if (threadIdx.x < 32) descend(s, desc, d, k, L, ox, oy, oz);
-            __syncthreads();
-        }
-
-        // 3. fine levels, one barrier each
-        for (uint32_t j = 0; j < k; ++j) {
-            cube_level(s, E, T, j);
-            __syncthreads();
-        }
-
-        // 4. owned vertices to HBM: [0, T) per axis, plus the far face on the last tile
-        float inv_scale = 1.f, offset = 0.f;
-        if constexpr (!kGrid) {
-            if (a.scale_offset) {
-                const float2 so = a.scale_offset[blk];
-                inv_scale = 1.f / so.x;
-                offset = so.y;
-            }
-        }
-        OutT* out = reinterpret_cast<OutT*>(a.out) + dense_off;
-        const uint32_t OY = T + (ty == mL - 1 ? 1u : 0u);
-        const uint32_t OZ = T + (tz == mL - 1 ? 1u : 0u);
-        const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-        // rows of T values along x: 32/T rows per warp step (T <= 32), no divisions
-        const uint32_t per = T < 32 ? 32u / T : 1u;
-        const uint32_t lx = lane & (T - 1), sub = T < 32 ? lane >> k : 0u;
-        const bool far_x = tx == mL - 1; // the last tile along x also writes its x = T column
-        for (uint32_t lz = 0; lz < OZ; ++lz) {
-            const uint64_t gz = (uint64_t)(oz + lz) * e;
-            for (uint32_t ly = warp * per + sub; ly < OY; ly += nwarps * per) {
-                const uint64_t g = (gz + (oy + ly)) * e + ox;
-                const uint32_t sp = E * (ly + E * lz);
-                Store<OutT>::put(out, g + lx, s[sp + lx], inv_scale, offset);
-                if (far_x && lx == 0) Store<OutT>::put(out, g + T, s[sp + T], inv_scale, offset);
-            }
+        const uint32_t mL = 1u << t.L;
+        t.tx = tile & (mL - 1);
+        t.ty = (tile >> t.L) & (mL - 1);
+        t.tz = tile >> (2 * t.L);
+        switch (t.k) {
+        case 0: run_tile<1, kGrid, OutT>(a, s, desc, t); break;
+        case 1: run_tile<2, kGrid, OutT>(a, s, desc, t); break;
+        case 2: run_tile<4, kGrid, OutT>(a, s, desc, t); break;
+        case 3: run_tile<8, kGrid, OutT>(a, s, desc, t); break;
+        case 4: run_tile<16, kGrid, OutT>(a, s, desc, t); break;
+        default: run_tile<32, kGrid, OutT>(a, s, desc, t); break;
         }
         __syncthreads();
     }

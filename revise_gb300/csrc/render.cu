@@ -410,10 +410,23 @@ __global__ void frame_render_kernel(FrameArgs fa)
     const s3r_view v = *fa.view;
     const uint32_t nthreads = blockDim.x * blockDim.y;
     const uint32_t tid = threadIdx.y * blockDim.x + threadIdx.x;
-    for (uint32_t i = tid; i < v.tf_n; i += nthreads) tf[i] = reinterpret_cast<const float4*>(fa.tf)[i];
-    __syncthreads();
     const uint32_t vx = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t vy = blockIdx.y * blockDim.y + threadIdx.y;
+    {
+        // CTAs whose pixels no block covers only clear their pixels
+        const int4 cv = *reinterpret_cast<const int4*>(fa.cover);
+        const int32_t x0 = blockIdx.x * blockDim.x, y0 = blockIdx.y * blockDim.y;
+        if (x0 >= cv.z || x0 + (int32_t)blockDim.x <= cv.x || y0 >= cv.w || y0 + (int32_t)blockDim.y <= cv.y) {
+            if (vx < v.W && vy < v.H) {
+                const size_t o = (size_t)(v.H - 1 - vy) * v.W + vx;
+                if (fa.rgba) reinterpret_cast<float4*>(fa.rgba)[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (fa.argb) fa.argb[o] = 0u;
+            }
+            return;
+        }
+    }
+    for (uint32_t i = tid; i < v.tf_n; i += nthreads) tf[i] = reinterpret_cast<const float4*>(fa.tf)[i];
+    __syncthreads();
     uint32_t taken = 0;
     if (vx < v.W && vy < v.H) {
         float org[3], dir[3];

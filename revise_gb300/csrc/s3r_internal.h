@@ -30,7 +30,7 @@ struct TileArgs {
     const uint2* items;           // {block, tile} per work item
     uint32_t nitems;
     const uint64_t* entry_off;    // nitems+1 prefix offsets into local/node
-    const uint16_t* entry_local;  // node position inside its tile (x + e*(y + e*z), e = 2^k+1)
+    const uint16_t* entry_local;  // node position inside its tile (tile_offset)
     const uint32_t* entry_node;   // node index within its block
     // entry_local >= (2^k+1)^3 addresses descent slot 27*level + point instead of the tile
     const float* sparse;          // node values
@@ -42,6 +42,21 @@ struct TileArgs {
     uint32_t grid_depth;
     uint32_t grid_tile_log2;
 };
+
+// Position of vertex (x, y, z) inside the shared tile of T cells, as the
+// interpolation kernel lays it out: for T >= 2 the parity-split layout (eight
+// sub-arrays by the parities of x, y, z, each x fastest; see interp.cu), for
+// T = 1 plain x + 2(y + 2z).  The plan stores node positions in this form.
+inline __host__ __device__ uint32_t tile_offset(uint32_t T, uint32_t x, uint32_t y, uint32_t z)
+{
+    if (T < 2) return x + 2 * (y + 2 * z);
+    const uint32_t H = T / 2, G = H + 1;
+    const uint32_t c = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
+    uint32_t base = 0;
+    for (uint32_t i = 0; i < c; ++i) base += ((i & 1) ? H : G) * (((i >> 1) & 1) ? H : G) * (((i >> 2) & 1) ? H : G);
+    const uint32_t nx = (x & 1) ? H : G, ny = (y & 1) ? H : G;
+    return base + (x >> 1) + nx * ((y >> 1) + ny * (z >> 1));
+}
 
 // Per-block entry of the render block table (dense over the (2^level)^3 block grid).
 struct RenderBlock {
@@ -71,6 +86,7 @@ struct FrameArgs {
     uint32_t* argb;                // optional
     unsigned long long* samples;   // optional
     const float2* scale_offset;    // per block {scale, offset} (16-bit bricks)
+    const int32_t* cover;          // device {x0, y0, x1, y1}: union of the blocks' view rectangles
     // adjoint
     const float* fwd_rgba;
     const float* dl_drgba;

@@ -32,7 +32,7 @@ def test_dense_field_interpolator_adapter_compiles(tmp_path):
     src = tmp_path / "adapter_check.cpp"
     src.write_text(SRC)
     cmd = ["g++", "-std=c++20", "-fsyntax-only", "-DS3DMM_REAL_TYPE=float", "-DS3DMM_ENABLE_CUDA",
-           "-DS3DMM_PROGRESS_REPORT", f"-I{ROOT / 'oracle' / 'shims'}", f"-I{REFERENCE / 'include'}",
+           "-DS3DMM_PROGRESS_REPORT", f"-I{ROOT / 'oracle' / 'shims_cpu'}", f"-I{ROOT / 'oracle' / 'shims'}", f"-I{REFERENCE / 'include'}",
            f"-I{ROOT / 'include'}", f"-I{ROOT / 'revise_gb300' / 'adapters'}", f"-I{cuda_inc}", str(src)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]

@@ -155,6 +155,29 @@ def test_graph_replay_equals_direct_render(ctx):
     plan.close()
 
 
+def test_graph_replay_follows_camera_changes(ctx):
+    """The captured frame reads the view, the block rectangles and the covered
+    screen area from device memory: moving the camera between replays must give
+    the image a direct render gives for the new camera."""
+    import torch
+    from revise_gb300.api import FramePlan
+    w = workloads.small(seed=13, level=2, depths=(2, 3), W=96, H=72)
+    plan = FramePlan(ctx, w)
+    sp, tf = _dev(w.sparse), _dev(w.tf)
+    a = torch.zeros(w.W * w.H * 4, device="cuda")
+    b = torch.zeros_like(a)
+    for eye in ((3.0, 6.0, 14.0), (-9.0, 2.0, 7.0), (0.5, -12.0, 3.0)):
+        w.eye = eye
+        view = host.view_for(w)
+        plan.run(view, sp, tf, b)
+        plan.interp(sp)
+        plan.render(view, tf, a)
+        torch.cuda.synchronize()
+        assert torch.equal(a, b), eye
+        assert float(a.view(-1, 4)[:, 3].max()) > 0.05
+    plan.close()
+
+
 def test_alpha_stop_bounded_difference(ctx):
     w = workloads.small(seed=6, level=2, depths=(2, 3), W=64, H=48)
     _, _, full, _, s_full = _frame(ctx, w, alpha_stop=2.0)
