@@ -44,10 +44,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--config", choices=["cfg3", "cfg2"], default="cfg3")
+    ap.add_argument("--config", choices=["cfg3", "cfg2", "cfg3-l3"], default="cfg3",
+                    help="cfg3-l3: the same block recipe at level 3 (512 blocks, ~97 M vertices), "
+                         "the small case for kernel captures")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--no-extras", action="store_true", help="skip the adjoint and 16-bit measurements")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the adjoint, 16-bit and reference-CUDA measurements")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     return ap.parse_args()
 
 
@@ -58,6 +62,8 @@ def dist_env():
 
 def make_workload(name):
     from revise_gb300 import workloads
+    if name == "cfg3-l3":
+        return workloads.cfg3(level=3)
     return workloads.cfg3() if name == "cfg3" else workloads.cfg2()
 
 
@@ -142,8 +148,42 @@ def run_reference(a):
                                    "restated DenseFieldInterpolator<3> (oracle/s3r_oracle.c)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if not a.no_extras:
+        line["reference_cuda"] = reference_cuda_frames(w, a)
     print(json.dumps(line))
     return 0
+
+
+def reference_cuda_frames(w, a):
+    """The reference's own GPU renderer on the same frame: its CUDA kernels (compiled
+    from its sources into oracle/_ref/*.cubin) driven block by block in back-to-front
+    order by the restated worker loop -- per block: upload of the sparse values,
+    the d-pass dense interpolation, renderKernel<Argb> into the shared viewport;
+    then the image read back and cropped.  Wall-clock ms per frame."""
+    try:
+        import numpy as np
+        import torch
+        from oracle import refcu
+        if not (torch.cuda.is_available() and refcu.available()):
+            return {"unavailable": "reference cubins not built (they compile from the reference tree)"}
+        from revise_gb300 import host
+        view = host.view_for(w)
+        refcu.set_tf(np.ascontiguousarray(w.tf, np.float32))
+        m = 1 << w.level
+        order = host.b2f_order([0, 0, 0], [m, m, m], [-5.0] * 3, [5.0] * 3, w.eye)
+        idx = {tuple(b[:3]): i for i, b in enumerate(w.blocks.tolist())}
+        oi = np.array([idx[tuple(b)] for b in order.tolist()])
+        rects = np.array([host.block_view_rect(view, w.blocks[b, :3]) for b in range(w.nblocks)], np.int32)
+        times = []
+        for i in range(2 + max(1, min(a.steps, 5))):
+            _, _, ms = refcu.worker(view, w, oi, rects)
+            if i >= 2:
+                times.append(ms)
+        ms = statistics.median(times)
+        return {"ms_per_frame": ms, "frames_per_s": 1e3 / ms, "frames": len(times),
+                "what": "reference CUDA kernels, reference worker loop (per-block H2D, interpolate, render)"}
+    except Exception as e:  # the CPU line stands without it
+        return {"unavailable": f"{type(e).__name__}: {e}"}
 
 
 # ------------------------------------------------------------------ clocks
@@ -310,7 +350,7 @@ def run_gb300(a):
         traffic = json.loads(tp.read_text()).get("dram_bytes_per_launch")
 
     cpu = None
-    if rank == 0:
+    if rank == 0 and not a.no_cpu:
         blocks = _sample_blocks(w, a.cpu_seconds, seed=2)
         rate, secs = cpu_interp_rate(w, blocks, processes=1)
         sv = sum(((1 << int(w.blocks[b, 3])) + 1) ** 3 for b in blocks)

@@ -94,7 +94,10 @@ def build_oracle(reference: str | None = None) -> None:
     _run(["make", "-s", "-C", str(oracle), "port"])
     ref = Path(reference or os.environ.get("S3R_REFERENCE", "/root/reference"))
     if (ref / "include" / "s3dmm" / "DenseFieldInterpolator.hpp").exists():
-        _run(["make", "-s", "-C", str(oracle), "ref", f"REFERENCE={ref}"])
+        _run(["make", "-s", "-C", str(oracle), "ref", "refcu", f"REFERENCE={ref}"])
+    # the harness around the reference's CUDA kernels builds anywhere the cubins exist
+    if (oracle / "_ref" / "ref_render.cubin").exists() and (oracle / "_ref" / "ref_interp.cubin").exists():
+        _run(["make", "-s", "-C", str(oracle), "refcu-harness", f"NVCC={cuda_home() / 'bin' / 'nvcc'}"])
 
 
 def main(argv: list[str] | None = None) -> int:

@@ -944,7 +944,7 @@ int s3r_frame_plan(s3r_ctx* ctx, const s3r_frame_desc* desc, s3r_plan** out)
     p->nblocks = desc->nblocks;
     p->level = desc->level;
     p->fmt = desc->brick_format;
-    p->render_tile = desc->render_tile % kRenderShapes;
+    p->render_tile = desc->render_tile % kRenderTiles;
     p->blocks.assign(desc->blocks, desc->blocks + 4 * (size_t)desc->nblocks);
     p->node_off.assign(desc->node_off, desc->node_off + desc->nblocks + 1);
     p->nodes = p->node_off[desc->nblocks];
@@ -1189,7 +1189,9 @@ int s3r_plan_autotune(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const 
     if ((rc = plan_stage_view(plan, view, s))) return cleanup(rc);
     uint32_t best_shape = plan->render_tile;
     best = 3.4e38f;
-    for (uint32_t shape = 0; shape < (uint32_t)kRenderShapes; ++shape) {
+    for (uint32_t shape = 0; shape < (uint32_t)kRenderTiles; ++shape) {
+        // several lanes per ray only where rays composite every block (alpha_stop >= 1)
+        if (shape >= (uint32_t)kRenderShapes && view->alpha_stop < 1.f) break;
         plan->render_tile = shape;
         float ms = 0;
         rc = timed([&](uint32_t* kk) { return plan_launch_render(plan, tf, img, nullptr, nullptr, s, kk); }, ms);

@@ -220,60 +220,126 @@ template <uint32_t T> struct SplitTile {
     }
 };
 
-// The finest level of a tile in the split layout: one thread per 2x2x2 cube
-// (H^3 cubes), reading its 27 points -- corners from the even sub-array, the
-// 19 midpoint slots (a sparse value or NaN) from their class sub-arrays --
-// filling the NaN midpoints in registers (edges, faces, centre; stencil sums in
-// the reference's order) and writing back the ones it owns (low side and
-// middle, plus the far side on the last cube along an axis).  A warp's 32 cubes
-// are consecutive along x within each class row, so every load and store is a
-// run of consecutive words.
-template <uint32_t T> __device__ __forceinline__ void finest_level(float* s)
+// Marks the finest-level cubes holding a sparse value at one of their
+// midpoints (tile position (x, y, z), at least one coordinate odd): the cube
+// along each odd axis, both neighbours along each even one.
+__device__ __forceinline__ void flag_cubes(uint32_t* flags, uint32_t H, uint32_t x, uint32_t y, uint32_t z)
+{
+    if (!((x | y | z) & 1)) return;
+    const uint32_t x0 = (x & 1) ? x >> 1 : (x ? (x >> 1) - 1 : 0), x1 = (x & 1) ? x >> 1 : min(x >> 1, H - 1);
+    const uint32_t y0 = (y & 1) ? y >> 1 : (y ? (y >> 1) - 1 : 0), y1 = (y & 1) ? y >> 1 : min(y >> 1, H - 1);
+    const uint32_t z0 = (z & 1) ? z >> 1 : (z ? (z >> 1) - 1 : 0), z1 = (z & 1) ? z >> 1 : min(z >> 1, H - 1);
+    for (uint32_t k = z0; k <= z1; ++k)
+        for (uint32_t j = y0; j <= y1; ++j)
+            for (uint32_t i = x0; i <= x1; ++i) {
+                const uint32_t c = i + H * (j + H * k);
+                atomicOr(&flags[c >> 5], 1u << (c & 31));
+            }
+}
+
+// The 19 midpoints of one 2x2x2 cube from its 8 corners (v[p], p = a + 3b + 9c,
+// a, b, c in {0, 1, 2}); kSlots: v also holds sparse values (or NaN) at the
+// midpoints, which are kept.  Edges, then faces, then the centre, stencil sums
+// in the reference's order.
+template <bool kSlots> __device__ __forceinline__ void fill_cube(float v[27])
+{
+#pragma unroll
+    for (int p = 0; p < 27; ++p) {
+        const int a = p % 3, b = (p / 3) % 3, cc = p / 9;
+        if ((a & 1) + (b & 1) + (cc & 1) == 1 && (!kSlots || isnan(v[p]))) {
+            const int st = (a & 1) ? 1 : ((b & 1) ? 3 : 9);
+            v[p] = kHalf * (v[p - st] + v[p + st]);
+        }
+    }
+#pragma unroll
+    for (int p = 0; p < 27; ++p) {
+        const int a = p % 3, b = (p / 3) % 3, cc = p / 9;
+        if ((a & 1) + (b & 1) + (cc & 1) == 2 && (!kSlots || isnan(v[p]))) {
+            const int s1 = (a & 1) ? 1 : 3;
+            const int s2 = (cc & 1) ? 9 : 3;
+            v[p] = kQuarter * (v[p - s1] + v[p + s1] + v[p - s2] + v[p + s2]);
+        }
+    }
+    if (!kSlots || isnan(v[13])) v[13] = kSixth * (v[12] + v[14] + v[10] + v[16] + v[4] + v[22]);
+}
+
+// The finest level of a tile, written straight to HBM: one thread per 2x2x2
+// cube (H^3 cubes, consecutive along x within a warp).  A cube reads its 8
+// corners from the even sub-array; only cubes flagged as holding a sparse
+// midpoint also read their 19 midpoint slots.  It computes its midpoints in
+// registers and stores the vertices it owns -- its low octant, plus the far
+// side where it is the last cube of the block along an axis -- with the
+// no-field -> NaN and 16-bit encoding fused into the store.
+template <uint32_t T, typename OutT>
+__device__ __forceinline__ void finest_store(const float* s, const uint32_t* flags, OutT* out, uint64_t e,
+                                             uint32_t ox, uint32_t oy, uint32_t oz, bool far_x, bool far_y,
+                                             bool far_z, float inv_scale, float offset)
 {
     using S = SplitTile<T>;
     constexpr uint32_t H = S::H;
     constexpr uint32_t lh = (H >= 2) ? (31 - __builtin_clz(H)) : 0;
     constexpr uint32_t ncubes = H * H * H;
+    const uint64_t e2 = e * e;
 #pragma unroll 1
     for (uint32_t c = threadIdx.x; c < ncubes; c += blockDim.x) {
         const uint32_t ci = c & (H - 1), cj = (c >> lh) & (H - 1), ck = c >> (2 * lh);
         float v[27];
+        const bool has = (flags[c >> 5] >> (c & 31)) & 1u;
 #pragma unroll
         for (int p = 0; p < 27; ++p) {
             const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
-            const uint32_t cls = (a & 1) | ((b & 1) << 1) | ((cc & 1) << 2);
-            v[p] = s[S::idx(cls, ci + (a >> 1), cj + (b >> 1), ck + (cc >> 1))];
+            if (!((a | b | cc) & 1)) v[p] = s[S::idx(0, ci + (a >> 1), cj + (b >> 1), ck + (cc >> 1))];
         }
+        if (has) {
 #pragma unroll
-        for (int p = 0; p < 27; ++p) {
-            const int a = p % 3, b = (p / 3) % 3, cc = p / 9;
-            if ((a & 1) + (b & 1) + (cc & 1) == 1 && isnan(v[p])) {
-                const int st = (a & 1) ? 1 : ((b & 1) ? 3 : 9);
-                v[p] = kHalf * (v[p - st] + v[p + st]);
-            }
-        }
-#pragma unroll
-        for (int p = 0; p < 27; ++p) {
-            const int a = p % 3, b = (p / 3) % 3, cc = p / 9;
-            if ((a & 1) + (b & 1) + (cc & 1) == 2 && isnan(v[p])) {
-                const int s1 = (a & 1) ? 1 : 3;
-                const int s2 = (cc & 1) ? 9 : 3;
-                v[p] = kQuarter * (v[p - s1] + v[p + s1] + v[p - s2] + v[p + s2]);
-            }
-        }
-        if (isnan(v[13])) v[13] = kSixth * (v[12] + v[14] + v[10] + v[16] + v[4] + v[22]);
-        const bool lx = ci == H - 1, ly = cj == H - 1, lz = ck == H - 1;
-#pragma unroll
-        for (int p = 0; p < 27; ++p) {
-            const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
-            if ((a & 1) + (b & 1) + (cc & 1) == 0) continue;
-            if ((a < 2 || lx) && (b < 2 || ly) && (cc < 2 || lz)) {
+            for (int p = 0; p < 27; ++p) {
+                const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
                 const uint32_t cls = (a & 1) | ((b & 1) << 1) | ((cc & 1) << 2);
-                s[S::idx(cls, ci + (a >> 1), cj + (b >> 1), ck + (cc >> 1))] = v[p];
+                if (cls) v[p] = s[S::idx(cls, ci + (a >> 1), cj + (b >> 1), ck + (cc >> 1))];
             }
+            fill_cube<true>(v);
+        } else {
+            fill_cube<false>(v);
+        }
+        const bool lx = far_x && ci == H - 1, ly = far_y && cj == H - 1, lz = far_z && ck == H - 1;
+        OutT* base = out + ((uint64_t)(oz + 2 * ck) * e + (oy + 2 * cj)) * e + (ox + 2 * ci);
+#pragma unroll
+        for (int p = 0; p < 27; ++p) {
+            const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
+            if ((a < 2 || lx) && (b < 2 || ly) && (cc < 2 || lz))
+                Store<OutT>::put(base, (uint64_t)a + b * e + cc * e2, v[p], inv_scale, offset);
         }
     }
-    __syncthreads();
+}
+
+// Entries of the next work item, loaded into registers while the current
+// item's finest level runs (their chain of dependent global loads -- item,
+// block, entry, node value -- would otherwise stall the CTA at every tile).
+constexpr uint32_t kPrefetch = 2; // entries per thread held in registers
+struct Prefetch {
+    uint32_t item;
+    uint64_t node_base, e0, e1;
+    uint32_t loc[kPrefetch];
+    float val[kPrefetch];
+};
+
+__device__ __forceinline__ void prefetch_entries(Prefetch& pf, const TileArgs& a, uint32_t item)
+{
+    pf.item = item;
+    pf.e0 = pf.e1 = 0;
+    if (item >= a.nitems) return;
+    const uint32_t blk = a.items[item].x;
+    pf.node_base = a.blocks[blk].node_base;
+    pf.e0 = a.entry_off[item];
+    pf.e1 = a.entry_off[item + 1];
+#pragma unroll
+    for (uint32_t q = 0; q < kPrefetch; ++q) {
+        const uint64_t i = pf.e0 + threadIdx.x + q * blockDim.x;
+        if (i < pf.e1) {
+            pf.loc[q] = a.entry_local[i];
+            pf.val[q] = a.sparse[pf.node_base + a.entry_node[i]];
+        }
+    }
 }
 
 struct TileItem {
@@ -285,7 +351,8 @@ struct TileItem {
 // One tile of T = 2^k cells.  Tiles of T >= 2 use the split layout; T = 1
 // (depth-0 blocks) is a plain 2x2x2 copy of the root corners.
 template <uint32_t T, bool kGrid, typename OutT>
-__device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* desc, const TileItem& t)
+__device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* desc, uint32_t* flags, const TileItem& t,
+                                         Prefetch& pf, const uint32_t* next_item)
 {
     constexpr uint32_t E = T + 1, E3 = E * E * E;
     using S = SplitTile<T < 2 ? 2 : T>;
@@ -296,12 +363,18 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
     const uint32_t d = t.d, L = t.L;
     const uint32_t ox = t.tx * T, oy = t.ty * T, oz = t.tz * T;
     const uint32_t e = (1u << d) + 1u;
+    constexpr uint32_t nflags = T >= 2 ? (S::H * S::H * S::H + 31) / 32 : 0;
+    for (uint32_t q = threadIdx.x; q < nflags; q += blockDim.x) flags[q] = 0u;
     // 1. the tile's sparse values (NaN elsewhere) and the descent's
     if constexpr (kGrid) {
+        __syncthreads(); // flags cleared
 #pragma unroll 1
         for (uint32_t p = threadIdx.x; p < E3; p += blockDim.x) {
             const uint32_t lx = p % E, r = p / E, ly = r % E, lz = r / E;
-            s[at(lx, ly, lz)] = to_internal(a.grid[((uint64_t)(oz + lz) * e + (oy + ly)) * e + (ox + lx)]);
+            const float v = to_internal(a.grid[((uint64_t)(oz + lz) * e + (oy + ly)) * e + (ox + lx)]);
+            s[at(lx, ly, lz)] = v;
+            if constexpr (T >= 2)
+                if (!isnan(v)) flag_cubes(flags, S::H, lx, ly, lz);
         }
         for (uint32_t q = threadIdx.x; q < 27 * L; q += blockDim.x) {
             const uint32_t l = q / 27, p = q % 27;
@@ -319,13 +392,31 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
         }
         for (uint32_t q = threadIdx.x; q < 27 * L; q += blockDim.x) desc[q] = qnan();
         __syncthreads();
-        const uint64_t b0 = a.entry_off[t.item], b1 = a.entry_off[t.item + 1];
-        for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
-            const uint32_t loc = a.entry_local[i];
-            const float v = to_internal(a.sparse[t.node_base + a.entry_node[i]]);
-            if (loc < E3) s[loc] = v;
-            else desc[loc - E3] = v;
-        }
+        auto place = [&](uint32_t loc, float v) {
+            if (loc < E3) {
+                s[loc] = v;
+                if constexpr (T >= 2) {
+                    // tile position of the split offset: class, then (i, j, k) inside it
+                    uint32_t c = 0;
+#pragma unroll
+                    for (uint32_t q = 1; q < 8; ++q) c += loc >= S::base(q) ? 1u : 0u;
+                    if (c) {
+                        const uint32_t r = loc - S::base(c);
+                        const uint32_t nx = S::n(c & 1), ny = S::n((c >> 1) & 1);
+                        const uint32_t ii = r % nx, rr = r / nx, jj = rr % ny, kk = rr / ny;
+                        flag_cubes(flags, S::H, 2 * ii + (c & 1), 2 * jj + ((c >> 1) & 1), 2 * kk + (c >> 2));
+                    }
+                }
+            } else {
+                desc[loc - E3] = v;
+            }
+        };
+        // the prefetched entries, then any beyond what the registers held
+#pragma unroll
+        for (uint32_t q = 0; q < kPrefetch; ++q)
+            if (pf.e0 + threadIdx.x + q * blockDim.x < pf.e1) place(pf.loc[q], to_internal(pf.val[q]));
+        for (uint64_t i = pf.e0 + threadIdx.x + kPrefetch * blockDim.x; i < pf.e1; i += blockDim.x)
+            place(a.entry_local[i], to_internal(a.sparse[t.node_base + a.entry_node[i]]));
     }
     __syncthreads();
     // 2. tile corners from the coarse levels
@@ -339,16 +430,16 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
         }
         __syncthreads();
     }
-    // 3. levels: the coarser ones on the even sub-array (a tile of T/2 cells), then the finest
+    // 3. the coarser levels on the even sub-array (a tile of T/2 cells)
     if constexpr (T >= 2) {
         constexpr uint32_t kk = (T >= 2) ? (31 - __builtin_clz(T)) : 0;
         for (uint32_t j = 0; j + 1 < kk; ++j) {
             cube_level(s, S::G, S::H, j);
             __syncthreads();
         }
-        finest_level<T>(s);
     }
-    // 4. owned vertices to HBM: [0, T) per axis, plus the far side on the last tiles
+    // 4. the finest level, straight to HBM, while the next item's entries load
+    if constexpr (!kGrid) prefetch_entries(pf, a, *next_item);
     float inv_scale = 1.f, offset = 0.f;
     if constexpr (!kGrid) {
         if (a.scale_offset) {
@@ -359,36 +450,15 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
     }
     const uint32_t mL = 1u << L;
     OutT* out = reinterpret_cast<OutT*>(a.out) + t.dense_off;
-    const uint32_t OY = T + (t.ty == mL - 1 ? 1u : 0u);
-    const uint32_t OZ = T + (t.tz == mL - 1 ? 1u : 0u);
-    const bool far_x = t.tx == mL - 1;
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    constexpr uint32_t per = T < 32 ? 32u / T : 1u; // rows per warp step
-    const uint32_t lx = lane & (T - 1), sub = T < 32 ? lane / T : 0u;
-    // A lane keeps its x; its rows keep their y parity (the row step is even),
-    // so only z's parity changes: two sub-array bases per lane.
-    const uint32_t y0 = warp * per + sub;
-    static_assert(kInterpThreads % 64 == 0, "the row step must stay even");
-    uint32_t base_z[2] = {0, 0}, nx = 0, nxy = 0;
+    const bool far_x = t.tx == mL - 1, far_y = t.ty == mL - 1, far_z = t.tz == mL - 1;
     if constexpr (T >= 2) {
-        const uint32_t xo = lx & 1, yo = y0 & 1;
-        nx = xo ? S::H : S::G;
-        nxy = nx * (yo ? S::H : S::G);
-        base_z[0] = S::idx(xo | (yo << 1), lx >> 1, 0, 0);
-        base_z[1] = S::idx(xo | (yo << 1) | 4, lx >> 1, 0, 0);
-    }
-#pragma unroll 1
-    for (uint32_t lz = 0; lz < OZ; ++lz) {
-        const uint64_t gz = (uint64_t)(oz + lz) * e;
-        const uint32_t bz = base_z[lz & 1] + nxy * (lz >> 1);
-#pragma unroll 1
-        for (uint32_t ly = y0; ly < OY; ly += nwarps * per) {
-            const uint64_t g = (gz + (oy + ly)) * e + ox;
-            uint32_t sp;
-            if constexpr (T >= 2) sp = bz + nx * (ly >> 1);
-            else sp = at(lx, ly, lz);
-            Store<OutT>::put(out, g + lx, s[sp], inv_scale, offset);
-            if (far_x && lx == 0) Store<OutT>::put(out, g + T, s[at(T, ly, lz)], inv_scale, offset);
+        finest_store<T, OutT>(s, flags, out, e, ox, oy, oz, far_x, far_y, far_z, inv_scale, offset);
+    } else {
+        // depth-0 block: its 8 root corners
+        for (uint32_t q = threadIdx.x; q < 8; q += blockDim.x) {
+            const uint32_t x = q & 1, y = (q >> 1) & 1, z = q >> 2;
+            Store<OutT>::put(out, ((uint64_t)(oz + z) * e + (oy + y)) * e + ox + x, s[at(x, y, z)], inv_scale,
+                             offset);
         }
     }
 }
@@ -399,15 +469,24 @@ __global__ void __launch_bounds__(kInterpThreads, 8) interp_tiles_kernel(TileArg
     extern __shared__ float4 s_tile[]; // tile_smem_bytes(): (2^k+1)^3 floats rounded up to whole float4s
     float* s = reinterpret_cast<float*>(s_tile);
     __shared__ float desc[27 * kMaxDescentLevels];
-    __shared__ uint32_t item_s;
+    __shared__ uint32_t flags[(16 * 16 * 16) / 32]; // one bit per finest cube, tiles up to 32 cells
+    __shared__ uint32_t item_s, next_s[2];
     const uint32_t nitems = a.nitems;
     // Work items come from the queue counter when there is one (zeroed before
-    // the launch), else item blockIdx.x once per CTA.
+    // the launch), else item blockIdx.x once per CTA.  The next item is taken
+    // at the start of the current one so its entries can be prefetched.  The
+    // slot it goes to alternates: a warp still reading slot i & 1 after the
+    // loop's closing barrier must not see thread 0 refill it for item i + 2
+    // (the barriers inside the tile keep thread 0 from getting that far).
+    if (threadIdx.x == 0) item_s = a.queue ? atomicAdd(a.queue, 1u) : blockIdx.x;
+    __syncthreads();
+    uint32_t item = item_s;
+    Prefetch pf;
+    if constexpr (!kGrid) prefetch_entries(pf, a, item);
     for (uint32_t iter = 0;; ++iter) {
-        if (threadIdx.x == 0) item_s = a.queue ? atomicAdd(a.queue, 1u) : (iter == 0 ? blockIdx.x : nitems);
-        __syncthreads();
-        const uint32_t item = item_s;
         if (item >= nitems) break;
+        uint32_t* next_p = &next_s[iter & 1];
+        if (threadIdx.x == 0) *next_p = a.queue ? atomicAdd(a.queue, 1u) : nitems;
         TileItem t;
         uint32_t tile;
         t.item = item;
@@ -435,14 +514,15 @@ __global__ void __launch_bounds__(kInterpThreads, 8) interp_tiles_kernel(TileArg
         t.ty = (tile >> t.L) & (mL - 1);
         t.tz = tile >> (2 * t.L);
         switch (t.k) {
-        case 0: run_tile<1, kGrid, OutT>(a, s, desc, t); break;
-        case 1: run_tile<2, kGrid, OutT>(a, s, desc, t); break;
-        case 2: run_tile<4, kGrid, OutT>(a, s, desc, t); break;
-        case 3: run_tile<8, kGrid, OutT>(a, s, desc, t); break;
-        case 4: run_tile<16, kGrid, OutT>(a, s, desc, t); break;
-        default: run_tile<32, kGrid, OutT>(a, s, desc, t); break;
+        case 0: run_tile<1, kGrid, OutT>(a, s, desc, flags, t, pf, next_p); break;
+        case 1: run_tile<2, kGrid, OutT>(a, s, desc, flags, t, pf, next_p); break;
+        case 2: run_tile<4, kGrid, OutT>(a, s, desc, flags, t, pf, next_p); break;
+        case 3: run_tile<8, kGrid, OutT>(a, s, desc, flags, t, pf, next_p); break;
+        case 4: run_tile<16, kGrid, OutT>(a, s, desc, flags, t, pf, next_p); break;
+        default: run_tile<32, kGrid, OutT>(a, s, desc, flags, t, pf, next_p); break;
         }
         __syncthreads();
+        item = *next_p;
     }
 }
 

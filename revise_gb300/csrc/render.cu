@@ -403,21 +403,28 @@ __device__ __forceinline__ Premul march_block(const s3r_view& v, const BlockRay&
     return acc;
 }
 
-template <int Fmt>
+// One pixel ray per R consecutive lanes: the ray's block sequence (the DDA
+// order) is cut into R contiguous runs, lane r composites run r, and the R
+// premultiplied partial results are merged front to back with shuffles (the
+// over operator is associative).  With R > 1 a ray stops early only inside its
+// run, so R = 1 is used when view.alpha_stop < 1.
+template <int Fmt, int R>
 __global__ void frame_render_kernel(FrameArgs fa)
 {
     extern __shared__ float4 tf[];
     const s3r_view v = *fa.view;
     const uint32_t nthreads = blockDim.x * blockDim.y;
     const uint32_t tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const uint32_t vx = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t seg = threadIdx.x % R;
+    const uint32_t px_per_row = blockDim.x / R;
+    const uint32_t vx = blockIdx.x * px_per_row + threadIdx.x / R;
     const uint32_t vy = blockIdx.y * blockDim.y + threadIdx.y;
     {
         // CTAs whose pixels no block covers only clear their pixels
         const int4 cv = *reinterpret_cast<const int4*>(fa.cover);
-        const int32_t x0 = blockIdx.x * blockDim.x, y0 = blockIdx.y * blockDim.y;
-        if (x0 >= cv.z || x0 + (int32_t)blockDim.x <= cv.x || y0 >= cv.w || y0 + (int32_t)blockDim.y <= cv.y) {
-            if (vx < v.W && vy < v.H) {
+        const int32_t x0 = blockIdx.x * px_per_row, y0 = blockIdx.y * blockDim.y;
+        if (x0 >= cv.z || x0 + (int32_t)px_per_row <= cv.x || y0 >= cv.w || y0 + (int32_t)blockDim.y <= cv.y) {
+            if (seg == 0 && vx < v.W && vy < v.H) {
                 const size_t o = (size_t)(v.H - 1 - vy) * v.W + vx;
                 if (fa.rgba) reinterpret_cast<float4*>(fa.rgba)[o] = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (fa.argb) fa.argb[o] = 0u;
@@ -428,12 +435,27 @@ __global__ void frame_render_kernel(FrameArgs fa)
     for (uint32_t i = tid; i < v.tf_n; i += nthreads) tf[i] = reinterpret_cast<const float4*>(fa.tf)[i];
     __syncthreads();
     uint32_t taken = 0;
-    if (vx < v.W && vy < v.H) {
+    Premul acc{0.f, 0.f, 0.f, 0.f};
+    const bool inside = vx < v.W && vy < v.H;
+    if (inside) {
         float org[3], dir[3];
         pixel_ray(v, vx, vy, org, dir);
         const float of = (v.threshold - v.field_min) / (v.field_max - v.field_min);
-        Premul acc{0.f, 0.f, 0.f, 0.f};
-        walk_blocks(org, dir, v.level, [&](uint32_t b, uint32_t ix, uint32_t iy, uint32_t iz) {
+        int lo = 0, hi = 1 << 30;
+        if (R > 1) {
+            int n = 0;
+            walk_blocks(org, dir, v.level, [&](uint32_t, uint32_t, uint32_t, uint32_t) {
+                ++n;
+                return true;
+            });
+            const int chunk = (n + R - 1) / R;
+            lo = (int)seg * chunk;
+            hi = lo + chunk;
+        }
+        int idx = 0;
+        walk_blocks(org, dir, v.level, [&](uint32_t b, uint32_t, uint32_t, uint32_t) {
+            if (idx >= hi) return false;
+            if (idx++ < lo) return true;
             const RenderBlock* rb = &fa.table[b];
             const uint32_t depth = rb->depth;
             if (depth == 0xffffffffu) return true;
@@ -458,6 +480,23 @@ __global__ void frame_render_kernel(FrameArgs fa)
             acc.a = __fmaf_rn(T, p.a, acc.a);
             return !(acc.a > v.alpha_stop);
         });
+    }
+    // merge the runs front to back: lane seg (a multiple of 2*off) takes lane seg+off behind it
+#pragma unroll
+    for (int off = 1; off < R; off <<= 1) {
+        const float br = __shfl_down_sync(0xffffffffu, acc.r, off, R);
+        const float bg = __shfl_down_sync(0xffffffffu, acc.g, off, R);
+        const float bb = __shfl_down_sync(0xffffffffu, acc.b, off, R);
+        const float ba = __shfl_down_sync(0xffffffffu, acc.a, off, R);
+        if ((seg & (2 * off - 1)) == 0) {
+            const float T = __fsub_rn(1.f, acc.a);
+            acc.r = __fmaf_rn(T, br, acc.r);
+            acc.g = __fmaf_rn(T, bg, acc.g);
+            acc.b = __fmaf_rn(T, bb, acc.b);
+            acc.a = __fmaf_rn(T, ba, acc.a);
+        }
+    }
+    if (inside && seg == 0) {
         const size_t o = (size_t)(v.H - 1 - vy) * v.W + vx;
         float4 out = make_float4(0.f, 0.f, 0.f, acc.a);
         if (acc.a > 0.f) {
@@ -634,20 +673,36 @@ cudaError_t launch_render_block_argb(const s3r_view* view_host, const float* bri
     return cudaGetLastError();
 }
 
+template <int Fmt>
+cudaError_t launch_frame_render_fmt(const FrameArgs& a, dim3 grid, dim3 block, size_t smem, uint32_t R, cudaStream_t s)
+{
+    switch (R) {
+    case 1: frame_render_kernel<Fmt, 1><<<grid, block, smem, s>>>(a); break;
+    case 2: frame_render_kernel<Fmt, 2><<<grid, block, smem, s>>>(a); break;
+    case 4: frame_render_kernel<Fmt, 4><<<grid, block, smem, s>>>(a); break;
+    default: frame_render_kernel<Fmt, 8><<<grid, block, smem, s>>>(a); break;
+    }
+    return cudaGetLastError();
+}
+
 cudaError_t launch_frame_render(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, uint32_t fmt,
                                 uint32_t tile_shape, cudaStream_t s)
 {
-    const int sx = kRenderShapeX[tile_shape % kRenderShapes], sy = kRenderShapeY[tile_shape % kRenderShapes];
-    dim3 block(sx, sy);
-    dim3 grid((W + sx - 1) / sx, (H + sy - 1) / sy);
+    // tile_shape: CTA pixel shape (low 2 bits) and lanes per ray R = 2^(bits 2-3)
+    const uint32_t shape = tile_shape % kRenderShapes;
+    const uint32_t R = 1u << ((tile_shape / kRenderShapes) % 4);
+    const int sx = kRenderShapeX[shape], sy = kRenderShapeY[shape];
+    // R lanes per pixel: keep 128-ish threads per CTA by narrowing the pixel tile
+    const int px = sx / (int)R > 0 ? sx / (int)R : 1;
+    dim3 block(px * R, sy);
+    dim3 grid((W + px - 1) / px, (H + sy - 1) / sy);
     const size_t smem = tf_n * sizeof(float4);
     switch (fmt) {
-    case S3R_BRICK_F32: frame_render_kernel<S3R_BRICK_F32><<<grid, block, smem, s>>>(a); break;
-    case S3R_BRICK_F16: frame_render_kernel<S3R_BRICK_F16><<<grid, block, smem, s>>>(a); break;
-    case S3R_BRICK_BF16: frame_render_kernel<S3R_BRICK_BF16><<<grid, block, smem, s>>>(a); break;
+    case S3R_BRICK_F32: return launch_frame_render_fmt<S3R_BRICK_F32>(a, grid, block, smem, R, s);
+    case S3R_BRICK_F16: return launch_frame_render_fmt<S3R_BRICK_F16>(a, grid, block, smem, R, s);
+    case S3R_BRICK_BF16: return launch_frame_render_fmt<S3R_BRICK_BF16>(a, grid, block, smem, R, s);
     default: return cudaErrorInvalidValue;
     }
-    return cudaGetLastError();
 }
 
 cudaError_t launch_frame_backward(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, cudaStream_t s)

@@ -121,8 +121,10 @@ cudaError_t launch_crop(const uint32_t* img, uint32_t W, const int32_t rect[4], 
 cudaError_t launch_compose(const s3r_image_part* parts_dev, uint32_t nparts, int32_t just_copy_first, uint32_t* dst,
                            int32_t dw, int32_t dh, int32_t offx, int32_t offy, cudaStream_t s);
 
-// Render CTA shapes the autotuner chooses from: {x, y} threads.
+// Render CTA pixel shapes the autotuner chooses from: {x, y} pixels; a render
+// tile id is shape + kRenderShapes * log2(lanes per ray), lanes per ray 1..8.
 constexpr int kRenderShapes = 4;
+constexpr int kRenderTiles = kRenderShapes * 4;
 constexpr int kRenderShapeX[kRenderShapes] = {16, 32, 8, 16};
 constexpr int kRenderShapeY[kRenderShapes] = {8, 4, 8, 16};
 

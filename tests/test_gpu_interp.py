@@ -2,8 +2,16 @@
 import numpy as np
 import pytest
 
+import functools
+
 import oracle
 from revise_gb300 import _lib, workloads
+
+
+@functools.lru_cache(maxsize=1)
+def _cfg3():
+    return workloads.cfg3()
+
 
 pytestmark = pytest.mark.gpu
 
@@ -132,7 +140,7 @@ def test_cfg3_full_size_plan_sampled_blocks(ctx):
     """4096 blocks of depth 3..7 in one launch; a seeded sample of blocks against the oracle."""
     import torch
     from revise_gb300.api import FramePlan
-    w = workloads.cfg3()
+    w = _cfg3()
     plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=16)
     plan.interp(torch.from_numpy(w.sparse).cuda())
     torch.cuda.synchronize()
@@ -146,4 +154,35 @@ def test_cfg3_full_size_plan_sampled_blocks(ctx):
         assert _same(bricks[a:c].cpu().numpy(), oracle.interp_f32(n2i, sp, int(w.blocks[b, 3]))), b
     # every vertex was written: NaN only where the oracle says so (checked above) and none left uninitialised
     assert plan.info.vertices == w.vertices
+    plan.close()
+
+
+@pytest.mark.parametrize("tile", [8, 16, 32])
+def test_cfg3_every_block_matches_single_block_path(ctx, tile):
+    """Whole cfg3 in one batched launch (work queue, thousands of CTAs racing for
+    items) against the single-block entry point, every block, bit for bit; then
+    two more launches into the same store give the same bits."""
+    import torch
+    from revise_gb300.api import FramePlan, to_device_n2i
+    w = _cfg3()
+    plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=tile)
+    sp = torch.from_numpy(w.sparse).cuda()
+    plan.interp(sp)
+    torch.cuda.synchronize()
+    bricks, offs = plan.bricks()
+    first = bricks.view(torch.int32).clone()
+    for _ in range(2):
+        plan.interp(sp)
+    torch.cuda.synchronize()
+    assert torch.equal(first, bricks.view(torch.int32))
+    no = w.node_off
+    n2i_all = to_device_n2i(w.n2i)
+    bad = []
+    for b in range(w.nblocks):
+        d = int(w.blocks[b, 3])
+        n0, n1 = int(no[b]), int(no[b + 1])
+        one = ctx.interp_dense(n2i_all[n0:n1], sp[n0:n1], d)
+        if not torch.equal(one.view(torch.int32), first[int(offs[b]):int(offs[b + 1])]):
+            bad.append(b)
+    assert not bad, bad[:10]
     plan.close()

@@ -195,3 +195,30 @@ def test_16bit_bricks_image_error_is_bounded(ctx, fmt):
     err = np.abs(img - ref)[flags == 0]
     assert err.max() <= (0.02 if fmt == _lib.BRICK_F16 else 0.06)
     plan.close()
+
+
+def test_render_tiles_agree(ctx):
+    """Every CTA shape and lanes-per-ray choice renders the same cfg2 frame: R = 1
+    shapes bit-identical, R > 1 (partial composites merged by shuffles in another
+    association order) within 1e-5."""
+    import torch
+    from revise_gb300.api import FramePlan
+    w = workloads.cfg2()
+    view = host.view_for(w)
+    sp, tf = _dev(w.sparse), _dev(w.tf)
+    rgba = torch.zeros(w.W * w.H * 4, device="cuda")
+    base = None
+    for rt in range(16):
+        plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=16, render_tile=rt)
+        rgba.fill_(-1.0)
+        plan.interp(sp)
+        plan.render(view, tf, rgba)
+        torch.cuda.synchronize()
+        img = rgba.clone()
+        plan.close()
+        assert float(img.min()) >= 0.0, rt  # every pixel written
+        if base is None:
+            base = img
+            continue
+        d = float((img - base).abs().max())
+        assert d == 0.0 if rt < 4 else d <= 1e-5, (rt, d)
