@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define S3R_ABI_VERSION 1
+#define S3R_ABI_VERSION 2
 
 /* status codes */
 #define S3R_OK 0
@@ -135,8 +135,21 @@ typedef struct s3r_view {
     float quality;         /* sampling quality (renderQuality) */
     uint32_t tf_n;         /* transfer-function entries, RGBA float each, 2..4096 */
     float alpha_stop;      /* batched path: stop a ray once its alpha exceeds this (>= 1: never) */
-    uint32_t reserved[3];
+    uint32_t filter;       /* S3R_FILTER_EXACT or S3R_FILTER_TEXTURE */
+    uint32_t reserved[2];
 } s3r_view;
+
+/* How a sample is filtered from a brick and from the transfer function.
+ * EXACT: FP32 trilinear / linear interpolation with the exact fractions; a
+ *   sample whose 8 texels hold a NaN is skipped.
+ * TEXTURE: the linear filtering the GPU texture unit applies to the
+ *   reference's tex3D / tex1D fetches (RenderFuncInput.hpp:42-50,
+ *   renderArgb.hpp:44): 8-bit fractions, weights rounded to 1/256 in the
+ *   unit's own order, and a NaN texel skipping the sample only when all its
+ *   per-axis weights are nonzero -- results match the reference's renderer.
+ *   No adjoint (the weights are piecewise constant). */
+#define S3R_FILTER_EXACT 0u
+#define S3R_FILTER_TEXTURE 1u
 
 /* getLookAt(eye, center, up) + the eye set-up of DenseFieldRenderer_cu.cu:353-372.
  * Perspective: fovy_deg is the vertical field of view.  Orthographic (ortho != 0):
@@ -273,15 +286,17 @@ int s3r_frame_render(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const f
                      uint32_t* argb, unsigned long long* samples, void* stream);
 
 /* s3r_frame_interp + s3r_frame_render as one CUDA graph, captured on the first
- * call for this (plan, pointers) and replayed afterwards; the view is copied to
- * the device before each replay.  Allocates on the first call. */
+ * call for this (plan, pointers, viewport size, tf_n, filter) and replayed
+ * afterwards; the view is copied to the device before each replay.  Allocates
+ * on the first call. */
 int s3r_frame_run(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* sparse, const float* tf,
                   float* rgba, uint32_t* argb, unsigned long long* samples, void* stream);
 
 /* Adjoint of s3r_frame_render (F32 bricks) for L = 1/2 sum (I - target)^2:
  * given the forward image rgba (device) and dl_drgba = I - target (device,
  * W*H*4), accumulates dL/dtf (device, tf_n*4 floats) and dL/ddense (device,
- * one float per brick vertex).  Sample positions are recomputed per ray. */
+ * one float per brick vertex).  Sample positions are recomputed per ray.
+ * view->filter must be S3R_FILTER_EXACT (else S3R_ERR_UNSUPPORTED). */
 int s3r_render_argb_backward(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* tf,
                              const float* rgba, const float* dl_drgba, float* dtf, float* ddense, void* stream);
 

@@ -31,7 +31,7 @@ class OrcCamera(C.Structure):
 class OrcView(C.Structure):
     _fields_ = [("cam", OrcCamera), ("W", C.c_uint32), ("H", C.c_uint32), ("level", C.c_uint32),
                 ("field_min", C.c_float), ("field_max", C.c_float), ("threshold", C.c_float),
-                ("quality", C.c_float), ("tf_n", C.c_uint32)]
+                ("quality", C.c_float), ("tf_n", C.c_uint32), ("filter", C.c_uint32)]
 
 
 def _p(a, t):
@@ -73,6 +73,7 @@ def view_from(v) -> OrcView:
     o.cam.w, o.cam.h, o.cam.ortho = v.cam.w, v.cam.h, v.cam.ortho
     o.W, o.H, o.level = v.W, v.H, v.level
     o.field_min, o.field_max, o.threshold, o.quality, o.tf_n = v.field_min, v.field_max, v.threshold, v.quality, v.tf_n
+    o.filter = v.filter
     return o
 
 
@@ -139,6 +140,17 @@ def render_block_argb8(view: OrcView, brick: np.ndarray, depth: int, idx, rect, 
     r = (C.c_int32 * 4)(*[int(x) for x in rect])
     port().orc_render_block_argb8(C.byref(view), _p(brick, C.c_float), C.c_uint32(depth), i, r,
                                   _p(tf, C.c_float), _p(viewport, C.c_uint32))
+
+
+def tex3d_weights(tc, n: int):
+    """Texture-unit weights (int, units of 1/256), NaN-footprint flags and texel indices
+    of the 8 texels around texel coordinate tc = (x, y, z) in an n^3 clamped texture."""
+    t = (C.c_float * 3)(*[float(x) for x in tc])
+    w = (C.c_int32 * 8)()
+    f = (C.c_uint8 * 8)()
+    i = (C.c_uint32 * 8)()
+    port().orc_tex3d_weights(t, C.c_uint32(n), w, f, i)
+    return np.array(w[:]), np.array(f[:], dtype=bool), np.array(i[:])
 
 
 def _frame_args(w, dense, rects):

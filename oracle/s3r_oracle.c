@@ -345,9 +345,109 @@ static float opacity_factor(const orc_view* v)
     return (v->threshold - v->field_min) / (v->field_max - v->field_min);
 }
 
+/* ======================================================================
+ * Texture-unit filtering (cudaFilterModeLinear, cudaAddressModeClamp, float
+ * texels), as the reference's tex3D / tex1D fetches (RenderFuncInput.hpp:42-50,
+ * renderArgb.hpp:44) return it on this GPU.  Measured with one-hot 2x2x2
+ * textures over a lattice of coordinates and restated here:
+ *  - per axis, xb = coordinate - 0.5, texels floor(xb) and floor(xb) + 1
+ *    (clamped), fraction held as an integer a = floor(frac(xb) * 256 + 1/2)
+ *    in 0..256 (CUDA documents 8 fractional bits);
+ *  - 1D: weights (256 - a, a) / 256;
+ *  - 3D: the z split is exact (zt = 256 - c or c); within each z half the
+ *    x-high weight is xh = round(a * zt / 256) (halves up) and x-low is
+ *    xl = zt - xh; the y split rounds the y-high part under xh,
+ *    yh = round(xh * b / 256), and the y-low part under xl,
+ *    yl = round(xl * (256 - b) / 256), the other part being the rest, so the
+ *    eight weights always sum to 256;
+ *  - a NaN texel makes the result NaN when its per-axis factors (a or 256 - a,
+ *    ...) are all nonzero, even where its rounded weight is 0; a NaN texel
+ *    whose factor on some axis is 0 is ignored.
+ * The weighted sum is formed in double and rounded to float once.
+ * ====================================================================== */
+
+static int32_t rn8(int32_t x, int32_t y) { return (x * y + 128) >> 8; }
+
+static void tex_axis(float tc, uint32_t n, uint32_t* i0, uint32_t* i1, int32_t* a)
+{
+    double xb = (double)(tc - 0.5f);
+    double q = floor(xb * 256.0 + 0.5);
+    double fl = floor(q / 256.0);
+    *a = (int32_t)(q - 256.0 * fl);
+    long lo = (long)fl, hi = lo + 1, top = (long)n - 1;
+    *i0 = (uint32_t)(lo < 0 ? 0 : (lo > top ? top : lo));
+    *i1 = (uint32_t)(hi < 0 ? 0 : (hi > top ? top : hi));
+}
+
+/* returns 0 for NaN */
+static int tex3d_sample(const orc_ray* r, const float tc[3], const float* brick, float* out)
+{
+    uint32_t i0[3], i1[3];
+    int32_t a[3];
+    for (int d = 0; d < 3; ++d)
+        tex_axis(tc[d], r->n, &i0[d], &i1[d], &a[d]);
+    int32_t w[8];
+    for (int hz = 0; hz < 2; ++hz) {
+        const int32_t zt = hz ? a[2] : 256 - a[2];
+        const int32_t xh = rn8(a[0], zt), xl = zt - xh;
+        const int32_t yhh = rn8(xh, a[1]);
+        const int32_t yll = rn8(xl, 256 - a[1]);
+        w[1 | 2 | (hz << 2)] = yhh;
+        w[1 | (hz << 2)] = xh - yhh;
+        w[(hz << 2)] = yll;
+        w[2 | (hz << 2)] = xl - yll;
+    }
+    const uint64_t n = r->n;
+    double acc = 0.0;
+    for (int t = 0; t < 8; ++t) {
+        const int hx = t & 1, hy = (t >> 1) & 1, hz = (t >> 2) & 1;
+        const int32_t fx = hx ? a[0] : 256 - a[0], fy = hy ? a[1] : 256 - a[1], fz = hz ? a[2] : 256 - a[2];
+        const uint64_t x = hx ? i1[0] : i0[0], y = hy ? i1[1] : i0[1], z = hz ? i1[2] : i0[2];
+        const float val = brick[(z * n + y) * n + x];
+        if (isnan(val)) {
+            if (fx && fy && fz) return 0;
+            continue;
+        }
+        acc += (double)w[t] * (double)val;
+    }
+    *out = (float)(acc / 256.0);
+    return 1;
+}
+
+void orc_tex3d_weights(const float tc[3], uint32_t n, int32_t w[8], uint8_t footprint[8], uint32_t texel[8])
+{
+    uint32_t i0[3], i1[3];
+    int32_t a[3];
+    for (int d = 0; d < 3; ++d)
+        tex_axis(tc[d], n, &i0[d], &i1[d], &a[d]);
+    for (int hz = 0; hz < 2; ++hz) {
+        const int32_t zt = hz ? a[2] : 256 - a[2];
+        const int32_t xh = rn8(a[0], zt), xl = zt - xh;
+        const int32_t yhh = rn8(xh, a[1]), yll = rn8(xl, 256 - a[1]);
+        w[3 | (hz << 2)] = yhh;
+        w[1 | (hz << 2)] = xh - yhh;
+        w[hz << 2] = yll;
+        w[2 | (hz << 2)] = xl - yll;
+    }
+    for (int t = 0; t < 8; ++t) {
+        const int hx = t & 1, hy = (t >> 1) & 1, hz = (t >> 2) & 1;
+        footprint[t] = (uint8_t)((hx ? a[0] : 256 - a[0]) && (hy ? a[1] : 256 - a[1]) && (hz ? a[2] : 256 - a[2]));
+        const uint32_t x = hx ? i1[0] : i0[0], y = hy ? i1[1] : i0[1], z = hz ? i1[2] : i0[2];
+        texel[t] = (z * n + y) * n + x;
+    }
+}
+
+static float tex1d_tf(const float* tf, uint32_t tfn, float v01, int ch)
+{
+    uint32_t i0, i1;
+    int32_t a;
+    tex_axis(v01 * (float)tfn, tfn, &i0, &i1, &a);
+    return (float)(((double)(256 - a) * tf[4 * i0 + ch] + (double)a * tf[4 * i1 + ch]) / 256.0);
+}
+
 /* One block's float RGBA along one ray (non-premultiplied, reference order). */
 static void march_block_f32(const orc_view* v, const orc_ray* r, const float* brick, uint32_t depth,
-                            const float* tf, float rgba[4])
+                            const float* tf, float rgba[4], int tex)
 {
     const float span = v->field_max - v->field_min;
     const float of = opacity_factor(v);
@@ -355,27 +455,32 @@ static void march_block_f32(const orc_view* v, const orc_ray* r, const float* br
     rgba[0] = rgba[1] = rgba[2] = rgba[3] = 0.f;
     for (int i = 1; i < r->sample_count; ++i) {
         float tc[3];
-        corner8 c;
+        float val;
         sample_coord(r, i - 1, tc);
-        corners(r, tc, &c);
-        float t[8];
-        int nan = 0;
-        for (int k = 0; k < 8; ++k) {
-            t[k] = brick[c.off[k]];
-            nan |= isnan(t[k]);
+        if (tex) {
+            if (!tex3d_sample(r, tc, brick, &val)) continue;
+        } else {
+            corner8 c;
+            corners(r, tc, &c);
+            float t[8];
+            int nan = 0;
+            for (int k = 0; k < 8; ++k) {
+                t[k] = brick[c.off[k]];
+                nan |= isnan(t[k]);
+            }
+            if (nan) continue;
+            float x00 = t[0] + c.f[0] * (t[1] - t[0]);
+            float x10 = t[2] + c.f[0] * (t[3] - t[2]);
+            float x01 = t[4] + c.f[0] * (t[5] - t[4]);
+            float x11 = t[6] + c.f[0] * (t[7] - t[6]);
+            float y0 = x00 + c.f[1] * (x10 - x00);
+            float y1 = x01 + c.f[1] * (x11 - x01);
+            val = y0 + c.f[2] * (y1 - y0);
         }
-        if (nan) continue;
-        float x00 = t[0] + c.f[0] * (t[1] - t[0]);
-        float x10 = t[2] + c.f[0] * (t[3] - t[2]);
-        float x01 = t[4] + c.f[0] * (t[5] - t[4]);
-        float x11 = t[6] + c.f[0] * (t[7] - t[6]);
-        float y0 = x00 + c.f[1] * (x10 - x00);
-        float y1 = x01 + c.f[1] * (x11 - x01);
-        float val = y0 + c.f[2] * (y1 - y0);
         float v01 = (val - v->field_min) / span;
         float col[4];
         for (int ch = 0; ch < 4; ++ch)
-            col[ch] = tf_lookup_f32(tf, v->tf_n, v01, ch);
+            col[ch] = tex ? tex1d_tf(tf, v->tf_n, v01, ch) : tf_lookup_f32(tf, v->tf_n, v01, ch);
         col[3] = 1.f - powf(1.f - col[3] * of, il);
         blend_behind(rgba, col);
         if (rgba[3] > 0.996f) break;
@@ -396,7 +501,7 @@ void orc_render_block_argb8(const orc_view* v, const float* brick, uint32_t dept
             ray_for_pixel(v, vx, vy, org, dir);
             if (!ray_block(v, org, dir, c, h, depth, &r)) continue;
             float rgba[4], ex[4];
-            march_block_f32(v, &r, brick, depth, tf, rgba);
+            march_block_f32(v, &r, brick, depth, tf, rgba, v->filter == 1);
             uint32_t* px = &viewport[(size_t)(v->H - 1 - vy) * v->W + vx];
             argb_to_rgba(*px, ex);
             blend_above(ex, rgba);
@@ -466,27 +571,75 @@ static int sample_f64(const orc_view* v, const orc_ray* r, int k, const float* b
                       sample64* s)
 {
     float tc[3];
-    corner8 c;
     sample_coord(r, k, tc);
-    corners(r, tc, &c);
-    double t[8];
-    for (int i = 0; i < 8; ++i) {
-        float x = brick[c.off[i]];
-        if (isnan(x)) return 0;
-        t[i] = x;
-        s->off[i] = c.off[i];
-    }
-    double fx = c.f[0], fy = c.f[1], fz = c.f[2];
-    for (int i = 0; i < 8; ++i)
-        s->w[i] = ((i & 1) ? fx : 1 - fx) * ((i & 2) ? fy : 1 - fy) * ((i & 4) ? fz : 1 - fz);
     double val = 0;
-    for (int i = 0; i < 8; ++i) val += s->w[i] * t[i];
+    if (v->filter == 1) {
+        /* texture-unit weights (integers / 256, see tex3d_sample), summed exactly in double */
+        uint32_t i0[3], i1[3];
+        int32_t a3[3];
+        for (int d = 0; d < 3; ++d)
+            tex_axis(tc[d], r->n, &i0[d], &i1[d], &a3[d]);
+        int32_t w[8];
+        for (int hz = 0; hz < 2; ++hz) {
+            const int32_t zt = hz ? a3[2] : 256 - a3[2];
+            const int32_t xh = rn8(a3[0], zt), xl = zt - xh;
+            const int32_t yhh = rn8(xh, a3[1]), yll = rn8(xl, 256 - a3[1]);
+            w[3 | (hz << 2)] = yhh;
+            w[1 | (hz << 2)] = xh - yhh;
+            w[(hz << 2)] = yll;
+            w[2 | (hz << 2)] = xl - yll;
+        }
+        const uint64_t n = r->n;
+        for (int i = 0; i < 8; ++i) {
+            const int hx = i & 1, hy = (i >> 1) & 1, hz = (i >> 2) & 1;
+            const uint64_t x = hx ? i1[0] : i0[0], y = hy ? i1[1] : i0[1], z = hz ? i1[2] : i0[2];
+            s->off[i] = (z * n + y) * n + x;
+            const float xv = brick[s->off[i]];
+            const int32_t fx = hx ? a3[0] : 256 - a3[0], fy = hy ? a3[1] : 256 - a3[1], fz = hz ? a3[2] : 256 - a3[2];
+            if (isnan(xv)) {
+                if (fx && fy && fz) return 0;
+                s->w[i] = 0;
+                continue;
+            }
+            s->w[i] = w[i] / 256.0;
+            val += s->w[i] * (double)xv;
+        }
+    } else {
+        corner8 c;
+        corners(r, tc, &c);
+        double t[8];
+        for (int i = 0; i < 8; ++i) {
+            float x = brick[c.off[i]];
+            if (isnan(x)) return 0;
+            t[i] = x;
+            s->off[i] = c.off[i];
+        }
+        double fx = c.f[0], fy = c.f[1], fz = c.f[2];
+        for (int i = 0; i < 8; ++i)
+            s->w[i] = ((i & 1) ? fx : 1 - fx) * ((i & 2) ? fy : 1 - fy) * ((i & 4) ? fz : 1 - fz);
+        for (int i = 0; i < 8; ++i) val += s->w[i] * t[i];
+    }
     s->val = val;
     double span = (double)v->field_max - (double)v->field_min;
     double v01 = (val - (double)v->field_min) / span;
     s->v01 = v01;
     /* normalized-coordinate linear filtering with clamp addressing */
     double u = v01 * (double)v->tf_n - 0.5;
+    if (v->filter == 1) {
+        /* 8-bit weight, coordinate formed in float as the fetch receives it */
+        uint32_t j0, j1;
+        int32_t aq;
+        tex_axis((float)v01 * (float)v->tf_n, v->tf_n, &j0, &j1, &aq);
+        s->ti0 = j0;
+        s->ti1 = j1;
+        s->tf_f = aq / 256.0;
+        for (int ch = 0; ch < 4; ++ch) {
+            double ta = tf[4 * j0 + ch], tb = tf[4 * j1 + ch];
+            s->col[ch] = ta + s->tf_f * (tb - ta);
+            s->dcol[ch] = 0.0;
+        }
+        return 1;
+    }
     double fl = floor(u);
     double f = u - fl;
     long a = (long)fl, b = a + 1, hi = (long)v->tf_n - 1;
@@ -569,7 +722,7 @@ void orc_render_frame_argb8(const orc_view* v, uint32_t nb, const uint32_t* bloc
             for (int j = 0; j < nh; ++j) { /* far first */
                 uint32_t b = hits[j].block;
                 float rgba[4], ex[4];
-                march_block_f32(v, &hits[j].r, dense + dense_off[b], blocks[4 * b + 3], tf, rgba);
+                march_block_f32(v, &hits[j].r, dense + dense_off[b], blocks[4 * b + 3], tf, rgba, v->filter == 1);
                 argb_to_rgba(*px, ex);
                 blend_above(ex, rgba);
                 *px = rgba_to_argb(ex);

@@ -54,6 +54,8 @@ typedef struct orc_view {
     float threshold;        /* absolute threshold; opacity factor = (threshold-min)/(max-min) */
     float quality;
     uint32_t tf_n;          /* transfer-function entries (RGBA float each) */
+    uint32_t filter;        /* 0: exact trilinear / linear filtering; 1: the GPU texture unit's
+                               linear filtering of the reference's textures (s3r_oracle.c) */
 } orc_view;
 
 /* ---- dense interpolation (include/s3dmm/DenseFieldInterpolator.hpp:198-419) ---- */
@@ -73,6 +75,10 @@ void orc_block_view_rect(const orc_view* v, const float r[9], const float t[3], 
  * brick: (2^depth+1)^3 floats, x fastest; tf: tf_n RGBA floats; viewport: W*H ARGB32, top row first. */
 void orc_render_block_argb8(const orc_view* v, const float* brick, uint32_t depth, const uint32_t idx[3],
                             const int32_t rect[4], const float* tf, uint32_t* viewport);
+
+/* Texture-unit weights (units of 1/256) of the 8 texels around texel coordinate tc in an
+ * n^3 clamped texture, whether each texel is in the NaN footprint, and its linear index. */
+void orc_tex3d_weights(const float tc[3], uint32_t n, int32_t w[8], uint8_t footprint[8], uint32_t texel[8]);
 
 /* ---- frame render in FP64, float RGBA out (batched-path semantics) ----
  * For each listed pixel: every block the ray enters, in ray order, is marched exactly as the

@@ -21,6 +21,8 @@ NO_FIELD_VALUE = 1e30
 MAX_DEPTH = 9
 
 BRICK_F32, BRICK_F16, BRICK_BF16 = 0, 1, 2
+FILTER_EXACT, FILTER_TEXTURE = 0, 1
+ABI_VERSION = 2
 
 u8p = C.POINTER(C.c_uint8)
 u16p = C.POINTER(C.c_uint16)
@@ -42,7 +44,7 @@ class View(C.Structure):
     _fields_ = [("cam", Camera), ("W", C.c_uint32), ("H", C.c_uint32), ("level", C.c_uint32),
                 ("field_min", C.c_float), ("field_max", C.c_float), ("threshold", C.c_float),
                 ("quality", C.c_float), ("tf_n", C.c_uint32), ("alpha_stop", C.c_float),
-                ("reserved", C.c_uint32 * 3)]
+                ("filter", C.c_uint32), ("reserved", C.c_uint32 * 2)]
 
 
 class FrameDesc(C.Structure):

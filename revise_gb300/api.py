@@ -261,11 +261,12 @@ class DenseFieldRenderer:
 class RenderSharedState:
     """The parts of s3vs::VsRenderSharedState (include/s3vs/VsRenderSharedState.hpp:29-46)
     the Argb path reads: field service (block nodes and values), camera/view and
-    transfer function."""
+    transfer function.  Samples are filtered as the reference's textures are
+    (S3R_FILTER_TEXTURE) unless filter says otherwise."""
 
-    def __init__(self, workload, alpha_stop: float = 2.0):
+    def __init__(self, workload, alpha_stop: float = 2.0, filter: int = _lib.FILTER_TEXTURE):
         self.w = workload
-        self.view = host.view_for(workload, alpha_stop)
+        self.view = host.view_for(workload, alpha_stop, filter)
         self.tf = workload.tf
         self.blocks = workload.blocks
         self.block_index = {(int(b[0]), int(b[1]), int(b[2])): i for i, b in enumerate(workload.blocks)}

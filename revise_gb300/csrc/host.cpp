@@ -74,6 +74,7 @@ struct s3r_plan {
     // graph of s3r_frame_run
     cudaGraphExec_t exec = nullptr;
     const void* g_key[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    uint32_t g_dims[4] = {0, 0, 0, 0}; // W, H, tf_n, filter the graph's launches were sized for
     uint32_t graph_kernels = 0;
 };
 
@@ -184,6 +185,8 @@ int check_view(s3r_ctx* ctx, const s3r_view* v)
     if (v->level > 12) return fail(ctx, S3R_ERR_INVALID, "level out of range");
     if (!(v->field_max > v->field_min)) return fail(ctx, S3R_ERR_INVALID, "field range is empty");
     if (!(v->quality > 0.f)) return fail(ctx, S3R_ERR_INVALID, "quality must be positive");
+    if (v->filter != S3R_FILTER_EXACT && v->filter != S3R_FILTER_TEXTURE)
+        return fail(ctx, S3R_ERR_INVALID, "unknown filter");
     return S3R_OK;
 }
 
@@ -548,7 +551,7 @@ int plan_launch_render(s3r_plan* p, const float* tf, float* rgba, uint32_t* argb
     fa.scale_offset = p->fmt == S3R_BRICK_F32 ? nullptr : p->scale_offset_dev;
     fa.cover = p->cover_dev;
     S3R_CUDA(p->ctx, launch_frame_render(fa, p->last_view.W, p->last_view.H, p->last_view.tf_n, p->fmt,
-                                         p->render_tile, s));
+                                         p->render_tile, p->last_view.filter, s));
     ++*kernels;
     return S3R_OK;
 }
@@ -1103,9 +1106,9 @@ int s3r_frame_run(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const floa
     cudaStream_t s = as_stream(stream);
     if ((rc = plan_stage_view(plan, view, s))) return rc;
     const void* key[5] = {sparse, tf, rgba, argb, samples};
+    const uint32_t dims[4] = {view->W, view->H, view->tf_n, view->filter};
     const bool same = plan->exec && std::memcmp(key, plan->g_key, sizeof(key)) == 0 &&
-                      plan->last_view.W == view->W && plan->last_view.H == view->H &&
-                      plan->last_view.tf_n == view->tf_n;
+                      std::memcmp(dims, plan->g_dims, sizeof(dims)) == 0;
     if (!same) {
         plan_drop_graph(plan);
         cudaStream_t cs = ctx->capture;
@@ -1127,6 +1130,7 @@ int s3r_frame_run(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const floa
             return cuda_fail(ctx, e, "cudaGraphInstantiate");
         }
         std::memcpy(plan->g_key, key, sizeof(key));
+        std::memcpy(plan->g_dims, dims, sizeof(dims));
         plan->graph_kernels = k;
     }
     S3R_CUDA(ctx, cudaGraphLaunch(plan->exec, s));
@@ -1214,6 +1218,8 @@ int s3r_render_argb_backward(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view,
     if (plan->fmt != S3R_BRICK_F32) return fail(ctx, S3R_ERR_UNSUPPORTED, "the adjoint needs FP32 bricks");
     int rc = check_view(ctx, view);
     if (rc) return rc;
+    if (view->filter != S3R_FILTER_EXACT)
+        return fail(ctx, S3R_ERR_UNSUPPORTED, "the adjoint needs S3R_FILTER_EXACT (texture weights are piecewise constant)");
     if (view->level != plan->level) return fail(ctx, S3R_ERR_INVALID, "view level differs from the plan level");
     if ((rc = set_device(ctx))) return rc;
     cudaStream_t s = as_stream(stream);

@@ -58,18 +58,25 @@ __global__ void scatter_kernel(float* grid, uint32_t e, const uint16_t* n2i, con
     grid[((uint64_t)z * e + y) * e + x] = sparse[i];
 }
 
+// put(): v may be +inf (internal no-field) or NaN; put_nan(): v is already NaN
+// wherever it is masked (see inf_to_nan), so the float store needs no test.
 template <typename OutT> struct Store;
 template <> struct Store<float> {
     __device__ static void put(float* out, uint64_t i, float v, float, float)
     {
         out[i] = isinf(v) ? qnan() : v;
     }
+    __device__ static void put_nan(float* out, uint64_t i, float v, float, float) { out[i] = v; }
 };
 template <> struct Store<__half> {
     __device__ static void put(__half* out, uint64_t i, float v, float inv_scale, float offset)
     {
         out[i] = (isinf(v) || isnan(v)) ? __ushort_as_half((unsigned short)0x7e00)
                                              : __float2half_rn((v - offset) * inv_scale);
+    }
+    __device__ static void put_nan(__half* out, uint64_t i, float v, float inv_scale, float offset)
+    {
+        out[i] = isnan(v) ? __ushort_as_half((unsigned short)0x7e00) : __float2half_rn((v - offset) * inv_scale);
     }
 };
 template <> struct Store<__nv_bfloat16> {
@@ -78,7 +85,17 @@ template <> struct Store<__nv_bfloat16> {
         out[i] = (isinf(v) || isnan(v)) ? __ushort_as_bfloat16((unsigned short)0x7fc0)
                                              : __float2bfloat16_rn((v - offset) * inv_scale);
     }
+    __device__ static void put_nan(__nv_bfloat16* out, uint64_t i, float v, float inv_scale, float offset)
+    {
+        out[i] = isnan(v) ? __ushort_as_bfloat16((unsigned short)0x7fc0)
+                          : __float2bfloat16_rn((v - offset) * inv_scale);
+    }
 };
+
+// +inf -> NaN in one FFMA, every other value (-0 included) unchanged:
+// 0 * v is +-0 for finite v (the sign of v, so v + 0 * v == v exactly) and NaN
+// for infinite v.
+__device__ __forceinline__ float inf_to_nan(float v) { return __fmaf_rn(0.f, v, v); }
 
 // Internally a masked value is +inf: every stencil sum that touches it is
 // +inf, which reproduces the reference's rule "any no-field value in the
@@ -269,7 +286,10 @@ template <bool kSlots> __device__ __forceinline__ void fill_cube(float v[27])
 // midpoint also read their 19 midpoint slots.  It computes its midpoints in
 // registers and stores the vertices it owns -- its low octant, plus the far
 // side where it is the last cube of the block along an axis -- with the
-// no-field -> NaN and 16-bit encoding fused into the store.
+// 16-bit encoding fused into the store.  Masked corners become NaN as they are
+// loaded, so unflagged cubes produce NaN directly (a NaN in a stencil sum gives
+// NaN as +inf gives +inf); flagged cubes test their slots for NaN ("no sparse
+// value") before any slot is overwritten, then turn masked sparse values to NaN.
 template <uint32_t T, typename OutT>
 __device__ __forceinline__ void finest_store(const float* s, const uint32_t* flags, OutT* out, uint64_t e,
                                              uint32_t ox, uint32_t oy, uint32_t oz, bool far_x, bool far_y,
@@ -288,7 +308,7 @@ __device__ __forceinline__ void finest_store(const float* s, const uint32_t* fla
 #pragma unroll
         for (int p = 0; p < 27; ++p) {
             const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
-            if (!((a | b | cc) & 1)) v[p] = s[S::idx(0, ci + (a >> 1), cj + (b >> 1), ck + (cc >> 1))];
+            if (!((a | b | cc) & 1)) v[p] = inf_to_nan(s[S::idx(0, ci + (a >> 1), cj + (b >> 1), ck + (cc >> 1))]);
         }
         if (has) {
 #pragma unroll
@@ -298,16 +318,26 @@ __device__ __forceinline__ void finest_store(const float* s, const uint32_t* fla
                 if (cls) v[p] = s[S::idx(cls, ci + (a >> 1), cj + (b >> 1), ck + (cc >> 1))];
             }
             fill_cube<true>(v);
+#pragma unroll
+            for (int p = 0; p < 27; ++p)
+                if ((p % 3) & 1 || ((p / 3) % 3) & 1 || (p / 9) & 1) v[p] = inf_to_nan(v[p]);
         } else {
             fill_cube<false>(v);
         }
-        const bool lx = far_x && ci == H - 1, ly = far_y && cj == H - 1, lz = far_z && ck == H - 1;
         OutT* base = out + ((uint64_t)(oz + 2 * ck) * e + (oy + 2 * cj)) * e + (ox + 2 * ci);
 #pragma unroll
         for (int p = 0; p < 27; ++p) {
             const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
-            if ((a < 2 || lx) && (b < 2 || ly) && (cc < 2 || lz))
-                Store<OutT>::put(base, (uint64_t)a + b * e + cc * e2, v[p], inv_scale, offset);
+            if (a < 2 && b < 2 && cc < 2) Store<OutT>::put_nan(base, (uint64_t)a + b * e + cc * e2, v[p], inv_scale, offset);
+        }
+        const bool lx = far_x && ci == H - 1, ly = far_y && cj == H - 1, lz = far_z && ck == H - 1;
+        if (lx || ly || lz) {
+#pragma unroll
+            for (int p = 0; p < 27; ++p) {
+                const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
+                if ((a == 2 || b == 2 || cc == 2) && (a < 2 || lx) && (b < 2 || ly) && (cc < 2 || lz))
+                    Store<OutT>::put_nan(base, (uint64_t)a + b * e + cc * e2, v[p], inv_scale, offset);
+            }
         }
     }
 }

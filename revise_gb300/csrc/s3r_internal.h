@@ -113,7 +113,7 @@ cudaError_t launch_block_ranges(const PlanBlock* blocks, uint32_t nblocks, const
 cudaError_t launch_render_block_argb(const s3r_view* view_host, const float* brick, const RenderBlock& rb,
                                      const float* tf, uint32_t* viewport, cudaStream_t s);
 cudaError_t launch_frame_render(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, uint32_t fmt,
-                                uint32_t tile_shape, cudaStream_t s);
+                                uint32_t tile_shape, uint32_t filter, cudaStream_t s);
 cudaError_t launch_frame_backward(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, cudaStream_t s);
 
 cudaError_t launch_bound_rect(const uint32_t* img, uint32_t W, uint32_t H, int32_t* rect_dev, cudaStream_t s);

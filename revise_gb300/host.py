@@ -24,7 +24,9 @@ def camera_look_at(eye, center, up, fovy_deg: float, W: int, H: int, ortho: bool
 
 
 def make_view(cam: Camera, W: int, H: int, level: int, field_min: float, field_max: float, threshold: float,
-              quality: float, tf_n: int, alpha_stop: float = 2.0) -> View:
+              quality: float, tf_n: int, alpha_stop: float = 2.0, filter: int = _lib.FILTER_EXACT) -> View:
+    """filter: _lib.FILTER_EXACT (exact FP32 filtering) or _lib.FILTER_TEXTURE (the texture
+    unit's filtering of the reference's textures, giving the reference's images)."""
     v = View()
     v.cam = cam
     v.W, v.H, v.level = W, H, level
@@ -32,14 +34,15 @@ def make_view(cam: Camera, W: int, H: int, level: int, field_min: float, field_m
     v.threshold, v.quality = threshold, quality
     v.tf_n = tf_n
     v.alpha_stop = alpha_stop
+    v.filter = filter
     return v
 
 
-def view_for(w, alpha_stop: float = 2.0) -> View:
+def view_for(w, alpha_stop: float = 2.0, filter: int = _lib.FILTER_EXACT) -> View:
     """The view of a revise_gb300.workloads.Workload."""
     cam = camera_look_at(w.eye, w.center, w.up, w.fovy, w.W, w.H, w.ortho, w.ortho_height)
     return make_view(cam, w.W, w.H, w.level, w.field_min, w.field_max, w.threshold, w.quality, w.tf.shape[0],
-                     alpha_stop)
+                     alpha_stop, filter)
 
 
 def block_cube(level: int, idx):

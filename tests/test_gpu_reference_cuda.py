@@ -33,34 +33,35 @@ def test_reference_cuda_interpolation_matches(ctx, seed):
         assert np.all(np.abs(got[m] - ref[m]) <= 1e-6 * np.maximum(np.abs(ref[m]), scale)), b
 
 
-def test_reference_cuda_render_matches_block_by_block(ctx):
-    """Whole worker frames, block by block in back-to-front order: the reference's
-    renderKernel<Argb> (texture-unit filtering with 8-bit fractions) against the
-    exact-FP32-filtering plain kernel; both quantize to ARGB8 after every block."""
+def test_texture_filter_matches_reference_cuda_renderer(ctx):
+    """The plain per-block kernel with S3R_FILTER_TEXTURE against the reference's
+    own renderKernel<Argb> (hardware tex3D/tex1D), block by block in back-to-front
+    order into one ARGB8 viewport, on scenes with masked nodes: equal but for
+    isolated 1-2 LSB differences (weighted sums rounded in another order, powf)."""
+    import sys
+    from pathlib import Path
     import torch
+    from revise_gb300 import _lib
     from revise_gb300.api import to_device_n2i
-    w = workloads.small(seed=2, level=1, depths=(3, 4), W=160, H=120, mask_fraction=0.1)
-    view = host.view_for(w)
-    w_tf = np.ascontiguousarray(w.tf, dtype=np.float32)
-    refcu.set_tf(w_tf)
-    order = host.b2f_order([0, 0, 0], [2, 2, 2], [-5.0] * 3, [5.0] * 3, w.eye)
-    idx = {tuple(b[:3]): i for i, b in enumerate(w.blocks.tolist())}
-    ref = np.zeros(w.W * w.H, np.uint32)
-    vp = torch.zeros(w.W * w.H, dtype=torch.int32, device="cuda")
-    tf = torch.from_numpy(w_tf).cuda()
-    for blk in order.tolist():
-        b = idx[tuple(blk)]
-        n2i, sp = w.block_nodes(b)
-        d = int(w.blocks[b, 3])
-        rect = host.block_view_rect(view, blk)
-        refcu.render_block(view, n2i, sp, d, blk, rect, ref)
-        dense = ctx.interp_dense(to_device_n2i(n2i), torch.from_numpy(sp).cuda(), d)
-        ctx.render_block_argb(view, dense, d, blk, rect, tf, vp)
-    got = vp.cpu().numpy().view(np.uint32)
-    a = got.view(np.uint8).reshape(-1, 4).astype(int)
-    r = ref.view(np.uint8).reshape(-1, 4).astype(int)
-    diff = np.abs(a - r).max(axis=1)
-    assert (ref >> 24).astype(bool).mean() > 0.05
-    # texture filtering quantizes interpolation fractions to 1/256: a few LSB where the field is steep
-    assert np.mean(diff) < 0.5, np.mean(diff)
-    assert np.percentile(diff, 99) <= 4, np.percentile(diff, 99)
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    import texture_variants as tv
+    for variant in tv.VARIANTS:
+        w = tv.workload(variant)
+        view = host.view_for(w, filter=_lib.FILTER_TEXTURE)
+        refcu.set_tf(w.tf)
+        ref = np.zeros(w.W * w.H, np.uint32)
+        vp = torch.zeros(w.W * w.H, dtype=torch.int32, device="cuda")
+        tf = torch.from_numpy(w.tf).cuda()
+        for b in tv.b2f_blocks(w):
+            n2i, sp = w.block_nodes(b)
+            d = int(w.blocks[b, 3])
+            blk = [int(x) for x in w.blocks[b, :3]]
+            rect = host.block_view_rect(view, blk)
+            refcu.render_block(view, n2i, sp, d, blk, rect, ref)
+            dense = ctx.interp_dense(to_device_n2i(n2i), torch.from_numpy(sp).cuda(), d)
+            ctx.render_block_argb(view, dense, d, blk, rect, tf, vp)
+        got = vp.cpu().numpy().view(np.uint32)
+        diff = np.abs(got.view(np.uint8).reshape(-1, 4).astype(int) - ref.view(np.uint8).reshape(-1, 4).astype(int)).max(1)
+        assert (ref >> 24).astype(bool).mean() > 0.05
+        assert diff.max() <= 2, (variant, diff.max())
+        assert (diff > 0).mean() < 0.01, (variant, (diff > 0).mean())

@@ -27,11 +27,12 @@ def _argb_diff(a, b):
     return np.abs(a - b).max(axis=1)
 
 
+@pytest.mark.parametrize("filt", [_lib.FILTER_EXACT, _lib.FILTER_TEXTURE])
 @pytest.mark.parametrize("seed", [0, 1])
-def test_plain_block_render_vs_oracle(ctx, seed):
+def test_plain_block_render_vs_oracle(ctx, seed, filt):
     import torch
     w = workloads.small(seed=seed, level=1, depths=(2, 3, 4), W=80, H=60)
-    view = host.view_for(w)
+    view = host.view_for(w, filter=filt)
     ov = oracle.view_from(view)
     dense = oracle.interp_workload(w)
     vo = w.vertex_off
@@ -73,10 +74,10 @@ def test_worker_scene_part_vs_oracle(ctx):
     assert diff.max() <= 1 and (diff > 0).mean() < 0.02
 
 
-def _frame(ctx, w, fmt=_lib.BRICK_F32, alpha_stop=2.0, tile=16):
+def _frame(ctx, w, fmt=_lib.BRICK_F32, alpha_stop=2.0, tile=16, filt=_lib.FILTER_EXACT):
     import torch
     from revise_gb300.api import FramePlan
-    view = host.view_for(w, alpha_stop)
+    view = host.view_for(w, alpha_stop, filt)
     plan = FramePlan(ctx, w, fmt, tile_cells=tile)
     sp = _dev(w.sparse)
     tf = _dev(w.tf)
@@ -89,10 +90,11 @@ def _frame(ctx, w, fmt=_lib.BRICK_F32, alpha_stop=2.0, tile=16):
     return plan, view, rgba.cpu().numpy().reshape(-1, 4), argb.cpu().numpy().view(np.uint32), int(samples.item())
 
 
+@pytest.mark.parametrize("filt", [_lib.FILTER_EXACT, _lib.FILTER_TEXTURE])
 @pytest.mark.parametrize("name", ["small", "cfg1"])
-def test_frame_render_vs_fp64_oracle(ctx, name):
+def test_frame_render_vs_fp64_oracle(ctx, name, filt):
     w = workloads.small(seed=5, level=1, depths=(2, 3, 4, 5), W=96, H=64) if name == "small" else workloads.cfg1()
-    plan, view, img, argb, samples = _frame(ctx, w)
+    plan, view, img, argb, samples = _frame(ctx, w, filt=filt)
     ov = oracle.view_from(view)
     ref, flags = oracle.render_frame_f64(ov, w, oracle.interp_workload(w), _rects(w, view), w.tf)
     assert ref[:, 3].max() > 0.1 and samples > 0
@@ -222,3 +224,46 @@ def test_render_tiles_agree(ctx):
             continue
         d = float((img - base).abs().max())
         assert d == 0.0 if rt < 4 else d <= 1e-5, (rt, d)
+
+
+def test_graph_recaptured_when_viewport_tf_size_or_filter_change(ctx):
+    """Same buffers, different W x H, tf_n or filter between replays: each replay
+    must equal a direct render of its own view (the graph's launch dimensions and
+    shared-memory size follow the view)."""
+    import torch
+    from revise_gb300.api import FramePlan
+    w = workloads.small(seed=14, level=1, depths=(2, 3), W=96, H=72)
+    plan = FramePlan(ctx, w)
+    sp = _dev(w.sparse)
+    tf512 = _dev(host.make_color_transfer(*workloads.colormap_points(), 512))
+    a = torch.zeros(128 * 96 * 4, device="cuda")
+    b = torch.zeros_like(a)
+    for (W, H, n, f) in ((96, 72, 256, 0), (128, 96, 256, 0), (128, 96, 512, 0), (128, 96, 512, 1), (96, 72, 512, 1)):
+        w.W, w.H = W, H
+        w.tf = np.zeros((n, 4), np.float32)  # only its length enters the view
+        view = host.view_for(w, filter=f)
+        a.zero_()
+        b.zero_()
+        plan.run(view, sp, tf512, b)
+        plan.interp(sp)
+        plan.render(view, tf512, a)
+        torch.cuda.synchronize()
+        assert torch.equal(a, b), (W, H, n, f)
+        assert float(a[:W * H * 4].view(-1, 4)[:, 3].max()) > 0.05
+    plan.close()
+
+
+def test_adjoint_rejects_texture_filter(ctx):
+    import torch
+    from revise_gb300.api import FramePlan
+    w = workloads.small(seed=15, level=1, depths=(2,), W=32, H=24)
+    plan = FramePlan(ctx, w)
+    plan.interp(_dev(w.sparse))
+    view = host.view_for(w, filter=_lib.FILTER_TEXTURE)
+    tf = _dev(w.tf)
+    img = torch.zeros(w.W * w.H * 4, device="cuda")
+    bricks, _ = plan.bricks()
+    with pytest.raises(_lib.S3RError) as e:
+        plan.backward(view, tf, img, img, torch.zeros(w.tf.size, device="cuda"), torch.zeros(bricks.numel(), device="cuda"))
+    assert e.value.code == _lib.S3R_ERR_UNSUPPORTED
+    plan.close()
