@@ -296,7 +296,8 @@ int s3r_frame_run(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const floa
  * given the forward image rgba (device) and dl_drgba = I - target (device,
  * W*H*4), accumulates dL/dtf (device, tf_n*4 floats) and dL/ddense (device,
  * one float per brick vertex).  Sample positions are recomputed per ray.
- * view->filter must be S3R_FILTER_EXACT (else S3R_ERR_UNSUPPORTED). */
+ * view->filter must be S3R_FILTER_EXACT (else S3R_ERR_UNSUPPORTED).
+ * Allocates its scratch (512 copies of the table gradient) on the first call. */
 int s3r_render_argb_backward(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* tf,
                              const float* rgba, const float* dl_drgba, float* dtf, float* ddense, void* stream);
 

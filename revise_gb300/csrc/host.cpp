@@ -73,6 +73,8 @@ struct s3r_plan {
     s3r_view last_view{};
     // graph of s3r_frame_run
     cudaGraphExec_t exec = nullptr;
+    float* dtf_part = nullptr; // adjoint: kDtfParts copies of the transfer-function gradient
+    size_t dtf_part_floats = 0;
     const void* g_key[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     uint32_t g_dims[4] = {0, 0, 0, 0}; // W, H, tf_n, filter the graph's launches were sized for
     uint32_t graph_kernels = 0;
@@ -1030,6 +1032,7 @@ int s3r_plan_destroy(s3r_plan* p)
     if (p->view_pinned) cudaFreeHost(p->view_pinned);
     if (p->cover_pinned) cudaFreeHost(p->cover_pinned);
     f(p->cover_dev);
+    f(p->dtf_part);
     if (p->staged) cudaEventDestroy(p->staged);
     delete p;
     return S3R_OK;
@@ -1233,8 +1236,21 @@ int s3r_render_argb_backward(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view,
     fa.dl_drgba = dl_drgba;
     fa.dtf = dtf;
     fa.ddense = ddense;
+    const size_t nparts = (size_t)kDtfParts * 4 * view->tf_n;
+    if (plan->dtf_part_floats < nparts) {
+        // allocation: synchronizes the device once, on the first adjoint call (or a larger table)
+        if (plan->dtf_part) cudaFree(plan->dtf_part);
+        plan->dtf_part = nullptr;
+        plan->dtf_part_floats = 0;
+        cudaError_t e = cudaMalloc(&plan->dtf_part, nparts * sizeof(float));
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(transfer-function gradient copies)");
+        plan->dtf_part_floats = nparts;
+    }
+    fa.dtf_part = plan->dtf_part;
+    S3R_CUDA(ctx, cudaMemsetAsync(plan->dtf_part, 0, nparts * sizeof(float), s));
     S3R_CUDA(ctx, launch_frame_backward(fa, view->W, view->H, view->tf_n, s));
-    ++ctx->launches;
+    S3R_CUDA(ctx, launch_dtf_reduce(plan->dtf_part, dtf, 4 * view->tf_n, s));
+    ctx->launches += 2;
     return S3R_OK;
 }
 

@@ -632,17 +632,24 @@ __global__ void frame_render_kernel(FrameArgs fa)
 //   dA/da_k = (1 - A) / (1 - a_k),
 // a_k = 1 - (1 - alpha_tf * of)^il, c_k / alpha_tf linear in the table
 // entries around v01, v01 linear in the trilinear value.
-__global__ void frame_backward_kernel(FrameArgs fa)
+__global__ void __launch_bounds__(128, 5) frame_backward_kernel(FrameArgs fa)
 {
     extern __shared__ float4 sm[];
     const s3r_view v = *fa.view;
     float4* tf = sm;
-    float* dtf_s = reinterpret_cast<float*>(sm + v.tf_n);
     const uint32_t nthreads = blockDim.x * blockDim.y;
     const uint32_t tid = threadIdx.y * blockDim.x + threadIdx.x;
     for (uint32_t i = tid; i < v.tf_n; i += nthreads) tf[i] = reinterpret_cast<const float4*>(fa.tf)[i];
-    for (uint32_t i = tid; i < 4 * v.tf_n; i += nthreads) dtf_s[i] = 0.f;
     __syncthreads();
+    // The transfer-function gradient goes to one of kDtfParts copies in global
+    // memory, an RGBA float4 reduction per table entry (fire and forget).  The copy
+    // is picked by CTA (modulo kDtfCtaGroups) and by lane (modulo kDtfLaneGroups):
+    // neighbouring rays -- neighbouring lanes -- add to the same entry at the same
+    // time, and reductions on one address serialize.  (Shared-memory atomics
+    // stalled the warps on exactly those collisions.)
+    float4* dtf4 = reinterpret_cast<float4*>(fa.dtf_part) +
+                   (size_t)(((blockIdx.y * gridDim.x + blockIdx.x) % kDtfCtaGroups) * kDtfLaneGroups +
+                            (tid & 31) % kDtfLaneGroups) * v.tf_n;
     const uint32_t vx = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t vy = blockIdx.y * blockDim.y + threadIdx.y;
     if (vx < v.W && vy < v.H) {
@@ -673,9 +680,10 @@ __global__ void frame_backward_kernel(FrameArgs fa)
             auto flush_tf = [&]() {
                 if (tf_i0 == 0xffffffffu) return;
 #pragma unroll
+                atomicAdd(&dtf4[tf_i0], make_float4(tf_a[0], tf_a[1], tf_a[2], tf_a[3]));
+                atomicAdd(&dtf4[tf_i1], make_float4(tf_b[0], tf_b[1], tf_b[2], tf_b[3]));
+#pragma unroll
                 for (int ch = 0; ch < 4; ++ch) {
-                    if (tf_a[ch] != 0.f) atomicAdd(&dtf_s[4 * tf_i0 + ch], tf_a[ch]);
-                    if (tf_b[ch] != 0.f) atomicAdd(&dtf_s[4 * tf_i1 + ch], tf_b[ch]);
                     tf_a[ch] = 0.f;
                     tf_b[ch] = 0.f;
                 }
@@ -720,12 +728,33 @@ __global__ void frame_backward_kernel(FrameArgs fa)
                     }
                     g_a += gA * (1.f - A) * inv_om;
                     g_col[3] = g_a * dadc;
-                    // transfer-function table: consecutive samples of a ray usually fall
-                    // between the same two entries; accumulate them in registers and
-                    // flush to shared memory when the pair changes
+                    // transfer-function table: accumulate the two entries of the current
+                    // pair in registers; when the pair changes, an entry the new pair
+                    // shares (a ray moving to the next interval) keeps its sum and only
+                    // the other one goes to shared memory
                     const float f = ts.f;
                     if (ts.i0 != tf_i0 || ts.i1 != tf_i1) {
-                        flush_tf();
+                        if (tf_i0 != 0xffffffffu && ts.i0 == tf_i1 && ts.i0 != ts.i1) {
+                            // moving up: old i1 becomes new i0
+#pragma unroll
+                            atomicAdd(&dtf4[tf_i0], make_float4(tf_a[0], tf_a[1], tf_a[2], tf_a[3]));
+#pragma unroll
+                            for (int ch = 0; ch < 4; ++ch) {
+                                tf_a[ch] = tf_b[ch];
+                                tf_b[ch] = 0.f;
+                            }
+                        } else if (tf_i0 != 0xffffffffu && ts.i1 == tf_i0 && ts.i0 != ts.i1) {
+                            // moving down: old i0 becomes new i1
+#pragma unroll
+                            atomicAdd(&dtf4[tf_i1], make_float4(tf_b[0], tf_b[1], tf_b[2], tf_b[3]));
+#pragma unroll
+                            for (int ch = 0; ch < 4; ++ch) {
+                                tf_b[ch] = tf_a[ch];
+                                tf_a[ch] = 0.f;
+                            }
+                        } else {
+                            flush_tf();
+                        }
                         tf_i0 = ts.i0;
                         tf_i1 = ts.i1;
                     }
@@ -762,11 +791,15 @@ __global__ void frame_backward_kernel(FrameArgs fa)
             flush_tf();
         }
     }
-    __syncthreads();
-    for (uint32_t i = tid; i < 4 * v.tf_n; i += nthreads) {
-        const float g = dtf_s[i];
-        if (g != 0.f) atomicAdd(&fa.dtf[i], g);
-    }
+}
+
+__global__ void dtf_reduce_kernel(const float* __restrict__ part, float* __restrict__ dtf, uint32_t n)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float g = 0.f;
+    for (uint32_t p = 0; p < kDtfParts; ++p) g += part[(size_t)p * n + i];
+    dtf[i] += g;
 }
 
 } // namespace
@@ -825,13 +858,19 @@ cudaError_t launch_frame_backward(const FrameArgs& a, uint32_t W, uint32_t H, ui
 {
     dim3 block(16, 8);
     dim3 grid((W + 15) / 16, (H + 7) / 8);
-    const size_t smem = tf_n * sizeof(float4) * 2;
+    const size_t smem = tf_n * sizeof(float4);
     if (smem > 48 * 1024) {
         cudaError_t err =
             cudaFuncSetAttribute(frame_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (err != cudaSuccess) return err;
     }
     frame_backward_kernel<<<grid, block, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dtf_reduce(const float* part, float* dtf, uint32_t n, cudaStream_t s)
+{
+    dtf_reduce_kernel<<<(n + 255) / 256, 256, 0, s>>>(part, dtf, n);
     return cudaGetLastError();
 }
 

@@ -92,7 +92,14 @@ struct FrameArgs {
     const float* dl_drgba;
     float* dtf;
     float* ddense;
+    float* dtf_part;      // kDtfParts zeroed copies of dtf (tf_n RGBA float4 each), summed into dtf afterwards
 };
+
+// The adjoint spreads its transfer-function gradient over kDtfParts copies
+// (CTA index modulo kDtfCtaGroups, lane modulo kDtfLaneGroups) so that global
+// reductions to one table entry rarely meet; a last kernel sums the copies.
+constexpr uint32_t kDtfCtaGroups = 64, kDtfLaneGroups = 8;
+constexpr uint32_t kDtfParts = kDtfCtaGroups * kDtfLaneGroups;
 
 // Records a failure for s3r_last_error(NULL) and returns code (host.cpp).
 int record_error(int code, const char* msg);
@@ -115,6 +122,8 @@ cudaError_t launch_render_block_argb(const s3r_view* view_host, const float* bri
 cudaError_t launch_frame_render(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, uint32_t fmt,
                                 uint32_t tile_shape, uint32_t filter, cudaStream_t s);
 cudaError_t launch_frame_backward(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, cudaStream_t s);
+// dtf[i] += sum over the kDtfParts copies of part[. * n + i], n = 4 * tf_n
+cudaError_t launch_dtf_reduce(const float* part, float* dtf, uint32_t n, cudaStream_t s);
 
 cudaError_t launch_bound_rect(const uint32_t* img, uint32_t W, uint32_t H, int32_t* rect_dev, cudaStream_t s);
 cudaError_t launch_crop(const uint32_t* img, uint32_t W, const int32_t rect[4], uint32_t* dst, cudaStream_t s);
