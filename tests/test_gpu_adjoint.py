@@ -109,3 +109,33 @@ def test_adjoint_vs_central_differences(ctx):
     # piecewise-linear transfer functions put kinks inside some +-eps intervals
     assert np.median(errs) < REL_TOL, np.sort(errs)
     assert np.mean(errs < 1e-2) >= 0.9, np.sort(errs)
+
+
+def test_autograd_binding_matches_the_adjoint(ctx):
+    """torch.autograd through revise_gb300.autograd.render_frame gives the same
+    gradients as calling s3r_render_argb_backward directly (reductions run in
+    another order between the two calls: 1e-5 relative)."""
+    import torch
+    from revise_gb300.api import FramePlan
+    from revise_gb300.autograd import render_frame
+    w = _setup(64, 64)
+    view = host.view_for(w)
+    plan = FramePlan(ctx, w)
+    plan.interp(torch.from_numpy(w.sparse).cuda())
+    bricks, _ = plan.bricks()
+    bricks.requires_grad_(True)
+    tf = torch.from_numpy(np.ascontiguousarray(w.tf)).cuda().requires_grad_(True)
+    target = torch.rand(w.H, w.W, 4, device="cuda")
+    img = render_frame(plan, view, tf, bricks)
+    loss = 0.5 * ((img - target) ** 2).sum()
+    loss.backward()
+    rgba = img.detach().reshape(-1).contiguous()
+    dl = (img.detach() - target).reshape(-1).contiguous()
+    dtf = torch.zeros(w.tf.size, device="cuda")
+    dd = torch.zeros(bricks.numel(), device="cuda")
+    plan.backward(view, tf.detach(), rgba, dl, dtf, dd)
+    torch.cuda.synchronize()
+    assert float(tf.grad.abs().max()) > 0
+    assert torch.allclose(tf.grad.reshape(-1), dtf, rtol=1e-5, atol=1e-6 * float(dtf.abs().max()))
+    assert torch.allclose(bricks.grad, dd, rtol=1e-5, atol=1e-6 * float(dd.abs().max()))
+    plan.close()
