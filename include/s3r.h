@@ -21,6 +21,9 @@
  *   s3r_clear_viewport         DenseFieldRenderer_cu::clearViewport (src/s3dmm_cuda/DenseFieldRenderer_cu.cu:268-277)
  *   s3r_render_block_argb      DenseFieldRenderer_cu::renderDenseField, Argb mode
  *                              (src/s3dmm_cuda/DenseFieldRenderer_cu.cu:279-486, renderArgb.hpp:30-55)
+ *   s3r_render_block           renderDenseField in every field mode (s3vs::FieldMode,
+ *                              include/s3vs/FieldMode.hpp:26-54; render*.hpp, cuda_lighting.hpp)
+ *   s3r_default_light          the renderer's single light source (DenseFieldRenderer_cu.cu:440-445)
  *   s3r_block_cube,
  *   s3r_block_view_rect,
  *   s3r_camera_look_at         the host-side parameter set-up of renderDenseField (:317-409, :353-372)
@@ -28,6 +31,7 @@
  *   s3r_bound_rect             getBoundRect (src/s3vs_worker/cuda/VsWorker_cu.cpp:51-88)
  *   s3r_blend_image_part_host,
  *   s3r_compose_parts          blendImagePart (src/s3vs_lib/BlendImagePart.hpp:61-145)
+ *   s3r_blend_image_part_mip_host  blendImagePartMaxIntensity (src/s3vs_lib/BlendImagePart.hpp:148-191)
  *   s3r_make_color_transfer    makeColorTransferVector (include/s3vs/ColorTransferFunction.hpp:27-69)
  *   s3r_frame_*                no single counterpart: the batched form of VsWorker_cu::renderScenePart
  *                              (src/s3vs_worker/cuda/VsWorker_cu.cpp:225-313) over a whole block cube
@@ -43,7 +47,7 @@
 extern "C" {
 #endif
 
-#define S3R_ABI_VERSION 2
+#define S3R_ABI_VERSION 3
 
 /* status codes */
 #define S3R_OK 0
@@ -179,6 +183,57 @@ int s3r_render_block_argb(s3r_ctx* ctx, const s3r_view* view, const float* brick
                           const uint32_t idx[3], const int32_t rect[4], const float* tf, uint32_t* viewport,
                           void* stream);
 
+/* Field modes, numbered as s3vs::FieldMode (include/s3vs/FieldMode.hpp:26-54). */
+#define S3R_MODE_ISOSURFACE 0u            /* one isosurface at view.threshold, lit */
+#define S3R_MODE_ISOSURFACES 1u           /* isosurfaces at presentation.levels, lit */
+#define S3R_MODE_MAX_INTENSITY 2u         /* maximum value above view.threshold; the pixel holds float bits */
+#define S3R_MODE_ARGB 3u                  /* volume rendering (s3r_render_block_argb) */
+#define S3R_MODE_ARGB_LIGHT 4u            /* volume rendering, every sample lit */
+#define S3R_MODE_DOMAIN_VOXELS 5u         /* constant colour where the field is defined */
+#define S3R_MODE_VALUE_ON_ISOSURFACE 6u   /* secondary field's colour on one isosurface of the primary */
+#define S3R_MODE_VALUE_ON_ISOSURFACES 7u  /* secondary field's colour on several isosurfaces */
+
+#define S3R_MAX_LEVELS 50u                /* RenderKernelPresentationParam::MaxLevels */
+#define S3R_MAX_LIGHTS 10u                /* RenderKernelLightsParam::MaxSources */
+
+/* A light source (LightSource, RenderKernelParam.hpp:68-74), world coordinates. */
+typedef struct s3r_light {
+    float pos[3];
+    float ambient[3];
+    float diffuse[3];
+    float specular[3];
+} s3r_light;
+
+/* What a field mode needs beyond s3r_view (RenderKernelPresentationParam and
+ * RenderKernelLightsParam): view.threshold is the isosurface level (absolute)
+ * in the single-isosurface modes and the opacity threshold otherwise, as the
+ * reference sets it (DenseFieldRenderer_cu.cu:418-434). */
+typedef struct s3r_presentation {
+    uint32_t mode;                   /* S3R_MODE_* */
+    float isosurface_opacity;        /* multiplies the transfer-function alpha on isosurfaces */
+    uint32_t level_count;            /* isosurface levels, absolute, ascending and distinct, <= S3R_MAX_LEVELS */
+    float levels[50];
+    uint32_t light_count;            /* <= S3R_MAX_LIGHTS */
+    s3r_light lights[10];
+    float secondary_min;             /* secondary field range (value-on-isosurface modes) */
+    float secondary_max;
+} s3r_presentation;
+
+/* The renderer's light: at eye + n + e2 * h, no ambient, diffuse 1, specular 0.1. */
+int s3r_default_light(const s3r_view* view, s3r_light* out);
+
+/* Ray-casts one block in any field mode into the viewport, as renderKernel<mode>
+ * does (DenseFieldRenderer_cu.cu:62-215 with render*.hpp): the same ray set-up,
+ * sampling (view.filter) and compositing as s3r_render_block_argb; lit modes
+ * shade with a central-difference gradient of the field (+-0.1 texel) and the
+ * Blinn model of cuda_lighting.hpp.  brick2: the secondary field's brick on the
+ * same block (value-on-isosurface modes, else NULL).  S3R_MODE_MAX_INTENSITY
+ * writes float bits (field value mapped to [0, 1], or the previous pixel) that
+ * s3r_blend_image_part_mip_host composes. */
+int s3r_render_block(s3r_ctx* ctx, const s3r_view* view, const s3r_presentation* pres, const float* brick,
+                     const float* brick2, uint32_t depth, const uint32_t idx[3], const int32_t rect[4],
+                     const float* tf, uint32_t* viewport, void* stream);
+
 /* ----------------------------------------------------------- ordering */
 
 /* Back-to-front order of the blocks of index box [bmin, bmax) whose world box
@@ -204,6 +259,11 @@ int s3r_crop(s3r_ctx* ctx, const uint32_t* image, uint32_t W, const int32_t rect
 /* Host restatement of blendImagePart: src (sw x sh at origin ox, oy) over dst (dw x dh). */
 int s3r_blend_image_part_host(uint32_t* dst, int32_t dw, int32_t dh, const uint32_t* src, int32_t sw, int32_t sh,
                               int32_t ox, int32_t oy, int32_t just_copy, int32_t offx, int32_t offy);
+
+/* Host restatement of blendImagePartMaxIntensity: pixels hold floats; a non-NaN
+ * source replaces a NaN or smaller destination. */
+int s3r_blend_image_part_mip_host(float* dst, int32_t dw, int32_t dh, const float* src, int32_t sw, int32_t sh,
+                                  int32_t ox, int32_t oy, int32_t just_copy, int32_t offx, int32_t offy);
 
 /* One image part for s3r_compose_parts: a device ARGB32 image at an origin. */
 typedef struct s3r_image_part {

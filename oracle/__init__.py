@@ -153,6 +153,36 @@ def tex3d_weights(tc, n: int):
     return np.array(w[:]), np.array(f[:], dtype=bool), np.array(i[:])
 
 
+class OrcLight(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("ambient", C.c_float * 3), ("diffuse", C.c_float * 3),
+                ("specular", C.c_float * 3)]
+
+
+class OrcPresentation(C.Structure):
+    _fields_ = [("mode", C.c_uint32), ("isosurface_opacity", C.c_float), ("level_count", C.c_uint32),
+                ("levels", C.c_float * 50), ("light_count", C.c_uint32), ("lights", OrcLight * 10),
+                ("secondary_min", C.c_float), ("secondary_max", C.c_float)]
+
+
+def presentation_from(p) -> OrcPresentation:
+    """OrcPresentation from a revise_gb300._lib.Presentation (same fields)."""
+    o = OrcPresentation()
+    C.memmove(C.byref(o), C.byref(p), C.sizeof(o))
+    return o
+
+
+def render_block_mode(view: OrcView, pres: OrcPresentation, brick: np.ndarray, depth: int, idx, rect,
+                      tf: np.ndarray, viewport: np.ndarray, brick2: np.ndarray = None) -> None:
+    brick = np.ascontiguousarray(brick, dtype=np.float32)
+    b2 = None if brick2 is None else np.ascontiguousarray(brick2, dtype=np.float32)
+    tf = np.ascontiguousarray(tf, dtype=np.float32)
+    i = (C.c_uint32 * 3)(*idx)
+    r = (C.c_int32 * 4)(*[int(x) for x in rect])
+    port().orc_render_block_mode(C.byref(view), C.byref(pres), _p(brick, C.c_float),
+                                 _p(b2, C.c_float) if b2 is not None else None, C.c_uint32(depth), i, r,
+                                 _p(tf, C.c_float), _p(viewport, C.c_uint32))
+
+
 def _frame_args(w, dense, rects):
     blocks = np.ascontiguousarray(w.blocks, dtype=np.uint32)
     off = np.ascontiguousarray(w.vertex_off[:-1], dtype=np.uint64)

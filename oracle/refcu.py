@@ -89,3 +89,18 @@ def worker(view, w, order_idx, rects):
                                _p(node_off, C.c_uint64), _p(n2i, C.c_uint16), _p(sparse, C.c_float),
                                _p(rects, C.c_int32), _p(vp, C.c_uint32), crop, C.byref(ms)))
     return vp, tuple(crop[:]), ms.value
+
+
+def render_block_mode(view, pres, n2i, sparse, depth, idx, rect, viewport, sparse2=None):
+    """renderKernel<pres.mode> for one block into a host ARGB32 viewport (in place);
+    pres: a revise_gb300._lib.Presentation; sparse2: the secondary field's node values."""
+    lib = load()
+    n2i = np.ascontiguousarray(n2i, dtype=np.uint16)
+    sparse = np.ascontiguousarray(sparse, dtype=np.float32)
+    s2 = None if sparse2 is None else np.ascontiguousarray(sparse2, dtype=np.float32)
+    i = (C.c_uint32 * 3)(*[int(x) for x in idx])
+    r = (C.c_int32 * 4)(*[int(x) for x in rect])
+    _check(lib.ref_cuda_render_block_mode(C.byref(view), C.byref(pres), _p(n2i, C.c_uint16), _p(sparse, C.c_float),
+                                          _p(s2, C.c_float) if s2 is not None else None,
+                                          C.c_uint32(sparse.shape[0]), C.c_uint32(depth), i, r,
+                                          _p(viewport, C.c_uint32)))

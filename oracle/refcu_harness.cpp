@@ -91,7 +91,19 @@ struct RenderKernelParam {
 struct Kernels {
     CUmodule interp = nullptr, render = nullptr;
     CUfunction fill = nullptr, scatter = nullptr, level = nullptr, nan = nullptr, argb = nullptr;
+    CUfunction mode[8] = {};  // renderKernel<FieldMode(m)>
 } K;
+
+// The product's s3r_presentation (include/s3r.h), field for field.
+struct Pres {
+    uint32_t mode;
+    float isosurface_opacity;
+    uint32_t level_count;
+    float levels[50];
+    uint32_t light_count;
+    struct { float pos[3], ambient[3], diffuse[3], specular[3]; } lights[10];
+    float secondary_min, secondary_max;
+};
 
 // View of the camera, as the product's s3r_view lays it out (include/s3r.h).
 struct View {
@@ -162,7 +174,7 @@ struct Array3 {
         a = nullptr;
         edge = 0;
     }
-} g_field;
+} g_field, g_field2;
 
 struct TfTexture {
     cudaArray_t a = nullptr;
@@ -201,9 +213,10 @@ int launch(CUfunction f, dim3 g, dim3 b, void** args)
     return 0;
 }
 
-// DenseFieldInterpolatorArr_cu_3::interpolate into g_field.
-int interp_into_field(const uint16_t* n2i, const float* sparse, uint32_t n, uint32_t depth)
+// DenseFieldInterpolatorArr_cu_3::interpolate into dst (g_field: primary, g_field2: secondary).
+int interp_into(Array3& dst, const uint16_t* n2i, const float* sparse, uint32_t n, uint32_t depth)
 {
+    Array3& g_field = dst;
     const unsigned e = (1u << depth) + 1u;
     if (g_field.resize(e)) return 1;
     // fill(verticesPerEdge, array, NAN): 8^3 blocks
@@ -248,8 +261,14 @@ int interp_into_field(const uint16_t* n2i, const float* sparse, uint32_t n, uint
     return 0;
 }
 
-// renderKernel<Argb> for one block (DenseFieldRenderer_cu.cu:317-482).
-int render_block(const View& v, uint32_t depth, const uint32_t idx[3], const int32_t rect[4], uint32_t* viewport_dev)
+int interp_into_field(const uint16_t* n2i, const float* sparse, uint32_t n, uint32_t depth)
+{
+    return interp_into(g_field, n2i, sparse, n, depth);
+}
+
+// renderKernel<mode> for one block (DenseFieldRenderer_cu.cu:317-482); pres == nullptr: Argb.
+int render_block(const View& v, uint32_t depth, const uint32_t idx[3], const int32_t rect[4], uint32_t* viewport_dev,
+                 const Pres* pres = nullptr)
 {
     if (rect[2] <= 0 || rect[3] <= 0) return 0;
     RenderKernelParam p;
@@ -274,12 +293,29 @@ int render_block(const View& v, uint32_t depth, const uint32_t idx[3], const int
     p.presentation.colorTex = g_tf.tex;
     p.presentation.quality = v.quality;
     p.lights.sourceCount = 1;
+    CUfunction kern = K.argb;
+    if (pres) {
+        if (pres->mode > 7 || !K.mode[pres->mode]) return fail("no kernel for mode " + std::to_string(pres->mode));
+        kern = K.mode[pres->mode];
+        p.presentation.isosurfaceOpacity = pres->isosurface_opacity;
+        p.presentation.levelCount = pres->level_count;
+        for (unsigned i = 0; i < pres->level_count && i < 50; ++i) p.presentation.levels[i] = pres->levels[i];
+        p.lights.sourceCount = pres->light_count;
+        for (unsigned i = 0; i < pres->light_count && i < 10; ++i) {
+            const auto& L = pres->lights[i];
+            p.lights.sources[i].pos = make_float3(L.pos[0], L.pos[1], L.pos[2]);
+            p.lights.sources[i].ambient = make_float3(L.ambient[0], L.ambient[1], L.ambient[2]);
+            p.lights.sources[i].diffuse = make_float3(L.diffuse[0], L.diffuse[1], L.diffuse[2]);
+            p.lights.sources[i].specular = make_float3(L.specular[0], L.specular[1], L.specular[2]);
+        }
+        p.secondaryField = {g_field2.tex, depth, pres->secondary_min, pres->secondary_max};
+    }
     // chooseKernelDim1d(view.W, 32), chooseKernelDim1d(view.H, 1)
     const unsigned W = rect[2], H = rect[3];
     dim3 grid(W <= 32 ? 1 : blocks_for(W, 32), H <= 1 ? 1 : H);
     dim3 block(W <= 32 ? W : 32, H <= 1 ? H : 1);
     void* args[] = {&p};
-    return launch(K.argb, grid, block, args);
+    return launch(kern, grid, block, args);
 }
 
 } // namespace
@@ -299,6 +335,10 @@ int ref_cuda_init(const char* interp_cubin, const char* render_cubin)
         find(K.interp, "transformInPlaceKernel", "ReplaceNoFieldValueWithNan", &K.nan) ||
         find(K.render, "renderKernel", "FieldModeE3", &K.argb))
         return 1;
+    for (int m = 0; m < 8; ++m) {
+        const std::string tag = "FieldModeE" + std::to_string(m) + "E";
+        if (find(K.render, "renderKernel", tag.c_str(), &K.mode[m])) return 1;
+    }
     size_t off = 0, size = 0;
     CKD(cuFuncGetParamInfo(K.argb, 0, &off, &size));
     if (size != sizeof(RenderKernelParam))
@@ -333,6 +373,25 @@ int ref_cuda_render_block(const void* view, const uint16_t* n2i, const float* sp
     CKR(cudaMalloc(&d, bytes));
     CKR(cudaMemcpy(d, viewport, bytes, cudaMemcpyHostToDevice));
     if (render_block(v, depth, idx, rect, d)) return 1;
+    CKR(cudaMemcpy(viewport, d, bytes, cudaMemcpyDeviceToHost));
+    CKR(cudaFree(d));
+    return 0;
+}
+
+// One block in any field mode (pres: the product's s3r_presentation); sparse2:
+// the secondary field's node values (same nodes) or NULL.
+int ref_cuda_render_block_mode(const void* view, const void* pres, const uint16_t* n2i, const float* sparse,
+                               const float* sparse2, uint32_t n, uint32_t depth, const uint32_t idx[3],
+                               const int32_t rect[4], uint32_t* viewport)
+{
+    const View& v = *static_cast<const View*>(view);
+    if (interp_into(g_field, n2i, sparse, n, depth)) return 1;
+    if (sparse2 && interp_into(g_field2, n2i, sparse2, n, depth)) return 1;
+    uint32_t* d = nullptr;
+    const size_t bytes = (size_t)v.W * v.H * 4;
+    CKR(cudaMalloc(&d, bytes));
+    CKR(cudaMemcpy(d, viewport, bytes, cudaMemcpyHostToDevice));
+    if (render_block(v, depth, idx, rect, d, static_cast<const Pres*>(pres))) return 1;
     CKR(cudaMemcpy(viewport, d, bytes, cudaMemcpyDeviceToHost));
     CKR(cudaFree(d));
     return 0;

@@ -453,10 +453,18 @@ static void march_block_f32(const orc_view* v, const orc_ray* r, const float* br
     const float of = opacity_factor(v);
     const float il = layer_exponent(v, depth);
     rgba[0] = rgba[1] = rgba[2] = rgba[3] = 0.f;
+    float tp[3] = {r->p0[0], r->p0[1], r->p0[2]}; /* texture filter: accumulated position */
     for (int i = 1; i < r->sample_count; ++i) {
         float tc[3];
         float val;
-        sample_coord(r, i - 1, tc);
+        if (tex) {
+            for (int d = 0; d < 3; ++d) {
+                tc[d] = (tp[d] - r->origin[d]) * r->factor;
+                tp[d] += r->step[d];
+            }
+        } else {
+            sample_coord(r, i - 1, tc);
+        }
         if (tex) {
             if (!tex3d_sample(r, tc, brick, &val)) continue;
         } else {
@@ -506,6 +514,286 @@ void orc_render_block_argb8(const orc_view* v, const float* brick, uint32_t dept
             argb_to_rgba(*px, ex);
             blend_above(ex, rgba);
             *px = rgba_to_argb(ex);
+        }
+    }
+}
+
+/* ======================================================================
+ * Plain per-block render in every field mode: renderKernel<mode>
+ * (DenseFieldRenderer_cu.cu:62-215) with renderIsosurface.hpp:34-66,
+ * renderIsosurfaces.hpp:34-106, renderMaxIntensityProjection.hpp:30-50,
+ * renderArgb.hpp:30-55, renderArgbLight.hpp:30-66, renderDomainVoxels.hpp:30-55,
+ * renderValueOnIsosurface.hpp:30-68, renderValueOnIsosurfaces.hpp, lighting
+ * cuda_lighting.hpp:26-95, findInterval cuda_findInterval.hpp:26-43.
+ * Sample positions entry + k*step (one fma), as the GPU kernel forms them;
+ * filtered values in float with single-rounding fmas as the kernel does.
+ * ====================================================================== */
+
+static float field_at(const orc_view* v, const float* brick, uint32_t n, const float tc[3])
+{
+    if (v->filter == 1) {
+        orc_ray rr;
+        float val;
+        rr.n = n;
+        if (!tex3d_sample(&rr, tc, brick, &val)) return NAN;
+        return val;
+    }
+    uint32_t i0[3], i1[3];
+    float f[3];
+    for (int d = 0; d < 3; ++d) filter_axis(tc[d], n, &i0[d], &i1[d], &f[d]);
+    float t[8];
+    for (int k = 0; k < 8; ++k) {
+        const uint64_t x = (k & 1) ? i1[0] : i0[0], y = (k & 2) ? i1[1] : i0[1], z = (k & 4) ? i1[2] : i0[2];
+        t[k] = brick[(z * n + y) * n + x];
+        if (isnan(t[k])) return NAN;
+    }
+    const float x00 = fmaf(f[0], t[1] - t[0], t[0]), x10 = fmaf(f[0], t[3] - t[2], t[2]);
+    const float x01 = fmaf(f[0], t[5] - t[4], t[4]), x11 = fmaf(f[0], t[7] - t[6], t[6]);
+    const float y0 = fmaf(f[1], x10 - x00, x00), y1 = fmaf(f[1], x11 - x01, x01);
+    return fmaf(f[2], y1 - y0, y0);
+}
+
+static void tf_rgba(const orc_view* v, const float* tf, float v01, float out[4])
+{
+    if (v->filter == 1) {
+        for (int ch = 0; ch < 4; ++ch) out[ch] = tex1d_tf(tf, v->tf_n, v01, ch);
+        return;
+    }
+    uint32_t i0, i1;
+    float f;
+    filter_axis(v01 * (float)v->tf_n, v->tf_n, &i0, &i1, &f);
+    for (int ch = 0; ch < 4; ++ch) out[ch] = fmaf(f, tf[4 * i1 + ch] - tf[4 * i0 + ch], tf[4 * i0 + ch]);
+}
+
+static float dot3(const float a[3], const float b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static void normalize3(float a[3])
+{
+    const float il = 1.f / sqrtf(dot3(a, a));
+    for (int d = 0; d < 3; ++d) a[d] *= il;
+}
+static float clamp01f(float x) { return fmaxf(0.f, fminf(1.f, x)); }
+
+static void frag_color(const orc_view* v, const orc_presentation* pr, const float* brick, uint32_t n,
+                       const float diffuse[4], const float surf[3], const float tc[3], float out[4])
+{
+    const float dl = 0.1f;
+    float a[3], b[3], N[3], V[3], c[3] = {0.f, 0.f, 0.f};
+    for (int d = 0; d < 3; ++d) {
+        float tm[3] = {tc[0], tc[1], tc[2]}, tp[3] = {tc[0], tc[1], tc[2]};
+        tm[d] = tc[d] - dl;
+        tp[d] = tc[d] + dl;
+        a[d] = field_at(v, brick, n, tm);
+        b[d] = field_at(v, brick, n, tp);
+    }
+    for (int d = 0; d < 3; ++d) N[d] = a[d] - b[d];
+    normalize3(N);
+    for (int d = 0; d < 3; ++d) V[d] = v->cam.eye[d] - surf[d];
+    normalize3(V);
+    for (uint32_t i = 0; i < pr->light_count; ++i) {
+        const orc_light* L0 = &pr->lights[i];
+        float L[3], H[3];
+        for (int d = 0; d < 3; ++d) L[d] = L0->pos[d] - surf[d];
+        normalize3(L);
+        if (dot3(L, N) < 0.f)
+            for (int d = 0; d < 3; ++d) N[d] = -N[d];
+        const float diff = (float)fmax((double)dot3(L, N), 0.0);
+        for (int d = 0; d < 3; ++d) H[d] = L[d] + V[d];
+        normalize3(H);
+        const float spec = diff > 0.f ? (float)pow(fmax((double)dot3(H, N), 0.0), 100.0) : 0.f;
+        for (int d = 0; d < 3; ++d)
+            c[d] += L0->ambient[d] + diffuse[d] * L0->diffuse[d] * diff + 0.5f * L0->specular[d] * spec;
+    }
+    for (int d = 0; d < 3; ++d) out[d] = clamp01f(c[d]);
+    out[3] = diffuse[3];
+}
+
+static int find_interval(float val, const float* levels, uint32_t count)
+{
+    if (val < levels[0]) return 0;
+    if (val >= levels[count - 1]) return (int)count;
+    int i1 = 0, i2 = (int)count;
+    while (i2 - i1 > 1) {
+        const int i = (i1 + i2) >> 1;
+        if (val < levels[i]) i2 = i;
+        else i1 = i;
+    }
+    return i2;
+}
+
+static void mode_pixel(const orc_view* v, const orc_presentation* pr, const orc_ray* r, const float* brick,
+                       const float* brick2, uint32_t depth, const float* tf, uint32_t* px)
+{
+    const uint32_t n = r->n;
+    const float span = v->field_max - v->field_min;
+    const uint32_t mode = pr->mode;
+    float pos[3], tc[3];
+    /* texture filter: positions accumulated step by step (increase(pos, step));
+       exact filter: entry + k * step (one fma) */
+    float seq[3] = {r->p0[0], r->p0[1], r->p0[2]};
+    int seq_k = 0;
+#define ORC_POS(k)                                                                                  \
+    do {                                                                                            \
+        if (v->filter == 1) {                                                                       \
+            for (; seq_k < (k); ++seq_k)                                                            \
+                for (int d_ = 0; d_ < 3; ++d_) seq[d_] += r->step[d_];                              \
+        }                                                                                           \
+        for (int d_ = 0; d_ < 3; ++d_) {                                                            \
+            pos[d_] = v->filter == 1 ? seq[d_] : fmaf(r->step[d_], (float)(k), r->p0[d_]);          \
+            tc[d_] = (pos[d_] - r->origin[d_]) * r->factor;                                         \
+        }                                                                                           \
+    } while (0)
+    if (mode == 2) { /* max intensity */
+        float maxv = v->field_min - span;
+        for (int i = 1; i < r->sample_count; ++i) {
+            ORC_POS(i - 1);
+            const float val = field_at(v, brick, n, tc);
+            if (val >= v->threshold && maxv < val) maxv = val;
+        }
+        if (maxv < v->field_min) return;
+        const float t = (maxv - v->field_min) / span;
+        float prev;
+        memcpy(&prev, px, 4);
+        if (!isnan(prev) && prev > t) return;
+        memcpy(px, &t, 4);
+        return;
+    }
+    float acc[4] = {0.f, 0.f, 0.f, 0.f}, ex[4];
+    if (mode == 3 || mode == 4 || mode == 5) {
+        const float of = opacity_factor(v), il = layer_exponent(v, depth);
+        float dom[4] = {0, 0, 0, 0};
+        if (mode == 5) {
+            tf_rgba(v, tf, 0.5f, dom);
+            dom[3] = 1.f - powf(1.f - dom[3] * of, il);
+        }
+        for (int i = 1; i < r->sample_count; ++i) {
+            ORC_POS(i - 1);
+            const float val = field_at(v, brick, n, tc);
+            if (isnan(val)) continue;
+            float col[4];
+            if (mode == 5) {
+                memcpy(col, dom, sizeof(col));
+            } else {
+                tf_rgba(v, tf, (val - v->field_min) / span, col);
+                col[3] = 1.f - powf(1.f - col[3] * of, il);
+                if (mode == 4) {
+                    if (!(col[3] >= 0.00001f)) continue;
+                    float lit[4];
+                    frag_color(v, pr, brick, n, col, pos, tc, lit);
+                    memcpy(col, lit, sizeof(col));
+                }
+            }
+            blend_behind(acc, col);
+            if (acc[3] > 0.996f) break;
+        }
+        argb_to_rgba(*px, ex);
+        blend_above(ex, acc);
+        *px = rgba_to_argb(ex);
+        return;
+    }
+    const int multi = mode == 1 || mode == 7, secondary = mode == 6 || mode == 7;
+    const uint32_t nl = pr->level_count;
+    if (multi && nl < 1) {
+        *px = 0u;
+        return;
+    }
+    ORC_POS(0);
+    float v1 = field_at(v, brick, n, tc);
+    int iint = multi ? (isnan(v1) ? -1 : find_interval(v1, pr->levels, nl)) : 0;
+    for (int i = 1; i < r->sample_count; ++i) {
+        ORC_POS(i);
+        const float v2 = field_at(v, brick, n, tc);
+        int nlev = 0, il = 0, dl = 0;
+        float levs[1] = {v->threshold};
+        if (!multi) {
+            if (!(!isnan(v1) && !isnan(v2) && (v1 - v->threshold) * (v2 - v->threshold) < 0.f)) {
+                v1 = v2;
+                continue;
+            }
+            nlev = 1;
+        } else {
+            if (isnan(v2)) {
+                iint = -1;
+                v1 = NAN;
+                continue;
+            }
+            if (isnan(v1)) {
+                v1 = v2;
+                iint = find_interval(v1, pr->levels, nl);
+                continue;
+            }
+            if (v2 < v1) {
+                if (iint == 0) {
+                    v1 = v2;
+                    continue;
+                }
+                il = iint - 1;
+                dl = -1;
+            } else {
+                if (iint == (int)nl) {
+                    v1 = v2;
+                    continue;
+                }
+                il = iint;
+                dl = 1;
+            }
+        }
+        for (;;) {
+            float level;
+            if (!multi) {
+                if (nlev-- <= 0) break;
+                level = levs[0];
+            } else {
+                if (!(il >= 0 && il < (int)nl)) break;
+                level = pr->levels[il];
+                if (!((v1 - level) * (v2 - level) < 0.f)) break;
+            }
+            const float t = (level - v1) / (v2 - v1);
+            float xpos[3], xtc[3], dif[4], col[4];
+            for (int d = 0; d < 3; ++d) {
+                xpos[d] = pos[d] + r->step[d] * t;
+                xtc[d] = (xpos[d] - r->origin[d]) * r->factor;
+            }
+            if (secondary) {
+                const float vs = field_at(v, brick2, n, xtc);
+                tf_rgba(v, tf, (vs - pr->secondary_min) / (pr->secondary_max - pr->secondary_min), dif);
+            } else {
+                tf_rgba(v, tf, (level - v->field_min) / span, dif);
+            }
+            dif[3] *= pr->isosurface_opacity;
+            frag_color(v, pr, brick, n, dif, xpos, xtc, col);
+            blend_behind(acc, col);
+            if (multi) {
+                iint += dl;
+                il += dl;
+            } else if (acc[3] > 0.996f) {
+                goto done;
+            }
+        }
+        if (multi && acc[3] > 0.996f) break;
+        v1 = v2;
+    }
+done:
+    argb_to_rgba(*px, ex);
+    blend_above(ex, acc);
+    *px = rgba_to_argb(ex);
+#undef ORC_POS
+}
+
+void orc_render_block_mode(const orc_view* v, const orc_presentation* pr, const float* brick, const float* brick2,
+                           uint32_t depth, const uint32_t idx[3], const int32_t rect[4], const float* tf,
+                           uint32_t* viewport)
+{
+    float c[3], h;
+    orc_block_cube(v->level, idx, c, &h);
+    for (int32_t yy = 0; yy < rect[3]; ++yy) {
+        for (int32_t xx = 0; xx < rect[2]; ++xx) {
+            uint32_t vx = (uint32_t)(rect[0] + xx), vy = (uint32_t)(rect[1] + yy);
+            if (vx >= v->W || vy >= v->H) continue;
+            float org[3], dir[3];
+            orc_ray r;
+            ray_for_pixel(v, vx, vy, org, dir);
+            if (!ray_block(v, org, dir, c, h, depth, &r)) continue;
+            mode_pixel(v, pr, &r, brick, brick2, depth, tf, &viewport[(size_t)(v->H - 1 - vy) * v->W + vx]);
         }
     }
 }

@@ -80,6 +80,26 @@ void orc_render_block_argb8(const orc_view* v, const float* brick, uint32_t dept
  * n^3 clamped texture, whether each texel is in the NaN footprint, and its linear index. */
 void orc_tex3d_weights(const float tc[3], uint32_t n, int32_t w[8], uint8_t footprint[8], uint32_t texel[8]);
 
+/* ---- plain per-block render in every field mode (s3vs::FieldMode) ----
+ * renderKernel<mode> with render*.hpp and cuda_lighting.hpp (see s3r_oracle.c);
+ * same conventions as orc_render_block_argb8, sampling per v->filter.  Modes are
+ * numbered as s3vs::FieldMode; MAX_INTENSITY (2) stores float bits. */
+typedef struct orc_light {
+    float pos[3], ambient[3], diffuse[3], specular[3];
+} orc_light;
+typedef struct orc_presentation {
+    uint32_t mode;
+    float isosurface_opacity;
+    uint32_t level_count;
+    float levels[50];
+    uint32_t light_count;
+    orc_light lights[10];
+    float secondary_min, secondary_max;
+} orc_presentation;
+void orc_render_block_mode(const orc_view* v, const orc_presentation* pr, const float* brick, const float* brick2,
+                           uint32_t depth, const uint32_t idx[3], const int32_t rect[4], const float* tf,
+                           uint32_t* viewport);
+
 /* ---- frame render in FP64, float RGBA out (batched-path semantics) ----
  * For each listed pixel: every block the ray enters, in ray order, is marched exactly as the
  * per-block kernel marches it (same float sample positions), with FP64 trilinear filtering,

@@ -22,7 +22,7 @@ MAX_DEPTH = 9
 
 BRICK_F32, BRICK_F16, BRICK_BF16 = 0, 1, 2
 FILTER_EXACT, FILTER_TEXTURE = 0, 1
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 u8p = C.POINTER(C.c_uint8)
 u16p = C.POINTER(C.c_uint16)
@@ -45,6 +45,22 @@ class View(C.Structure):
                 ("field_min", C.c_float), ("field_max", C.c_float), ("threshold", C.c_float),
                 ("quality", C.c_float), ("tf_n", C.c_uint32), ("alpha_stop", C.c_float),
                 ("filter", C.c_uint32), ("reserved", C.c_uint32 * 2)]
+
+
+MODE_ISOSURFACE, MODE_ISOSURFACES, MODE_MAX_INTENSITY, MODE_ARGB = 0, 1, 2, 3
+MODE_ARGB_LIGHT, MODE_DOMAIN_VOXELS, MODE_VALUE_ON_ISOSURFACE, MODE_VALUE_ON_ISOSURFACES = 4, 5, 6, 7
+MAX_LEVELS, MAX_LIGHTS = 50, 10
+
+
+class Light(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("ambient", C.c_float * 3), ("diffuse", C.c_float * 3),
+                ("specular", C.c_float * 3)]
+
+
+class Presentation(C.Structure):
+    _fields_ = [("mode", C.c_uint32), ("isosurface_opacity", C.c_float), ("level_count", C.c_uint32),
+                ("levels", C.c_float * MAX_LEVELS), ("light_count", C.c_uint32), ("lights", Light * MAX_LIGHTS),
+                ("secondary_min", C.c_float), ("secondary_max", C.c_float)]
 
 
 class FrameDesc(C.Structure):
@@ -78,6 +94,11 @@ _SIGS = {
     "s3r_block_view_rect": (C.c_int, [C.POINTER(View), u32p, i32p]),
     "s3r_clear_viewport": (C.c_int, [vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, vp]),
     "s3r_render_block_argb": (C.c_int, [vp, C.POINTER(View), vp, C.c_uint32, u32p, i32p, vp, vp, vp]),
+    "s3r_render_block": (C.c_int, [vp, C.POINTER(View), C.POINTER(Presentation), vp, vp, C.c_uint32, u32p, i32p, vp,
+                                   vp, vp]),
+    "s3r_default_light": (C.c_int, [C.POINTER(View), C.POINTER(Light)]),
+    "s3r_blend_image_part_mip_host": (C.c_int, [f32p, C.c_int32, C.c_int32, f32p, C.c_int32, C.c_int32, C.c_int32,
+                                                C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "s3r_b2f_order": (C.c_int, [u32p, u32p, f64p, f64p, f64p, u32p, C.c_uint32, u32p]),
     "s3r_index_box_world": (C.c_int, [C.c_uint32, u32p, u32p, f64p, f64p]),
     "s3r_bound_rect": (C.c_int, [vp, vp, C.c_uint32, C.c_uint32, i32p, vp]),

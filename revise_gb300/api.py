@@ -113,6 +113,14 @@ class Context:
         self._check(self.lib.s3r_render_block_argb(self.h, C.byref(view), ptr(brick), depth, i, r, ptr(tf_dev),
                                                    ptr(viewport), _stream(stream)))
 
+    def render_block(self, view: View, pres, brick, depth: int, idx, rect, tf_dev, viewport, brick2=None,
+                     stream=None):
+        """One block in any field mode (pres: revise_gb300.host.presentation)."""
+        i = (C.c_uint32 * 3)(*[int(x) for x in idx])
+        r = (C.c_int32 * 4)(*[int(x) for x in rect])
+        self._check(self.lib.s3r_render_block(self.h, C.byref(view), C.byref(pres), ptr(brick), ptr(brick2), depth,
+                                              i, r, ptr(tf_dev), ptr(viewport), _stream(stream)))
+
     def bound_rect(self, viewport, W: int, H: int, stream=None):
         r = (C.c_int32 * 4)()
         self._check(self.lib.s3r_bound_rect(self.h, ptr(viewport), W, H, r, _stream(stream)))

@@ -830,6 +830,73 @@ int s3r_crop(s3r_ctx* ctx, const uint32_t* image, uint32_t W, const int32_t rect
     return S3R_OK;
 }
 
+int s3r_default_light(const s3r_view* view, s3r_light* out)
+{
+    if (!view || !out) return fail(nullptr, S3R_ERR_INVALID, "null pointer");
+    const s3r_camera& c = view->cam;
+    for (int d = 0; d < 3; ++d) {
+        out->pos[d] = (c.eye[d] + c.n[d]) + c.e2[d] * c.h; // DenseFieldRenderer_cu.cu:442
+        out->ambient[d] = 0.f;
+        out->diffuse[d] = 1.f;
+        out->specular[d] = 0.1f;
+    }
+    return S3R_OK;
+}
+
+int s3r_render_block(s3r_ctx* ctx, const s3r_view* view, const s3r_presentation* pres, const float* brick,
+                     const float* brick2, uint32_t depth, const uint32_t idx[3], const int32_t rect[4],
+                     const float* tf, uint32_t* viewport, void* stream)
+{
+    if (!ctx) return fail(nullptr, S3R_ERR_INVALID, "ctx is null");
+    int rc = check_view(ctx, view);
+    if (rc) return rc;
+    if (!pres || !brick || !idx || !rect || !tf || !viewport) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (pres->mode > S3R_MODE_VALUE_ON_ISOSURFACES) return fail(ctx, S3R_ERR_INVALID, "unknown field mode");
+    if (pres->level_count > S3R_MAX_LEVELS) return fail(ctx, S3R_ERR_INVALID, "more than S3R_MAX_LEVELS levels");
+    if (pres->light_count > S3R_MAX_LIGHTS) return fail(ctx, S3R_ERR_INVALID, "more than S3R_MAX_LIGHTS lights");
+    for (uint32_t i = 1; i < pres->level_count; ++i)
+        if (!(pres->levels[i] > pres->levels[i - 1]))
+            return fail(ctx, S3R_ERR_INVALID, "levels must ascend strictly");
+    const bool secondary = pres->mode == S3R_MODE_VALUE_ON_ISOSURFACE || pres->mode == S3R_MODE_VALUE_ON_ISOSURFACES;
+    if (secondary && !brick2) return fail(ctx, S3R_ERR_INVALID, "this mode needs the secondary field's brick");
+    if (secondary && !(pres->secondary_max > pres->secondary_min))
+        return fail(ctx, S3R_ERR_INVALID, "secondary field range is empty");
+    if (depth > S3R_MAX_DEPTH) return fail(ctx, S3R_ERR_INVALID, "depth exceeds S3R_MAX_DEPTH");
+    const uint32_t m = 1u << view->level;
+    if (idx[0] >= m || idx[1] >= m || idx[2] >= m) return fail(ctx, S3R_ERR_INVALID, "block index outside level");
+    if (rect[2] < 0 || rect[3] < 0) return fail(ctx, S3R_ERR_INVALID, "negative view rectangle");
+    if ((rc = set_device(ctx))) return rc;
+    RenderBlock rb{};
+    block_sampling(view->level, idx, depth, rb);
+    for (int i = 0; i < 4; ++i) rb.rect[i] = rect[i];
+    S3R_CUDA(ctx, launch_render_block_mode(view, pres, brick, brick2, rb, tf, viewport, as_stream(stream)));
+    if (rect[2] > 0 && rect[3] > 0) ++ctx->launches;
+    return S3R_OK;
+}
+
+int s3r_blend_image_part_mip_host(float* dst, int32_t dw, int32_t dh, const float* src, int32_t sw, int32_t sh,
+                                  int32_t ox, int32_t oy, int32_t just_copy, int32_t offx, int32_t offy)
+{
+    if (!dst || (!src && sw * sh > 0)) return fail(nullptr, S3R_ERR_INVALID, "null pointer");
+    const int32_t dx = ox - offx, dy = oy - offy;
+    if (dx < 0 || dy < 0 || dx + sw > dw || dy + sh > dh)
+        return fail(nullptr, S3R_ERR_INVALID, "image part does not fit the destination");
+    for (int32_t y = 0; y < sh; ++y) {
+        const float* srow = src + (size_t)y * sw;
+        float* drow = dst + (size_t)dw * (dy + y) + dx;
+        if (just_copy) {
+            std::memcpy(drow, srow, sizeof(float) * sw);
+            continue;
+        }
+        for (int32_t i = 0; i < sw; ++i) {
+            const float sv = srow[i];
+            if (std::isnan(sv)) continue;
+            if (std::isnan(drow[i]) || drow[i] < sv) drow[i] = sv;
+        }
+    }
+    return S3R_OK;
+}
+
 int s3r_blend_image_part_host(uint32_t* dst, int32_t dw, int32_t dh, const uint32_t* src, int32_t sw, int32_t sh,
                               int32_t ox, int32_t oy, int32_t just_copy, int32_t offx, int32_t offy)
 {

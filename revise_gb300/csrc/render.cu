@@ -229,12 +229,13 @@ __device__ __forceinline__ float sample_tc(const BlockRay& r, int k, int d)
 template <int Fmt> struct Brick;
 
 template <int Fmt>
-__device__ __forceinline__ bool tex_trilinear(const void* brick, const BlockRay& r, int k, float& val)
+__device__ __forceinline__ bool tex_trilinear_at(const void* brick, uint32_t n, float tcx, float tcy, float tcz,
+                                                 float& val)
 {
-    const int hi = (int)r.n - 1;
-    const TexAxis x = tex_axis(sample_tc(r, k, 0), hi);
-    const TexAxis y = tex_axis(sample_tc(r, k, 1), hi);
-    const TexAxis z = tex_axis(sample_tc(r, k, 2), hi);
+    const int hi = (int)n - 1;
+    const TexAxis x = tex_axis(tcx, hi);
+    const TexAxis y = tex_axis(tcy, hi);
+    const TexAxis z = tex_axis(tcz, hi);
     int32_t w[8];
 #pragma unroll
     for (int hz = 0; hz < 2; ++hz) {
@@ -246,7 +247,7 @@ __device__ __forceinline__ bool tex_trilinear(const void* brick, const BlockRay&
         w[hz << 2] = yll;
         w[2 | (hz << 2)] = xl - yll;
     }
-    const uint64_t n64 = r.n;
+    const uint64_t n64 = n;
     float t[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -268,6 +269,12 @@ __device__ __forceinline__ bool tex_trilinear(const void* brick, const BlockRay&
     if (bad) return false;
     val = __fmul_rn(acc, 0.00390625f);
     return true;
+}
+
+template <int Fmt>
+__device__ __forceinline__ bool tex_trilinear(const void* brick, const BlockRay& r, int k, float& val)
+{
+    return tex_trilinear_at<Fmt>(brick, r.n, sample_tc(r, k, 0), sample_tc(r, k, 1), sample_tc(r, k, 2), val);
 }
 
 struct TfSample {
@@ -352,10 +359,16 @@ __global__ void render_block_argb_kernel(const s3r_view v, const float* __restri
     const float il = layer_exponent(depth, v.level, v.quality);
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     const bool tex = v.filter == S3R_FILTER_TEXTURE;
+    float tp[3] = {r.p0[0], r.p0[1], r.p0[2]}; // texture filter: accumulated position (increase(pos, step))
     for (int i = 1; i < r.samples; ++i) {
         float val;
         if (tex) {
-            if (!tex_trilinear<S3R_BRICK_F32>(brick, r, i - 1, val)) continue;
+            const float tcx = __fmul_rn(__fsub_rn(tp[0], r.origin[0]), r.factor);
+            const float tcy = __fmul_rn(__fsub_rn(tp[1], r.origin[1]), r.factor);
+            const float tcz = __fmul_rn(__fsub_rn(tp[2], r.origin[2]), r.factor);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) tp[d] = __fadd_rn(tp[d], r.step[d]);
+            if (!tex_trilinear_at<S3R_BRICK_F32>(brick, r.n, tcx, tcy, tcz, val)) continue;
         } else {
             Cell cell;
             sample_cell(r, i - 1, cell);
@@ -391,6 +404,318 @@ __global__ void render_block_argb_kernel(const s3r_view v, const float* __restri
     }
     ex.w = a;
     *px = rgba_to_argb(ex);
+}
+
+// ---------------------------------------------------------------- field modes (plain form)
+//
+// renderKernel<mode> with the reference's render functions (render*.hpp) and
+// lighting (cuda_lighting.hpp), on the plain form's ray set-up and sampling.
+
+// Field value at texel coordinate (x, y, z) -- the reference's fetch
+// coordinate -- filtered as kTex says; NaN where the filter gives NaN.
+template <bool kTex>
+__device__ __forceinline__ float field_at(const float* brick, uint32_t n, float x, float y, float z)
+{
+    float val;
+    if constexpr (kTex) {
+        if (!tex_trilinear_at<S3R_BRICK_F32>(brick, n, x, y, z, val)) return __int_as_float(0x7fc00000);
+        return val;
+    } else {
+        Cell c;
+        const int hi = (int)n - 1;
+        const float tc[3] = {x, y, z};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const float xb = __fsub_rn(tc[d], 0.5f);
+            const float fl = floorf(xb);
+            c.f[d] = __fsub_rn(xb, fl);
+            const int a = (int)fmaxf(fminf(fl, 1e9f), -1e9f), b = a + 1;
+            c.i0[d] = (uint32_t)min(max(a, 0), hi);
+            c.i1[d] = (uint32_t)min(max(b, 0), hi);
+        }
+        float t[8];
+        uint64_t off[8];
+        if (!trilinear<S3R_BRICK_F32>(brick, c, n, val, t, off)) return __int_as_float(0x7fc00000);
+        return val;
+    }
+}
+
+template <bool kTex> __device__ __forceinline__ float4 tf_rgba(const float4* tf, uint32_t tfn, float v01)
+{
+    if constexpr (kTex) return tex_tf_lookup(tf, tfn, v01);
+    else return tf_lookup(tf, tfn, v01).c;
+}
+
+struct F3 {
+    float x, y, z;
+};
+__device__ __forceinline__ F3 f3(const float* p) { return F3{p[0], p[1], p[2]}; }
+__device__ __forceinline__ F3 operator+(F3 a, F3 b) { return F3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ F3 operator-(F3 a, F3 b) { return F3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ F3 operator*(F3 a, float s) { return F3{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ F3 operator*(F3 a, F3 b) { return F3{a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ float dot3(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ F3 normalize3(F3 a) { return a * (1.f / sqrtf(dot3(a, a))); }
+__device__ __forceinline__ float clamp01(float x) { return fmaxf(0.f, fminf(1.f, x)); }
+
+// Blinn-Phong term of one light (cuda_lighting.hpp:26-50): material ambient 1,
+// diffuse = the transfer-function colour, specular 0.5, shininess 100; the
+// reference's max(., 0.0) and pow promote to double.
+__device__ __forceinline__ F3 blinn(F3 N, F3 V, F3 L, const s3r_light& light, F3 kd)
+{
+    const float diff = (float)fmax((double)dot3(L, N), 0.0);
+    const F3 H = normalize3(L + V);
+    const float spec = diff > 0.f ? (float)pow(fmax((double)dot3(H, N), 0.0), 100.0) : 0.f;
+    return f3(light.ambient) + kd * f3(light.diffuse) * diff + F3{0.5f, 0.5f, 0.5f} * f3(light.specular) * spec;
+}
+
+// computeFragColor (cuda_lighting.hpp:52-95): normal from central differences
+// of the field at +-0.1 texel, double-sided lighting, colour clamped to [0, 1].
+template <bool kTex>
+__device__ __forceinline__ float4 frag_color(const float* brick, uint32_t n, float4 diffuse, F3 eye, F3 surf, F3 tc,
+                                             const s3r_presentation& pr)
+{
+    constexpr float d = 0.1f;
+    const F3 a{field_at<kTex>(brick, n, tc.x - d, tc.y, tc.z), field_at<kTex>(brick, n, tc.x, tc.y - d, tc.z),
+               field_at<kTex>(brick, n, tc.x, tc.y, tc.z - d)};
+    const F3 b{field_at<kTex>(brick, n, tc.x + d, tc.y, tc.z), field_at<kTex>(brick, n, tc.x, tc.y + d, tc.z),
+               field_at<kTex>(brick, n, tc.x, tc.y, tc.z + d)};
+    F3 N = normalize3(a - b);
+    const F3 V = normalize3(eye - surf);
+    F3 c{0.f, 0.f, 0.f};
+    const F3 kd{diffuse.x, diffuse.y, diffuse.z};
+    for (uint32_t i = 0; i < pr.light_count; ++i) {
+        const F3 L = normalize3(f3(pr.lights[i].pos) - surf);
+        if (dot3(L, N) < 0.f) N = F3{-N.x, -N.y, -N.z};
+        c = c + blinn(N, V, L, pr.lights[i], kd);
+    }
+    return make_float4(clamp01(c.x), clamp01(c.y), clamp01(c.z), diffuse.w);
+}
+
+// blendBehind / blendAbove (cuda_blend.hpp:24-44), non-premultiplied
+__device__ __forceinline__ void blend_behind(float4& acc, float4 col)
+{
+    const float da = col.w * (1.f - acc.w);
+    const float a = acc.w + da;
+    if (a > 0.f) {
+        const float ka = acc.w / a, kd = da / a;
+        acc.x = acc.x * ka + col.x * kd;
+        acc.y = acc.y * ka + col.y * kd;
+        acc.z = acc.z * ka + col.z * kd;
+    }
+    acc.w = a;
+}
+
+__device__ __forceinline__ uint32_t blend_above_argb(uint32_t pix, float4 acc)
+{
+    float4 ex = argb_to_rgba(pix);
+    const float da = ex.w * (1.f - acc.w);
+    const float a = acc.w + da;
+    if (a > 0.f) {
+        const float kd = da / a, ki = acc.w / a;
+        ex.x = ex.x * kd + acc.x * ki;
+        ex.y = ex.y * kd + acc.y * ki;
+        ex.z = ex.z * kd + acc.z * ki;
+    }
+    ex.w = a;
+    return rgba_to_argb(ex);
+}
+
+// findInterval (cuda_findInterval.hpp:26-43): i with levels[i-1] <= v < levels[i]
+__device__ __forceinline__ int find_interval(float v, const float* levels, uint32_t count)
+{
+    if (v < levels[0]) return 0;
+    if (v >= levels[count - 1]) return (int)count;
+    int i1 = 0, i2 = (int)count;
+    while (i2 - i1 > 1) {
+        const int i = (i1 + i2) >> 1;
+        if (v < levels[i]) i2 = i;
+        else i1 = i;
+    }
+    return i2;
+}
+
+template <bool kTex>
+__global__ void render_block_mode_kernel(const s3r_view v, const s3r_presentation pr, const float* __restrict__ brick,
+                                         const float* __restrict__ brick2, const RenderBlock rb,
+                                         const float4* __restrict__ tf_g, uint32_t* __restrict__ viewport)
+{
+    extern __shared__ float4 tf[];
+    for (uint32_t i = threadIdx.y * blockDim.x + threadIdx.x; i < v.tf_n; i += blockDim.x * blockDim.y)
+        tf[i] = tf_g[i];
+    __syncthreads();
+    const int32_t xx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int32_t yy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (xx >= rb.rect[2] || yy >= rb.rect[3]) return;
+    const uint32_t vx = (uint32_t)(rb.rect[0] + xx), vy = (uint32_t)(rb.rect[1] + yy);
+    if (vx >= v.W || vy >= v.H) return;
+    float org[3], dir[3];
+    pixel_ray(v, vx, vy, org, dir);
+    BlockRay r;
+    if (!block_ray(v, org, dir, rb, r)) return;
+    uint32_t* px = &viewport[(size_t)(v.H - 1 - vy) * v.W + vx];
+    const uint32_t n = r.n;
+    const float span = v.field_max - v.field_min;
+    const F3 eye = f3(v.cam.eye);
+    const F3 step{r.step[0], r.step[1], r.step[2]};
+    // sample k's position: with the texture filter accumulated step by step from
+    // the entry point as the reference does (increase(pos, step)), because the
+    // texture unit's 8-bit fractions make it sensitive to the last ulp of the
+    // position; with the exact filter entry + k * step (one fma), as the oracle
+    // and the batched path form it.  k only grows within a march.
+    F3 seq{r.p0[0], r.p0[1], r.p0[2]};
+    int seq_k = 0;
+    auto pos_of = [&](int k) {
+        if constexpr (kTex) {
+            for (; seq_k < k; ++seq_k)
+                seq = F3{__fadd_rn(seq.x, r.step[0]), __fadd_rn(seq.y, r.step[1]), __fadd_rn(seq.z, r.step[2])};
+            return seq;
+        } else {
+            return F3{__fmaf_rn(r.step[0], (float)k, r.p0[0]), __fmaf_rn(r.step[1], (float)k, r.p0[1]),
+                      __fmaf_rn(r.step[2], (float)k, r.p0[2])};
+        }
+    };
+    auto tc_of = [&](F3 p) {
+        return F3{__fmul_rn(__fsub_rn(p.x, r.origin[0]), r.factor), __fmul_rn(__fsub_rn(p.y, r.origin[1]), r.factor),
+                  __fmul_rn(__fsub_rn(p.z, r.origin[2]), r.factor)};
+    };
+    auto value = [&](const float* b, F3 p) {
+        const F3 tc = tc_of(p);
+        return field_at<kTex>(b, n, tc.x, tc.y, tc.z);
+    };
+    constexpr float kMax = 0.996f; // AlphaThreshold / AlphaMaxThreshold
+    const uint32_t mode = pr.mode;
+    if (mode == S3R_MODE_MAX_INTENSITY) {
+        // renderMaxIntensityProjection.hpp:30-50; the pixel holds float bits
+        float maxv = v.field_min - span;
+        for (int i = 1; i < r.samples; ++i) {
+            const float val = value(brick, pos_of(i - 1));
+            if (val >= v.threshold && maxv < val) maxv = val;
+        }
+        if (maxv < v.field_min) return;
+        const float t = (maxv - v.field_min) / span;
+        const float prev = __uint_as_float(*px);
+        if (!isnan(prev) && prev > t) return;
+        *px = __float_as_uint(t);
+        return;
+    }
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (mode == S3R_MODE_ARGB || mode == S3R_MODE_ARGB_LIGHT || mode == S3R_MODE_DOMAIN_VOXELS) {
+        const float of = (v.threshold - v.field_min) / span;
+        const float il = layer_exponent(rb.depth, v.level, v.quality);
+        float4 dom = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (mode == S3R_MODE_DOMAIN_VOXELS) {
+            // renderDomainVoxels.hpp:41-42: one colour, the table's middle
+            dom = tf_rgba<kTex>(tf, v.tf_n, 0.5f);
+            dom.w = 1.f - powf(1.f - dom.w * of, il);
+        }
+        for (int i = 1; i < r.samples; ++i) {
+            const F3 p = pos_of(i - 1);
+            const float val = value(brick, p);
+            if (isnan(val)) continue;
+            float4 col;
+            if (mode == S3R_MODE_DOMAIN_VOXELS) {
+                col = dom;
+            } else {
+                col = tf_rgba<kTex>(tf, v.tf_n, (val - v.field_min) / span);
+                col.w = 1.f - powf(1.f - col.w * of, il);
+                if (mode == S3R_MODE_ARGB_LIGHT) {
+                    // renderArgbLight.hpp:44-56: only visible enough samples are lit
+                    if (!(col.w >= 0.00001f)) continue;
+                    col = frag_color<kTex>(brick, n, col, eye, p, tc_of(p), pr);
+                }
+            }
+            blend_behind(acc, col);
+            if (acc.w > kMax) break;
+        }
+        *px = blend_above_argb(*px, acc);
+        return;
+    }
+    // isosurface modes: v1 at the entry point, v2 at samples 1 .. sampleCount-1; the
+    // crossing is placed at pos + step * t from the later sample, as the reference does
+    const bool multi = mode == S3R_MODE_ISOSURFACES || mode == S3R_MODE_VALUE_ON_ISOSURFACES;
+    const bool secondary = mode == S3R_MODE_VALUE_ON_ISOSURFACE || mode == S3R_MODE_VALUE_ON_ISOSURFACES;
+    const uint32_t nl = pr.level_count;
+    if (multi && nl < 1) {
+        *px = 0u; // renderIsosurfaces.hpp:36-38
+        return;
+    }
+    auto surface_colour = [&](float level, F3 xpos) {
+        float4 dif;
+        if (secondary) {
+            const float vs = value(brick2, xpos);
+            dif = tf_rgba<kTex>(tf, v.tf_n, (vs - pr.secondary_min) / (pr.secondary_max - pr.secondary_min));
+        } else {
+            dif = tf_rgba<kTex>(tf, v.tf_n, (level - v.field_min) / span);
+        }
+        dif.w *= pr.isosurface_opacity;
+        return frag_color<kTex>(brick, n, dif, eye, xpos, tc_of(xpos), pr);
+    };
+    auto xpos_of = [&](F3 p, float t) {
+        return F3{__fadd_rn(p.x, __fmul_rn(step.x, t)), __fadd_rn(p.y, __fmul_rn(step.y, t)),
+                  __fadd_rn(p.z, __fmul_rn(step.z, t))};
+    };
+    float v1 = value(brick, pos_of(0));
+    if (!multi) {
+        const float thr = v.threshold;
+        for (int i = 1; i < r.samples; ++i) {
+            const F3 p = pos_of(i);
+            const float v2 = value(brick, p);
+            if (!isnan(v1) && !isnan(v2) && (v1 - thr) * (v2 - thr) < 0.f) {
+                const float t = (thr - v1) / (v2 - v1);
+                blend_behind(acc, surface_colour(thr, xpos_of(p, t)));
+                if (acc.w > kMax) break;
+            }
+            v1 = v2;
+        }
+    } else {
+        // renderIsosurfaces.hpp:34-106 / renderValueOnIsosurfaces.hpp
+        int iint = isnan(v1) ? -1 : find_interval(v1, pr.levels, nl);
+        for (int i = 1; i < r.samples; ++i) {
+            const F3 p = pos_of(i);
+            const float v2 = value(brick, p);
+            if (isnan(v2)) {
+                iint = -1;
+                v1 = __int_as_float(0x7fc00000);
+                continue;
+            }
+            if (isnan(v1)) {
+                v1 = v2;
+                iint = find_interval(v1, pr.levels, nl);
+                continue;
+            }
+            int il, dl;
+            if (v2 < v1) {
+                if (iint == 0) {
+                    v1 = v2;
+                    continue;
+                }
+                il = iint - 1;
+                dl = -1;
+            } else {
+                if (iint == (int)nl) {
+                    v1 = v2;
+                    continue;
+                }
+                il = iint;
+                dl = 1;
+            }
+            while (il >= 0 && il < (int)nl) {
+                const float level = pr.levels[il];
+                if ((v1 - level) * (v2 - level) < 0.f) {
+                    const float t = (level - v1) / (v2 - v1);
+                    blend_behind(acc, surface_colour(level, xpos_of(p, t)));
+                    iint += dl;
+                    il += dl;
+                } else {
+                    break;
+                }
+            }
+            if (acc.w > kMax) break;
+            v1 = v2;
+        }
+    }
+    *px = blend_above_argb(*px, acc);
 }
 
 // ---------------------------------------------------------------- batched form
@@ -679,7 +1004,6 @@ __global__ void __launch_bounds__(128, 5) frame_backward_kernel(FrameArgs fa)
             float tf_a[4] = {0.f, 0.f, 0.f, 0.f}, tf_b[4] = {0.f, 0.f, 0.f, 0.f};
             auto flush_tf = [&]() {
                 if (tf_i0 == 0xffffffffu) return;
-#pragma unroll
                 atomicAdd(&dtf4[tf_i0], make_float4(tf_a[0], tf_a[1], tf_a[2], tf_a[3]));
                 atomicAdd(&dtf4[tf_i1], make_float4(tf_b[0], tf_b[1], tf_b[2], tf_b[3]));
 #pragma unroll
@@ -736,7 +1060,6 @@ __global__ void __launch_bounds__(128, 5) frame_backward_kernel(FrameArgs fa)
                     if (ts.i0 != tf_i0 || ts.i1 != tf_i1) {
                         if (tf_i0 != 0xffffffffu && ts.i0 == tf_i1 && ts.i0 != ts.i1) {
                             // moving up: old i1 becomes new i0
-#pragma unroll
                             atomicAdd(&dtf4[tf_i0], make_float4(tf_a[0], tf_a[1], tf_a[2], tf_a[3]));
 #pragma unroll
                             for (int ch = 0; ch < 4; ++ch) {
@@ -745,7 +1068,6 @@ __global__ void __launch_bounds__(128, 5) frame_backward_kernel(FrameArgs fa)
                             }
                         } else if (tf_i0 != 0xffffffffu && ts.i1 == tf_i0 && ts.i0 != ts.i1) {
                             // moving down: old i0 becomes new i1
-#pragma unroll
                             atomicAdd(&dtf4[tf_i1], make_float4(tf_b[0], tf_b[1], tf_b[2], tf_b[3]));
 #pragma unroll
                             for (int ch = 0; ch < 4; ++ch) {
@@ -803,6 +1125,23 @@ __global__ void dtf_reduce_kernel(const float* __restrict__ part, float* __restr
 }
 
 } // namespace
+
+cudaError_t launch_render_block_mode(const s3r_view* view_host, const s3r_presentation* pres, const float* brick,
+                                     const float* brick2, const RenderBlock& rb, const float* tf, uint32_t* viewport,
+                                     cudaStream_t s)
+{
+    if (rb.rect[2] <= 0 || rb.rect[3] <= 0) return cudaSuccess;
+    dim3 block(16, 8);
+    dim3 grid((rb.rect[2] + 15) / 16, (rb.rect[3] + 7) / 8);
+    const size_t smem = view_host->tf_n * sizeof(float4);
+    if (view_host->filter == S3R_FILTER_TEXTURE)
+        render_block_mode_kernel<true><<<grid, block, smem, s>>>(*view_host, *pres, brick, brick2, rb,
+                                                                 reinterpret_cast<const float4*>(tf), viewport);
+    else
+        render_block_mode_kernel<false><<<grid, block, smem, s>>>(*view_host, *pres, brick, brick2, rb,
+                                                                  reinterpret_cast<const float4*>(tf), viewport);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_render_block_argb(const s3r_view* view_host, const float* brick, const RenderBlock& rb,
                                      const float* tf, uint32_t* viewport, cudaStream_t s)

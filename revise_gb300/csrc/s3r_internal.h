@@ -117,6 +117,9 @@ uint32_t interp_plan_ctas_per_sm(uint32_t fmt, uint32_t tile_log2);
 cudaError_t launch_block_ranges(const PlanBlock* blocks, uint32_t nblocks, const float* sparse,
                                 const uint64_t* node_off_dev, float2* scale_offset, cudaStream_t s);
 
+cudaError_t launch_render_block_mode(const s3r_view* view_host, const s3r_presentation* pres, const float* brick,
+                                     const float* brick2, const RenderBlock& rb, const float* tf, uint32_t* viewport,
+                                     cudaStream_t s);
 cudaError_t launch_render_block_argb(const s3r_view* view_host, const float* brick, const RenderBlock& rb,
                                      const float* tf, uint32_t* viewport, cudaStream_t s);
 cudaError_t launch_frame_render(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, uint32_t fmt,

@@ -8,7 +8,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import Camera, View, arr, check
+from ._lib import Camera, Light, Presentation, View, arr, check
 
 
 def camera_look_at(eye, center, up, fovy_deg: float, W: int, H: int, ortho: bool = False,
@@ -104,3 +104,41 @@ def blend_image_part(dst: np.ndarray, src: np.ndarray, origin, just_copy: bool =
     check(lib.s3r_blend_image_part_host(arr(dst, C.c_uint32), dst.shape[1], dst.shape[0], arr(src, C.c_uint32),
                                         src.shape[1], src.shape[0], int(origin[0]), int(origin[1]),
                                         1 if just_copy else 0, int(offset[0]), int(offset[1])))
+
+
+def default_light(view: View) -> Light:
+    """The reference renderer's single light source for this view."""
+    lib = _lib.load()
+    out = Light()
+    check(lib.s3r_default_light(C.byref(view), C.byref(out)))
+    return out
+
+
+def presentation(mode: int, view: View = None, isosurface_opacity: float = 1.0, levels=(), lights=None,
+                 secondary_range=(0.0, 1.0)) -> Presentation:
+    """s3r_presentation for a field mode.  levels: absolute isosurface values (sorted and
+    de-duplicated here, as the reference's makeLevels does); lights default to the
+    renderer's single light for view."""
+    p = Presentation()
+    p.mode = mode
+    p.isosurface_opacity = isosurface_opacity
+    lv = sorted(set(float(np.float32(x)) for x in levels))[:_lib.MAX_LEVELS]
+    p.level_count = len(lv)
+    for i, x in enumerate(lv):
+        p.levels[i] = x
+    if lights is None:
+        lights = [default_light(view)] if view is not None else []
+    p.light_count = len(lights)
+    for i, L in enumerate(lights):
+        p.lights[i] = L
+    p.secondary_min, p.secondary_max = secondary_range
+    return p
+
+
+def blend_image_part_mip(dst: np.ndarray, src: np.ndarray, origin, just_copy: bool = False, offset=(0, 0)) -> None:
+    """blendImagePartMaxIntensity on host float images (float32 arrays of shape (h, w)), in place on dst."""
+    lib = _lib.load()
+    assert dst.dtype == np.float32 and src.dtype == np.float32 and dst.flags.c_contiguous and src.flags.c_contiguous
+    check(lib.s3r_blend_image_part_mip_host(arr(dst, C.c_float), dst.shape[1], dst.shape[0], arr(src, C.c_float),
+                                            src.shape[1], src.shape[0], int(origin[0]), int(origin[1]),
+                                            1 if just_copy else 0, int(offset[0]), int(offset[1])))

@@ -9,8 +9,14 @@
 // coordinates (the fraction quantization), then the NaN footprint: texel 0 set
 // to NaN, the rest 1, over the same lattice.
 //
+// Then the ramp again at off-lattice coordinates: 65536 pseudo-random x in
+// [0.5, 1.5) with full mantissas, and x just either side of every rounding
+// boundary 0.5 + (j + 1/2)/256 at offsets of +-2^-e (e = 12 .. 23): how the unit
+// forms the 8-bit fraction from a float coordinate.
+//
 // Output (binary, little endian): int32 na, int32 A[na], float W[8][na^3]
-// (k slowest, i fastest), float ramp[4096], float nan_case[na^3].
+// (k slowest, i fastest), float ramp[4096], float nan_case[na^3],
+// int32 m, float xs[m], float ramp_off[m].
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -105,6 +111,27 @@ int main(int argc, char** argv)
     {
         const float v[8] = {NAN, 1, 1, 1, 1, 1, 1, 1};
         if (sample(v, lattice, out)) return 1;
+        std::fwrite(out.data(), sizeof(float), out.size(), f);
+    }
+    {
+        std::vector<float3> xs;
+        unsigned long long st = 0x9E3779B97F4A7C15ull;
+        for (int i = 0; i < 65536; ++i) {
+            st = st * 6364136223846793005ull + 1442695040888963407ull;
+            const float u = (float)((st >> 40) & 0xffffffull) / 16777216.f; // 24 random bits in [0, 1)
+            xs.push_back(make_float3(0.5f + u, 0.5f, 0.5f));
+        }
+        for (int j = 0; j < 256; ++j)
+            for (int e = 12; e <= 23; ++e)
+                for (int sgn = -1; sgn <= 1; sgn += 2) {
+                    const float x = 0.5f + (j + 0.5f) / 256.f + (float)sgn * std::ldexp(1.f, -e);
+                    xs.push_back(make_float3(x, 0.5f, 0.5f));
+                }
+        const float v[8] = {0, 1, 0, 1, 0, 1, 0, 1};
+        if (sample(v, xs, out)) return 1;
+        const int m = (int)xs.size();
+        std::fwrite(&m, sizeof(int), 1, f);
+        for (const float3& p : xs) std::fwrite(&p.x, sizeof(float), 1, f);
         std::fwrite(out.data(), sizeof(float), out.size(), f);
     }
     std::fclose(f);

@@ -55,6 +55,19 @@ def test_texture_nan_footprint_and_fraction_rounding_match_measured():
         assert ramp[q] == np.float32(w[(texel & 1) == 1].sum() / 256.0), q
 
 
+def test_texture_fraction_rule_at_off_lattice_coordinates():
+    """65,536 random float coordinates and coordinates 2^-12 .. 2^-23 either side of
+    every rounding boundary: the 8-bit fraction is floor((x - 0.5) * 256 + 1/2)
+    of the float coordinate, exactly."""
+    z = _load("texture_weights.npz")
+    if "xs" not in z:
+        pytest.skip("fixture predates the off-lattice probe")
+    xs, got = z["xs"], z["ramp_off"]
+    for x, g in zip(xs, got):
+        w, _, texel = oracle.tex3d_weights((float(x), 0.5, 0.5), 2)
+        assert g == np.float32(w[(texel & 1) == 1].sum() / 256.0), (x, g)
+
+
 @pytest.mark.parametrize("variant", tv.VARIANTS)
 def test_texture_mode_oracle_reproduces_reference_cuda_images(variant):
     """Per-block ARGB8 render in the oracle with texture-unit filtering against the
@@ -94,3 +107,38 @@ def test_exact_mode_differs_from_reference_where_masking_meets_texture_rounding(
     a_ref = (ref >> 24).astype(int)
     assert (a_ref - a_exact).min() >= -1
     assert (a_ref - a_exact).max() > 20
+
+
+@pytest.mark.parametrize("name", ["isosurface", "isosurfaces", "max_intensity", "argb_light", "domain_voxels",
+                                  "value_on_isosurface", "value_on_isosurfaces"])
+def test_oracle_field_modes_reproduce_reference_cuda_images(name):
+    """The oracle's restatement of every other field mode (texture filter) against
+    images of the reference's own renderKernel<mode>, with the tolerances the GPU
+    kernels meet (tests/test_gpu_modes.py)."""
+    import mode_scenes as ms
+    ref = _load("refcu_modes.npz")[name]
+    w, view, pres, sparse2 = ms.scene(name)
+    ov = oracle.view_from(view)
+    op = oracle.presentation_from(pres)
+    dense = oracle.interp_workload(w)
+    dense2 = None
+    if sparse2 is not None:
+        dense2 = np.concatenate([oracle.interp_f32(w.block_nodes(b)[0], sparse2[int(w.node_off[b]):int(w.node_off[b + 1])],
+                                                   int(w.blocks[b, 3])) for b in range(w.nblocks)])
+    img = np.full(w.W * w.H, ms.clear_value(pres), np.uint32)
+    for b in tv.b2f_blocks(w):
+        blk = [int(x) for x in w.blocks[b, :3]]
+        sl = slice(int(w.vertex_off[b]), int(w.vertex_off[b + 1]))
+        oracle.render_block_mode(ov, op, dense[sl], int(w.blocks[b, 3]), blk, host.block_view_rect(view, blk), w.tf,
+                                 img, None if dense2 is None else dense2[sl])
+    if name == "max_intensity":
+        a, b = img.view(np.float32), ref.view(np.float32)
+        assert np.array_equal(np.isnan(a), np.isnan(b))
+        m = ~np.isnan(a)
+        diff = np.abs(a[m] - b[m])
+        assert diff.max() <= 2e-4 and (diff > 1e-6).mean() < 0.02
+        return
+    lsb, frac = {"argb_light": (8, 0.10), "domain_voxels": (2, 0.01)}.get(name, (4, 0.01))
+    d = np.abs(img.view(np.uint8).reshape(-1, 4).astype(int) - ref.view(np.uint8).reshape(-1, 4).astype(int)).max(1)
+    assert (ref >> 24).astype(bool).mean() > 0.03
+    assert d.max() <= lsb and (d > 0).mean() <= frac, (d.max(), (d > 0).mean())
