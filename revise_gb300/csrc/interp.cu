@@ -106,51 +106,74 @@ __device__ __forceinline__ float to_internal(float v) { return v == kNoField ? _
 // Descent slots: 27 points (3x3x3, x fastest) per coarse level.
 constexpr int kMaxDescentLevels = S3R_MAX_DEPTH;
 
-// Warp 0: walk from the block's root corners down L levels, using the sparse
-// values already placed in desc[27*l + p] (NaN where no node); lanes 0-7 return
-// the tile's 8 corners.
-__device__ float descend(float* desc, uint32_t d, uint32_t k, uint32_t L, uint32_t ox, uint32_t oy, uint32_t oz)
+// One 27-point level held in registers: lane p < 27 holds point p (x fastest)
+// of a cube -- the 8 corners known, each midpoint its sparse value or NaN --
+// and gets it filled: edges from their two ends, faces from their four edges,
+// the centre from its six faces, the stencil sums in the reference's order.
+// Neighbours come by shuffle, so no shared memory and no __syncwarp.
+__device__ __forceinline__ float level27(float v, uint32_t lane)
 {
-    (void)k;
-    const uint32_t lane = threadIdx.x;
     const uint32_t px = lane % 3, py = (lane / 3) % 3, pz = lane / 9;
-    const uint32_t nodd = (px & 1) + (py & 1) + (pz & 1);
+    const uint32_t nodd = lane < 27 ? (px & 1) + (py & 1) + (pz & 1) : 3u;
+    {
+        const bool mine = nodd == 1;
+        const uint32_t st = (px & 1) ? 1 : ((py & 1) ? 3 : 9);
+        const float lo = __shfl_sync(0xffffffffu, v, mine ? lane - st : lane);
+        const float hi = __shfl_sync(0xffffffffu, v, mine ? lane + st : lane);
+        if (mine && isnan(v)) v = kHalf * (lo + hi);
+    }
+    {
+        const bool mine = nodd == 2;
+        const uint32_t s1 = (px & 1) ? 1 : 3; // the two odd axes, ascending
+        const uint32_t s2 = (pz & 1) ? 9 : 3;
+        const float a = __shfl_sync(0xffffffffu, v, mine ? lane - s1 : lane);
+        const float b = __shfl_sync(0xffffffffu, v, mine ? lane + s1 : lane);
+        const float c = __shfl_sync(0xffffffffu, v, mine ? lane - s2 : lane);
+        const float d = __shfl_sync(0xffffffffu, v, mine ? lane + s2 : lane);
+        if (mine && isnan(v)) v = kQuarter * (a + b + c + d);
+    }
+    {
+        const float f12 = __shfl_sync(0xffffffffu, v, 12), f14 = __shfl_sync(0xffffffffu, v, 14);
+        const float f10 = __shfl_sync(0xffffffffu, v, 10), f16 = __shfl_sync(0xffffffffu, v, 16);
+        const float f4 = __shfl_sync(0xffffffffu, v, 4), f22 = __shfl_sync(0xffffffffu, v, 22);
+        if (lane == 13 && isnan(v)) v = kSixth * (f12 + f14 + f10 + f16 + f4 + f22);
+    }
+    return v;
+}
+
+// One warp, all lanes: walk from the block's root corners down L levels to the
+// tile's cube, each level's 27 points in registers (level27) with the sparse
+// values found in desc[27*l + p] (NaN where no node; at levels below the root
+// the corner points come from the level above).  Lanes 0-7 return the tile's 8
+// corners (lane & 1, lane >> 1 & 1, lane >> 2).
+__device__ __forceinline__ float descend_regs(const float* desc, uint32_t d, uint32_t L, uint32_t ox, uint32_t oy,
+                                              uint32_t oz, uint32_t lane)
+{
+    const uint32_t px = lane % 3, py = (lane / 3) % 3, pz = lane / 9;
+    const bool is_corner = lane < 27 && !((px | py | pz) & 1);
+    const uint32_t from = is_corner ? (px >> 1) + 2 * (py >> 1) + 4 * (pz >> 1) : lane;
     uint32_t size = 1u << d, gx0 = 0, gy0 = 0, gz0 = 0;
     float corner = 0.f;
     for (uint32_t l = 0; l < L; ++l) {
-        float* c27 = desc + 27 * l;
-        const uint32_t hs = size >> 1;
+        float v = lane < 27 ? desc[27 * l + lane] : 0.f;
         if (l > 0) {
-            const uint32_t src = lane < 27 ? (px >> 1) + 2 * (py >> 1) + 4 * (pz >> 1) : 0;
-            const float cv = __shfl_sync(0xffffffffu, corner, (int)src);
-            if (lane < 27 && nodd == 0) c27[lane] = cv;
+            const float cv = __shfl_sync(0xffffffffu, corner, from);
+            if (is_corner) v = cv;
         }
-        __syncwarp();
-        if (lane < 27 && nodd == 1 && isnan(c27[lane])) {
-            const uint32_t st = (px & 1) ? 1 : ((py & 1) ? 3 : 9);
-            c27[lane] = kHalf * (c27[lane - st] + c27[lane + st]);
-        }
-        __syncwarp();
-        if (lane < 27 && nodd == 2 && isnan(c27[lane])) {
-            const uint32_t s1 = (px & 1) ? 1 : 3; // the two odd axes, ascending
-            const uint32_t s2 = (pz & 1) ? 9 : 3;
-            c27[lane] = kQuarter * (c27[lane - s1] + c27[lane + s1] + c27[lane - s2] + c27[lane + s2]);
-        }
-        __syncwarp();
-        if (lane == 13 && isnan(c27[13]))
-            c27[13] = kSixth * (c27[12] + c27[14] + c27[10] + c27[16] + c27[4] + c27[22]);
-        __syncwarp();
+        v = level27(v, lane);
+        const uint32_t hs = size >> 1;
         const uint32_t qx = (ox - gx0) >= hs ? 1u : 0u;
         const uint32_t qy = (oy - gy0) >= hs ? 1u : 0u;
         const uint32_t qz = (oz - gz0) >= hs ? 1u : 0u;
-        if (lane < 8) corner = c27[(qx + (lane & 1)) + 3 * (qy + ((lane >> 1) & 1)) + 9 * (qz + (lane >> 2))];
+        const uint32_t pick =
+            lane < 8 ? (qx + (lane & 1)) + 3 * (qy + ((lane >> 1) & 1)) + 9 * (qz + (lane >> 2)) : lane;
+        corner = __shfl_sync(0xffffffffu, v, pick);
         gx0 += qx * hs;
         gy0 += qy * hs;
         gz0 += qz * hs;
         size = hs;
-        __syncwarp();
     }
-    return corner; // lanes 0-7: corner (lane&1, lane>>1&1, lane>>2) of the tile
+    return corner;
 }
 
 // One level of one tile: every cube of the level (2^j per axis) is handled by
@@ -236,6 +259,20 @@ template <uint32_t T> struct SplitTile {
         return idx((x & 1) | ((y & 1) << 1) | ((z & 1) << 2), x >> 1, y >> 1, z >> 1);
     }
 };
+
+// Warp 0, T >= 4: the tile cube's 27 points (corners at 0 and T, midpoints at
+// T/2) from its corners and the sparse values already in the tile -- the
+// tile's first level, cube_level on its single cube, in registers.
+template <uint32_t T> __device__ __forceinline__ void tile_top(float* s, uint32_t lane)
+{
+    using S = SplitTile<T>;
+    const uint32_t px = lane % 3, py = (lane / 3) % 3, pz = lane / 9;
+    constexpr uint32_t h = T / 2;
+    const uint32_t off = lane < 27 ? S::at(px * h, py * h, pz * h) : 0;
+    float v = lane < 27 ? s[off] : 0.f;
+    v = level27(v, lane);
+    if (lane < 27 && ((px | py | pz) & 1)) s[off] = v;
+}
 
 // Marks the finest-level cubes holding a sparse value at one of their
 // midpoints (tile position (x, y, z), at least one coordinate odd): the cube
@@ -449,21 +486,24 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
             place(a.entry_local[i], to_internal(a.sparse[t.node_base + a.entry_node[i]]));
     }
     __syncthreads();
-    // 2. tile corners from the coarse levels
-    if (L > 0) {
+    // 2. tile corners from the coarse levels, then the tile cube's own midpoints
+    //    (its first level): warp 0, each level's 27 points in registers
+    if (L > 0 || T >= 4) {
         if (threadIdx.x < 32) {
-            float corner = descend(desc, d, t.k, L, ox, oy, oz);
-            if (threadIdx.x < 8) {
-                const uint32_t c = threadIdx.x;
-                s[at((c & 1) * T, ((c >> 1) & 1) * T, (c >> 2) * T)] = corner;
+            const uint32_t lane = threadIdx.x;
+            if (L > 0) {
+                const float corner = descend_regs(desc, d, L, ox, oy, oz, lane);
+                if (lane < 8) s[at((lane & 1) * T, ((lane >> 1) & 1) * T, (lane >> 2) * T)] = corner;
+                __syncwarp();
             }
+            if constexpr (T >= 4) tile_top<T>(s, lane);
         }
         __syncthreads();
     }
-    // 3. the coarser levels on the even sub-array (a tile of T/2 cells)
-    if constexpr (T >= 2) {
-        constexpr uint32_t kk = (T >= 2) ? (31 - __builtin_clz(T)) : 0;
-        for (uint32_t j = 0; j + 1 < kk; ++j) {
+    // 3. the remaining coarser levels on the even sub-array (a tile of T/2 cells)
+    if constexpr (T >= 8) {
+        constexpr uint32_t kk = 31 - __builtin_clz(T);
+        for (uint32_t j = 1; j + 1 < kk; ++j) {
             cube_level(s, S::G, S::H, j);
             __syncthreads();
         }
