@@ -36,6 +36,10 @@
  *   s3r_frame_*                no single counterpart: the batched form of VsWorker_cu::renderScenePart
  *                              (src/s3vs_worker/cuda/VsWorker_cu.cpp:225-313) over a whole block cube
  *   s3r_render_argb_backward   none (the reference has no adjoint)
+ *   s3r_dataset_*              BlockTreeFieldService<3> (include/s3dmm/BlockTreeFieldService.hpp:31-262),
+ *                              Metadata<3> (include/s3dmm/Metadata.hpp:119-499),
+ *                              BlockTreeFieldProvider<3>::fieldValues (include/s3dmm/BlockTreeFieldProvider.hpp:111-168),
+ *                              BlockTreeNodes<3> (include/s3dmm/BlockTreeNodes.hpp:51-183)
  */
 #ifndef S3R_H
 #define S3R_H
@@ -47,7 +51,7 @@
 extern "C" {
 #endif
 
-#define S3R_ABI_VERSION 3
+#define S3R_ABI_VERSION 4
 
 /* status codes */
 #define S3R_OK 0
@@ -360,6 +364,101 @@ int s3r_frame_run(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const floa
  * Allocates its scratch (512 copies of the table gradient) on the first call. */
 int s3r_render_argb_backward(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* tf,
                              const float* rgba, const float* dl_drgba, float* dtf, float* ddense, void* stream);
+
+/* ------------------------------------------------------ on-disk sparse fields
+ *
+ * Reader of the reference's dataset files, written by its preprocessing tools:
+ *   <base>.s3dmm-fields           text: time step count, then per field "name min max animated"
+ *                                 (BlockTreeFieldService::readFieldInfoFile, include/s3dmm/BlockTreeFieldService.hpp:178-262)
+ *   <frame>.s3dmm-meta            binary metadata: header, compressed block tree, per level a map
+ *                                 subtree root -> {tree position, field file offset, depth}, field file size
+ *                                 (Metadata<3>, include/s3dmm/Metadata.hpp:182-214, 401-443; v0 files without header too)
+ *   <frame>.s3dmm-field#<name>    per subtree at its offset: float min, max, then one float per node
+ *                                 (BlockTreeFieldProvider<3>::fieldValuesPriv, include/s3dmm/BlockTreeFieldProvider.hpp:157-168)
+ * <frame> is <base> for a single-frame dataset, <dir>/<stem>/<stem>_tNNNNNN<ext> when <dir>/<stem> is a
+ * directory (frameOutputFileName, include/filename_util.hpp:34-46).  A subtree's node order is the
+ * BlockTreeNodes<3> order (include/s3dmm/BlockTreeNodes.hpp:60-74): blocks in depth-first pre-order down to
+ * the subtree depth, per block its 8 corners (x fastest), each node where it first appears.  Files with
+ * real_type = float (the reference's default) are read.
+ *
+ * Host-only except s3r_dataset_frame_upload.  Failures set s3r_last_error(NULL).  A dataset handle may be
+ * used from one thread at a time. */
+
+typedef struct s3r_dataset s3r_dataset;
+
+typedef struct s3r_dataset_info {
+    uint32_t format_version;    /* metadata format: 0 (no header) or 1 */
+    uint32_t time_steps;        /* time frame count (.s3dmm-fields line 2) */
+    uint32_t field_count;
+    uint32_t max_subtree_depth;
+    uint32_t max_full_level;
+    uint32_t level_count;       /* levels holding subtree roots: 0 .. level_count-1 */
+    uint32_t subtree_count;     /* metadataBlockCount() */
+    uint32_t has_time_steps;    /* 1: per-frame files in <dir>/<stem>/ */
+    uint64_t tree_blocks;       /* blocks of the whole block tree */
+    uint64_t field_file_size;   /* bytes of each field file */
+    float bc_min[3];            /* block tree bounding cube */
+    float bc_size;
+} s3r_dataset_info;
+
+typedef struct s3r_subtree_info {
+    uint32_t level, x, y, z;    /* subtree root block: level and index at that level */
+    uint32_t depth;             /* subtree depth d: (2^d+1)^3 dense vertices */
+    uint32_t tree_index;        /* position of the root in the compressed block tree */
+    uint64_t values_offset;     /* byte offset of its {min, max, values...} in each field file */
+    uint64_t node_count;        /* BlockTreeNodes<3>::nodeCount() */
+} s3r_subtree_info;
+
+/* Opens a dataset by the base name the reference's BlockTreeFieldService takes
+ * (the preprocessed mesh file name; <base>.s3dmm-meta beside it is enough). */
+int s3r_dataset_open(const char* base_name, s3r_dataset** out);
+int s3r_dataset_close(s3r_dataset* ds);
+int s3r_dataset_info_get(const s3r_dataset* ds, s3r_dataset_info* out);
+/* Field `index`: its name (NUL-terminated, truncated to name_cap), global [min, max] (NaN where the file
+ * has "-") and animated flag. */
+int s3r_dataset_field(const s3r_dataset* ds, uint32_t index, char* name, size_t name_cap, float range[2],
+                      int32_t* animated);
+/* Index of the field called `name`, or S3R_ERR_INVALID (BlockTreeFieldService::fieldIndex). */
+int s3r_dataset_field_index(const s3r_dataset* ds, const char* name, uint32_t* index);
+/* The blocks of the whole block tree at `level` (Metadata::blockTree(), CompressedBlockTree<3>), in the
+ * tree's breadth-first order: idx triples to xyz (min(cap, count) of them), the level's count to *count. */
+int s3r_dataset_tree_blocks(const s3r_dataset* ds, uint32_t level, uint32_t* xyz, uint64_t cap, uint64_t* count);
+/* The subtree roots of one level (Metadata::levels()[level]), sorted by z, then y, then x.  Writes
+ * min(cap, count) records to out (may be NULL with cap 0) and the level's count to *count.  Computes and
+ * caches node counts. */
+int s3r_dataset_subtrees(s3r_dataset* ds, uint32_t level, s3r_subtree_info* out, uint32_t cap, uint32_t* count);
+/* The subtree rooted at block idx of `level` (Metadata::subtreeData + its node count); S3R_ERR_INVALID if
+ * that block is no subtree root. */
+int s3r_dataset_subtree(s3r_dataset* ds, uint32_t level, const uint32_t idx[3], s3r_subtree_info* out);
+/* BlockTreeNodes<3>(blockTree, root, depth).data().n2i of one subtree: node_count x {x, y, z} (host). */
+int s3r_dataset_subtree_nodes(s3r_dataset* ds, uint32_t level, const uint32_t idx[3], uint16_t* n2i,
+                              uint64_t cap_nodes, uint64_t* count);
+/* BlockTreeFieldProvider<3>::fieldValues of one subtree for field `field` at time frame `frame`: its
+ * stored [min, max] and node_count values (host), S3R_NO_FIELD_VALUE where masked. */
+int s3r_dataset_subtree_values(s3r_dataset* ds, uint32_t field, uint32_t frame, uint32_t level,
+                               const uint32_t idx[3], float range[2], float* values, uint64_t cap_nodes,
+                               uint64_t* count);
+
+/* A block set of one level for s3r_frame_plan: blocks idx[nb][3] (subtree roots of `level`).  Fills
+ * blocks[nb][4] = {ix, iy, iz, depth} and node_off[nb+1]; when n2i is not NULL also the concatenated node
+ * lists (node_off[nb] x 3 uint16, n2i_cap_nodes at least that).  Subtrees are walked on `threads` host
+ * threads (0 = all cores). */
+int s3r_dataset_frame_topology(s3r_dataset* ds, uint32_t level, const uint32_t* idx, uint32_t nb,
+                               uint32_t* blocks, uint64_t* node_off, uint16_t* n2i, uint64_t n2i_cap_nodes,
+                               uint32_t threads);
+/* The field values of those blocks at node_off (host; node_off[nb] floats), their stored ranges to
+ * ranges[nb][2] (optional), read on `threads` host threads (0 = all cores), one positioned read per block. */
+int s3r_dataset_frame_values(s3r_dataset* ds, uint32_t field, uint32_t frame, uint32_t level,
+                             const uint32_t* idx, uint32_t nb, const uint64_t* node_off, float* values,
+                             float* ranges, uint32_t threads);
+/* s3r_dataset_frame_values into one of two pinned staging buffers the dataset owns, then one
+ * cudaMemcpyAsync of all node_off[nb] values to sparse (device) on `stream`: the per-block file read and
+ * two host-to-device copies of the reference's worker loop become one read pass and one copy per frame.
+ * The buffer used by the call before the previous one is waited for before it is refilled, so reading
+ * frame t+1 overlaps the copy of frame t.  Allocates pinned memory when a larger frame arrives. */
+int s3r_dataset_frame_upload(s3r_ctx* ctx, s3r_dataset* ds, uint32_t field, uint32_t frame, uint32_t level,
+                             const uint32_t* idx, uint32_t nb, const uint64_t* node_off, float* sparse,
+                             float* ranges, uint32_t threads, void* stream);
 
 #ifdef __cplusplus
 }

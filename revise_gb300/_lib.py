@@ -22,7 +22,7 @@ MAX_DEPTH = 9
 
 BRICK_F32, BRICK_F16, BRICK_BF16 = 0, 1, 2
 FILTER_EXACT, FILTER_TEXTURE = 0, 1
-ABI_VERSION = 3
+ABI_VERSION = 4
 
 u8p = C.POINTER(C.c_uint8)
 u16p = C.POINTER(C.c_uint16)
@@ -79,6 +79,19 @@ class ImagePart(C.Structure):
     _fields_ = [("pixels", vp), ("origin", C.c_int32 * 2), ("size", C.c_int32 * 2)]
 
 
+class DatasetInfo(C.Structure):
+    _fields_ = [("format_version", C.c_uint32), ("time_steps", C.c_uint32), ("field_count", C.c_uint32),
+                ("max_subtree_depth", C.c_uint32), ("max_full_level", C.c_uint32), ("level_count", C.c_uint32),
+                ("subtree_count", C.c_uint32), ("has_time_steps", C.c_uint32), ("tree_blocks", C.c_uint64),
+                ("field_file_size", C.c_uint64), ("bc_min", C.c_float * 3), ("bc_size", C.c_float)]
+
+
+class SubtreeInfo(C.Structure):
+    _fields_ = [("level", C.c_uint32), ("x", C.c_uint32), ("y", C.c_uint32), ("z", C.c_uint32),
+                ("depth", C.c_uint32), ("tree_index", C.c_uint32), ("values_offset", C.c_uint64),
+                ("node_count", C.c_uint64)]
+
+
 # name -> (restype, argtypes)
 _SIGS = {
     "s3r_abi_version": (C.c_int, []),
@@ -118,6 +131,23 @@ _SIGS = {
     "s3r_frame_render": (C.c_int, [vp, vp, C.POINTER(View), vp, vp, vp, vp, vp]),
     "s3r_frame_run": (C.c_int, [vp, vp, C.POINTER(View), vp, vp, vp, vp, vp, vp]),
     "s3r_render_argb_backward": (C.c_int, [vp, vp, C.POINTER(View), vp, vp, vp, vp, vp, vp]),
+    "s3r_dataset_open": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
+    "s3r_dataset_close": (C.c_int, [vp]),
+    "s3r_dataset_info_get": (C.c_int, [vp, C.POINTER(DatasetInfo)]),
+    "s3r_dataset_field": (C.c_int, [vp, C.c_uint32, C.c_char_p, C.c_size_t, f32p, i32p]),
+    "s3r_dataset_field_index": (C.c_int, [vp, C.c_char_p, u32p]),
+    "s3r_dataset_tree_blocks": (C.c_int, [vp, C.c_uint32, u32p, C.c_uint64, u64p]),
+    "s3r_dataset_subtrees": (C.c_int, [vp, C.c_uint32, C.POINTER(SubtreeInfo), C.c_uint32, u32p]),
+    "s3r_dataset_subtree": (C.c_int, [vp, C.c_uint32, u32p, C.POINTER(SubtreeInfo)]),
+    "s3r_dataset_subtree_nodes": (C.c_int, [vp, C.c_uint32, u32p, vp, C.c_uint64, u64p]),
+    "s3r_dataset_subtree_values": (C.c_int, [vp, C.c_uint32, C.c_uint32, C.c_uint32, u32p, f32p, vp, C.c_uint64,
+                                             u64p]),
+    "s3r_dataset_frame_topology": (C.c_int, [vp, C.c_uint32, u32p, C.c_uint32, u32p, u64p, vp, C.c_uint64,
+                                             C.c_uint32]),
+    "s3r_dataset_frame_values": (C.c_int, [vp, C.c_uint32, C.c_uint32, C.c_uint32, u32p, C.c_uint32, u64p, vp,
+                                           vp, C.c_uint32]),
+    "s3r_dataset_frame_upload": (C.c_int, [vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, u32p, C.c_uint32, u64p,
+                                           vp, vp, C.c_uint32, vp]),
 }
 
 EXPORTED = sorted(_SIGS)

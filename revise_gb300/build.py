@@ -26,7 +26,7 @@ LIB = PKG / "libs3r.so"
 INCLUDE = ROOT / "include"
 
 CUDA_SOURCES = ["interp.cu", "render.cu", "compose.cu", "noalloc.cu"]
-HOST_SOURCES = ["host.cpp"]
+HOST_SOURCES = ["host.cpp", "dataset.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

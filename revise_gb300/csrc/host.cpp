@@ -80,6 +80,8 @@ struct s3r_plan {
     uint32_t graph_kernels = 0;
 };
 
+void s3r::set_thread_error(const char* msg) { g_last_error = msg; }
+
 namespace {
 
 int fail(s3r_ctx* ctx, int code, const std::string& msg)

@@ -8,6 +8,9 @@
 
 namespace s3r {
 
+// Sets the message s3r_last_error(NULL) returns on this thread (host.cpp).
+void set_thread_error(const char* msg);
+
 constexpr float kNoField = S3R_NO_FIELD_VALUE;
 constexpr int kInterpThreads = 128;
 
