@@ -334,6 +334,7 @@ def run_gb300(a):
     extras = {}
     if not a.no_extras and rank == 0:
         extras = measure_extras(ctx, torch, np)
+        extras["ingest"] = measure_ingest(ctx, torch, np, w, with_reference=not a.no_cpu)
 
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
@@ -390,6 +391,81 @@ def run_gb300(a):
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def measure_ingest(ctx, torch, np, w, with_reference: bool):
+    """Sparse-field ingestion from the reference's on-disk format: the workload written as a dataset
+    (outside the timing), then per frame its level read and uploaded (s3r_dataset_frame_upload:
+    parallel positioned reads into pinned staging, one host-to-device copy) against the reference
+    worker's pattern (per block: open, seek, read of the field file, then separate copies of the
+    block's node list and values to the device)."""
+    import shutil
+    import tempfile
+    import time
+    from revise_gb300 import workloads
+    from revise_gb300.dataset import BlockTreeFieldService, write_dataset
+    tmp = tempfile.mkdtemp(prefix="s3r_ingest_")
+    try:
+        t0 = time.perf_counter()
+        base = tmp + "/" + w.name + ".dat"
+        write_dataset(base, workloads.tree_blocks(w), 7, w.level, [("f", workloads.dataset_values(w))])
+        t_write = time.perf_counter() - t0
+        svc = BlockTreeFieldService(base)
+        fr = svc.level_topology(w.level, w.blocks[:, :3])
+        assert np.array_equal(fr.blocks, w.blocks) and np.array_equal(fr.node_off, w.node_off)
+        dev = torch.empty(fr.nodes, dtype=torch.float32, device="cuda")
+        stream = torch.cuda.current_stream()
+        nbytes = fr.nodes * 4
+
+        def batched():
+            svc.upload(ctx, fr, 0, 0, dev, stream=stream)
+            stream.synchronize()
+
+        for _ in range(3):
+            batched()
+        ts = []
+        for _ in range(10):
+            t = time.perf_counter()
+            batched()
+            ts.append(time.perf_counter() - t)
+        ms = statistics.median(ts) * 1e3
+        host = dev.cpu().numpy()
+        svc.read_level(fr, 0, 0)
+        ok = bool(np.array_equal(host.view(np.uint32), fr.sparse.view(np.uint32)))
+        out = {"workload": f"{w.name}: level {w.level}, {fr.nblocks} subtrees, {fr.nodes} nodes "
+                           f"({nbytes / 1e6:.1f} MB of values) from a reference-format dataset in the page cache",
+               "dataset_write_s": t_write, "ms_per_level": ms, "gb_per_s": nbytes / (ms * 1e-3) / 1e9,
+               "threads": os.cpu_count(), "h2d_copies": 1, "identical_to_host_read": ok}
+        if with_reference:
+            import oracle
+            subs = [svc.metadata().subtree_data(w.level, ix) for ix in w.blocks[:, :3]]
+            offs = np.array([x.values_offset for x in subs], dtype=np.uint64)
+            cnts = np.array([x.node_count for x in subs], dtype=np.uint64)
+            n2i = [torch.from_numpy(w.block_nodes(b)[0].view(np.int16)) for b in range(w.nblocks)]
+            no = [int(v) for v in w.node_off]
+
+            def per_block():
+                vals, _ = oracle.read_blocks_per_call(base + ".s3dmm-field#f", offs, cnts)
+                v = torch.from_numpy(vals)
+                for b in range(w.nblocks):
+                    n2i[b].to("cuda")
+                    v[no[b]:no[b + 1]].to("cuda")
+                torch.cuda.synchronize()
+
+            per_block()
+            tr = []
+            for _ in range(3):
+                t = time.perf_counter()
+                per_block()
+                tr.append(time.perf_counter() - t)
+            rms = statistics.median(tr) * 1e3
+            out["reference_pattern"] = {"ms_per_level": rms, "gb_per_s": nbytes / (rms * 1e-3) / 1e9,
+                                        "threads": 1, "h2d_copies": 2 * w.nblocks, "kind": "port",
+                                        "speedup_batched": rms / ms}
+        svc.close()
+        return out
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
 
 
 def measure_extras(ctx, torch, np):

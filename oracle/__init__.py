@@ -272,3 +272,19 @@ def ref_b2f_order(bmin, bmax, cmin, cmax, eye) -> np.ndarray:
     out = np.zeros((max(cap, 1), 3), dtype=np.uint32)
     n = ref().ref_b2f_order(a, b, c0, c1, e, _p(out, C.c_uint32), C.c_uint32(cap))
     return out[:n]
+
+
+def read_blocks_per_call(path: str, offsets, counts):
+    """The reference worker's per-block field read (open, seek, read, close per block): values
+    concatenated in block order and the (nb, 2) stored ranges."""
+    offsets = np.ascontiguousarray(offsets, dtype=np.uint64)
+    counts = np.ascontiguousarray(counts, dtype=np.uint64)
+    out = np.empty(int(counts.sum()), dtype=np.float32)
+    ranges = np.empty((counts.size, 2), dtype=np.float32)
+    lib = port()
+    lib.orc_read_blocks_per_call.restype = C.c_int
+    rc = lib.orc_read_blocks_per_call(str(path).encode(), _p(offsets, C.c_uint64), _p(counts, C.c_uint64),
+                                      C.c_uint32(counts.size), _p(out, C.c_float), _p(ranges, C.c_float))
+    if rc != 0:
+        raise IOError(f"per-block read of {path} failed")
+    return out, ranges

@@ -2,7 +2,11 @@
  * s3r oracle — TEST INFRASTRUCTURE ONLY (see s3r_oracle.h).
  * Plain-C restatement of the reference's hot path; compiled with -ffp-contract=off.
  */
+#define _POSIX_C_SOURCE 200809L /* fseeko */
 #include "s3r_oracle.h"
+
+#include <stdio.h>
+#include <sys/types.h>
 
 #include <math.h>
 #include <stdlib.h>
@@ -1212,4 +1216,27 @@ double orc_render_frame_grad_f64(const orc_view* v, uint32_t nb, const uint32_t*
     free(ks);
     free(hits);
     return loss;
+}
+
+/* ---------------------------------------------------------------- per-block field read */
+
+int orc_read_blocks_per_call(const char* path, const uint64_t* offsets, const uint64_t* counts, uint32_t nb,
+                             float* out, float* ranges)
+{
+    uint64_t at = 0;
+    for (uint32_t b = 0; b < nb; ++b) {
+        FILE* f = fopen(path, "rb");
+        if (!f) return -1;
+        float r[2];
+        int ok = fseeko(f, (off_t)offsets[b], SEEK_SET) == 0 && fread(r, sizeof(float), 2, f) == 2 &&
+                 fread(out + at, sizeof(float), counts[b], f) == counts[b];
+        fclose(f);
+        if (!ok) return -1;
+        if (ranges) {
+            ranges[2 * b] = r[0];
+            ranges[2 * b + 1] = r[1];
+        }
+        at += counts[b];
+    }
+    return 0;
 }

@@ -135,6 +135,15 @@ double orc_render_frame_grad_f64(const orc_view* v, uint32_t nb, const uint32_t*
                                  const float* tf, uint32_t np, const uint32_t* pixels, const float* target,
                                  double* dtf, double* ddense);
 
+/* ---- per-block field read, as the reference's worker does it ----
+ * BlockTreeFieldService::interpolateWith constructs a BlockTreeFieldProvider per call, which opens the
+ * field file (include/s3dmm/BlockTreeFieldService.hpp:118-145, BlockTreeFieldProvider.hpp:93-106), and
+ * fieldValuesPriv seeks to the subtree and reads its range and values (:157-168).  For each of nb blocks:
+ * open `path`, seek to offsets[b], read 2 + counts[b] floats, close; values to out at the prefix sum of
+ * counts, ranges (optional) to ranges[2b].  Returns 0, or -1 on an I/O failure. */
+int orc_read_blocks_per_call(const char* path, const uint64_t* offsets, const uint64_t* counts, uint32_t nb,
+                             float* out, float* ranges);
+
 #ifdef __cplusplus
 }
 #endif

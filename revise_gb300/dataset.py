@@ -282,6 +282,11 @@ def _key(xyz: np.ndarray) -> np.ndarray:
     return xyz[:, 0] | (xyz[:, 1] << np.uint64(21)) | (xyz[:, 2] << np.uint64(42))
 
 
+def _sorted_unique(k: np.ndarray) -> np.ndarray:
+    k = np.sort(k)
+    return k[np.concatenate([[True], k[1:] != k[:-1]])] if k.size else k
+
+
 def _unkey(k: np.ndarray) -> np.ndarray:
     m = np.uint64((1 << 21) - 1)
     return np.stack([k & m, (k >> np.uint64(21)) & m, k >> np.uint64(42)], axis=1).astype(np.uint32)
@@ -298,14 +303,12 @@ class BlockTreeLayout:
     def __init__(self, blocks: np.ndarray):
         blocks = np.asarray(blocks, dtype=np.int64).reshape(-1, 4)
         top = int(blocks[:, 0].max()) if blocks.size else 0
-        keys = [set() for _ in range(top + 1)]
-        per = [np.unique(_key(blocks[blocks[:, 0] == lv, 1:4])) for lv in range(top + 1)]
+        per = [_sorted_unique(_key(blocks[blocks[:, 0] == lv, 1:4])) for lv in range(top + 1)]
         # close under ancestors, deepest level first
         for lv in range(top, 0, -1):
-            parents = np.unique(_key(_unkey(per[lv]) >> 1))
-            per[lv - 1] = np.union1d(per[lv - 1], parents)
+            parents = _key(_unkey(per[lv]) >> 1)
+            per[lv - 1] = _sorted_unique(np.concatenate([per[lv - 1], parents]))
         per[0] = np.array([0], dtype=np.uint64)
-        del keys
         self.xyz = [np.zeros((1, 3), dtype=np.uint32)]
         self.masks = []
         for lv in range(top):
@@ -411,7 +414,7 @@ def write_dataset(base: str, blocks, max_subtree_depth: int, max_full_level: int
                                                                            max_full_level)
         masks = np.concatenate(tree.masks).tobytes()
         nblk = len(masks)
-        body = struct.pack("<ffff", *bc_min, bc_size) + struct.pack("<QQ", nblk << 3, nblk) + masks
+        body = bytearray(struct.pack("<ffff", *bc_min, bc_size) + struct.pack("<QQ", nblk << 3, nblk) + masks)
         nlev = max(lv for lv, _ in roots) + 1
         body += struct.pack("<Q", nlev)
         for lv in range(nlev):
@@ -423,7 +426,7 @@ def write_dataset(base: str, blocks, max_subtree_depth: int, max_full_level: int
                 depth = min(int(tree.depth[lv][r]), max_subtree_depth)
                 body += struct.pack("<IIIIQQ", x, y, z, int(tree.base[lv] + r), offsets[k], depth)
         body += struct.pack("<Q", file_size)
-        return hdr + struct.pack("<Q", len(hdr) + 8) + body
+        return hdr + struct.pack("<Q", len(hdr) + 8) + bytes(body)
 
     # metadata with placeholder offsets, then node counts from the reader, then the final file
     info_path.write_text("time_steps\n%d\n\nfield\tmin\tmax\tanimated\n" % time_steps +

@@ -299,4 +299,55 @@ def small(seed: int = 0, level: int = 1, depths=(2, 3, 4), W: int = 96, H: int =
                    0.0, 1.5, 0.5, _tf_default(), mask_fraction=mask_fraction)
 
 
+def tree_blocks(w: Workload) -> np.ndarray:
+    """The block tree a workload's node sets define, for writing it as a dataset: every block of
+    w.level and, below each, the cells of its octree -- a cell is refined exactly when its centre
+    is one of the block's nodes, since only the cell's own children have that point as a corner.
+    Returns (n, 4) [level, x, y, z]; the ancestors above w.level are implied."""
+    out = [np.concatenate([np.full((w.nblocks, 1), w.level, dtype=np.int64),
+                           w.blocks[:, :3].astype(np.int64)], axis=1)]
+    # all blocks at once: a node is keyed by (block, x, y, z), 10 bits per coordinate (depth <= 9)
+    counts = np.diff(w.node_off.astype(np.int64))
+    owner = np.repeat(np.arange(w.nblocks, dtype=np.int64), counts)
+
+    def key(b, xyz):
+        return (b << 30) | (xyz[:, 0] << 20) | (xyz[:, 1] << 10) | xyz[:, 2]
+
+    keys = np.sort(key(owner, w.n2i.astype(np.int64)))
+    depth = w.blocks[:, 3].astype(np.int64)
+    cb = np.arange(w.nblocks, dtype=np.int64)           # block of each cell
+    cells = np.zeros((w.nblocks, 3), dtype=np.int64)    # cell coordinates at relative level j
+    for j in range(int(depth.max(initial=0))):
+        live = depth[cb] > j
+        cb, cells = cb[live], cells[live]
+        size = (1 << (depth[cb] - j))[:, None]
+        ck = key(cb, cells * size + size // 2)
+        pos = np.minimum(np.searchsorted(keys, ck), keys.size - 1)
+        ref = keys[pos] == ck
+        if not ref.any():
+            break
+        cb = np.repeat(cb[ref], 8)
+        cells = (cells[ref][:, None, :] * 2 + _CORNERS[None, :, :]).reshape(-1, 3)
+        origin = w.blocks[cb, :3].astype(np.int64) * (2 << j)
+        out.append(np.concatenate([np.full((cb.size, 1), w.level + j + 1, dtype=np.int64), origin + cells], axis=1))
+    return np.concatenate(out)
+
+
+def dataset_values(w: Workload):
+    """values_fn for revise_gb300.dataset.write_dataset: on w.level's subtrees the workload's values
+    in the subtree's node order, on coarser subtrees the no-field value."""
+    where = {tuple(int(v) for v in w.blocks[b, :3]): b for b in range(w.nblocks)}
+
+    def fn(_frame, sub, n2i):
+        if sub.level != w.level:
+            return np.full(n2i.shape[0], NO_FIELD, dtype=np.float32)
+        wn, wv = w.block_nodes(where[tuple(sub.index)])
+        k = _pack(wn.astype(np.int64))
+        o = np.argsort(k)
+        pos = np.searchsorted(k[o], _pack(n2i.astype(np.int64)))
+        return wv[o[pos]]
+
+    return fn
+
+
 CONFIGS = {"cfg1": cfg1, "cfg2": cfg2, "cfg3": cfg3, "cfg5": cfg5, "small": small}

@@ -268,3 +268,26 @@ def test_written_dataset_read_by_reference_reader(tmp_path):
         assert [sha(v[pv:pv + 2 + n]) for v in vals] == r["values_sha256"]
         pn += n
         pv += 2 + n
+
+
+def test_workload_written_as_dataset_keeps_blocks_and_values(tmp_path):
+    """A synthetic workload written in the reference format (its octree cells recovered from the
+    node sets) reads back with the same blocks, depths, node counts and node -> value pairs."""
+    from revise_gb300 import workloads
+    from revise_gb300.dataset import write_dataset
+    w = workloads.small(seed=3, level=2, depths=(1, 2, 3, 4, 5))
+    write_dataset(str(tmp_path / "w.dat"), workloads.tree_blocks(w), 5, w.level,
+                  [("f", workloads.dataset_values(w))])
+    with BlockTreeFieldService(str(tmp_path / "w.dat")) as s:
+        assert [len(lv) for lv in s.metadata().levels()] == [1, 8, 64]
+        fr = s.read_level(s.level_topology(w.level, w.blocks[:, :3]), 0, 0)
+        assert np.array_equal(fr.blocks, w.blocks) and np.array_equal(fr.node_off, w.node_off)
+        for b in range(w.nblocks):
+            a, c = int(w.node_off[b]), int(w.node_off[b + 1])
+            key = lambda n: n[:, 0].astype(np.int64) << 20 | n[:, 1].astype(np.int64) << 10 | n[:, 2]  # noqa: E731
+            oa, ob = np.argsort(key(w.n2i[a:c])), np.argsort(key(fr.n2i[a:c]))
+            assert np.array_equal(w.n2i[a:c][oa], fr.n2i[a:c][ob])
+            assert np.array_equal(w.sparse[a:c][oa].view(np.uint32), fr.sparse[a:c][ob].view(np.uint32))
+        # coarser subtrees carry no field; their stored range is computeFieldRange's empty (0, -1)
+        rng, vals = s.field_values(0, 0, 0, (0, 0, 0))
+        assert rng == (0.0, -1.0) and np.all(vals == np.float32(1e30))
