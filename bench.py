@@ -436,8 +436,61 @@ def measure_ingest(ctx, torch, np, w, with_reference: bool):
                            f"({nbytes / 1e6:.1f} MB of values) from a reference-format dataset in the page cache",
                "dataset_write_s": t_write, "ms_per_level": ms, "gb_per_s": nbytes / (ms * 1e-3) / 1e9,
                "threads": os.cpu_count(), "h2d_copies": 1, "identical_to_host_read": ok}
+        # upstream generation: level w.level-1 from the uploaded level (s3r_dataset_propagate + divide)
+        from revise_gb300.dataset import field_divide
+        md = svc.metadata()
+        subs4 = md.level_blocks(w.level)
+        vals4 = np.concatenate([svc.field_values(0, 0, w.level, x.index)[1] for x in subs4])
+        child = torch.from_numpy(vals4).cuda()
+        np3 = sum(x.node_count for x in md.level_blocks(w.level - 1))
+        sums = torch.empty(np3, device="cuda")
+        wts = torch.empty(np3, device="cuda")
+        vals3 = torch.empty(np3, device="cuda")
+        t0 = time.perf_counter()
+        counts = svc.propagate(ctx, w.level - 1, child, sums, wts)
+        t_index = time.perf_counter() - t0
+
+        def prop():
+            svc.propagate(ctx, w.level - 1, child, sums, wts, stream=stream)
+            field_divide(ctx, sums, wts, vals3, stream=stream)
+
+        for _ in range(3):
+            prop()
+        pms = []
+        for _ in range(10):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            prop()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            pms.append(e0.elapsed_time(e1))
+        out["propagate"] = {"level": w.level - 1, "parents": int(counts.size), "complete_parents": int((counts == 8).sum()),
+                            "parent_nodes": int(np3), "child_nodes": int(vals4.size), "index_build_s": t_index,
+                            "ms_per_level": statistics.median(pms)}
         if with_reference:
             import oracle
+            from oracle import fieldgen
+            t0 = time.perf_counter()
+            cv, o = {}, 0
+            for x in subs4:
+                cv[tuple(x.index)] = (x.depth, vals4[o:o + x.node_count])
+                o += x.node_count
+            res = []
+            for x in md.level_blocks(w.level - 1):
+                n2i = md.block_tree_nodes(w.level - 1, x.index)
+                f = np.zeros(x.node_count, np.float32)
+                wt = np.zeros(x.node_count, np.float32)
+                kids = []
+                for c in range(8):
+                    ci = (2 * x.index[0] + (c & 1), 2 * x.index[1] + ((c >> 1) & 1), 2 * x.index[2] + (c >> 2))
+                    if ci in cv:
+                        kids.append((c, cv[ci][0], md.block_tree_nodes(w.level, ci), cv[ci][1]))
+                fieldgen.propagate_into(n2i, x.depth, kids, f, wt)
+                res.append(fieldgen.divide(f, wt))
+            t_port = time.perf_counter() - t0
+            same = bool(np.array_equal(np.concatenate(res).view(np.uint32), vals3.cpu().numpy().view(np.uint32)))
+            out["propagate"].update({"port_s": t_port, "port_kind": "numpy restatement (oracle/fieldgen.py), 1 core",
+                                     "identical_to_port": same})
             subs = [svc.metadata().subtree_data(w.level, ix) for ix in w.blocks[:, :3]]
             offs = np.array([x.values_offset for x in subs], dtype=np.uint64)
             cnts = np.array([x.node_count for x in subs], dtype=np.uint64)

@@ -40,6 +40,9 @@
  *                              Metadata<3> (include/s3dmm/Metadata.hpp:119-499),
  *                              BlockTreeFieldProvider<3>::fieldValues (include/s3dmm/BlockTreeFieldProvider.hpp:111-168),
  *                              BlockTreeNodes<3> (include/s3dmm/BlockTreeNodes.hpp:51-183)
+ *   s3r_dataset_propagate,
+ *   s3r_field_divide           BlockTreeFieldProvider<3>::generatePropagatedField's child -> parent step
+ *                              (include/s3dmm/BlockTreeFieldProvider.hpp:270-389)
  */
 #ifndef S3R_H
 #define S3R_H
@@ -459,6 +462,28 @@ int s3r_dataset_frame_values(s3r_dataset* ds, uint32_t field, uint32_t frame, ui
 int s3r_dataset_frame_upload(s3r_ctx* ctx, s3r_dataset* ds, uint32_t field, uint32_t frame, uint32_t level,
                              const uint32_t* idx, uint32_t nb, const uint64_t* node_off, float* sparse,
                              float* ranges, uint32_t threads, void* stream);
+
+/* ---------------------------------------------------- upstream field generation
+ *
+ * The propagation step of BlockTreeFieldProvider<3>::generatePropagatedField
+ * (include/s3dmm/BlockTreeFieldProvider.hpp:270-389), one level at a time on the GPU.  child_values (device):
+ * the field on every subtree of level+1, concatenated in s3r_dataset_subtrees order, each subtree's
+ * node_count values in its node order (S3R_NO_FIELD_VALUE where masked; may be NULL when level+1 has no
+ * subtrees).  sums, weights (device): one float per node of every subtree of `level`, in the same order:
+ * the sum, in child order (c = x + 2y + 4z), of the child values that land on the node and their count --
+ * the reference's fieldValues / weightValues after its child loop.  child_count (host, optional): per parent
+ * subtree how many child subtrees it has.  With all 8 the reference's value is s3r_field_divide of the
+ * two; with fewer it first adds its generator's contributions (BlockTreeFieldFromFunc adds the function at
+ * every block corner of the subtree) to both arrays, then divides the same way.  The first call for a
+ * level works out, on the device, which child nodes land on which parent nodes (uploads both levels' node
+ * lists, fills a (2^D+1)^3 vertex map per parent, checks that every child node finds its parent node,
+ * keeps 32 bytes per parent node and frees the rest; allocates and synchronizes the device); every call
+ * then runs one gather kernel on `stream` without synchronizing. */
+int s3r_dataset_propagate(s3r_ctx* ctx, s3r_dataset* ds, uint32_t level, const float* child_values, float* sums,
+                          float* weights, uint8_t* child_count, void* stream);
+/* values[i] = weights[i] > 0 ? sums[i] / weights[i] : S3R_NO_FIELD_VALUE for n floats (device), the
+ * final transform of generatePropagatedField and of BlockTreeFieldFromFunc::generate. */
+int s3r_field_divide(s3r_ctx* ctx, const float* sums, const float* weights, uint64_t n, float* values, void* stream);
 
 #ifdef __cplusplus
 }

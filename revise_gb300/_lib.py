@@ -146,6 +146,8 @@ _SIGS = {
                                              C.c_uint32]),
     "s3r_dataset_frame_values": (C.c_int, [vp, C.c_uint32, C.c_uint32, C.c_uint32, u32p, C.c_uint32, u64p, vp,
                                            vp, C.c_uint32]),
+    "s3r_dataset_propagate": (C.c_int, [vp, vp, C.c_uint32, vp, vp, vp, u8p, vp]),
+    "s3r_field_divide": (C.c_int, [vp, vp, vp, C.c_uint64, vp, vp]),
     "s3r_dataset_frame_upload": (C.c_int, [vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, u32p, C.c_uint32, u64p,
                                            vp, vp, C.c_uint32, vp]),
 }

@@ -25,7 +25,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libs3r.so"
 INCLUDE = ROOT / "include"
 
-CUDA_SOURCES = ["interp.cu", "render.cu", "compose.cu", "noalloc.cu"]
+CUDA_SOURCES = ["interp.cu", "render.cu", "compose.cu", "noalloc.cu", "propagate.cu"]
 HOST_SOURCES = ["host.cpp", "dataset.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -98,6 +98,15 @@ bool read_file(const std::string& path, std::vector<char>& out)
     return n == 0 || (bool)is.read(out.data(), n);
 }
 
+// Device state of the propagation of one level (built on first use): per parent node the indices of
+// the child nodes that land on it.
+struct PropLevel {
+    bool ready = false;
+    int32_t* src = nullptr;           // 8 per parent node, -1 = none
+    uint64_t parent_nodes = 0, child_nodes = 0;
+    std::vector<uint8_t> child_count; // per parent subtree
+};
+
 // Reusable per-thread scratch of the node walk.
 struct WalkScratch {
     std::vector<uint64_t> seen; // one bit per dense vertex of the subtree
@@ -131,6 +140,7 @@ struct s3r_dataset {
     cudaEvent_t copied[2] = {nullptr, nullptr};
     bool pending[2] = {false, false};
     int next = 0;
+    std::vector<PropLevel> prop; // per parent level
 };
 
 namespace {
@@ -464,6 +474,8 @@ int s3r_dataset_open(const char* base_name, s3r_dataset** out)
 int s3r_dataset_close(s3r_dataset* ds)
 {
     if (!ds) return S3R_OK;
+    for (PropLevel& pl : ds->prop)
+        if (pl.src) cudaFree(pl.src);
     for (auto& kv : ds->fds) ::close(kv.second);
     for (int i = 0; i < 2; ++i) {
         if (ds->copied[i]) {
@@ -732,6 +744,151 @@ int s3r_dataset_frame_upload(s3r_ctx* ctx, s3r_dataset* ds, uint32_t field, uint
     if (e != cudaSuccess) return fail(S3R_ERR_CUDA, std::string("staging record: ") + cudaGetErrorString(e));
     ds->pending[slot] = true;
     ds->next = slot ^ 1;
+    return S3R_OK;
+}
+
+} // extern "C"
+
+namespace {
+
+int prop_fail(s3r_ctx* ctx, cudaError_t e, const char* what)
+{
+    return fail(S3R_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// Uploads what the propagation into `level` needs: both levels' node lists, the parent maps' layout,
+// each child's parent, position and shift.
+int prop_prepare(s3r_dataset& ds, uint32_t level, PropLevel& pl)
+{
+    const uint32_t nl = (uint32_t)ds.level_map.size();
+    const uint32_t p0 = ds.level_begin[level], p1 = ds.level_begin[level + 1];
+    const uint32_t c0 = level + 1 < nl ? ds.level_begin[level + 1] : 0, c1 = level + 1 < nl ? ds.level_begin[level + 2] : 0;
+    const uint32_t np = p1 - p0, nc = c1 - c0;
+    // node counts and node lists of both levels
+    std::vector<uint64_t> poff(np + 1, 0), coff(nc + 1, 0);
+    int st = parallel_ranges(np + nc, thread_count(0, (np + nc) / 16 + 1), [&](uint32_t b, uint32_t e, uint32_t) {
+        WalkScratch ws;
+        for (uint32_t i = b; i < e; ++i)
+            if (int r = ensure_node_count(ds, ds.subtrees[i < np ? p0 + i : c0 + (i - np)], ws)) return r;
+        return (int)S3R_OK;
+    });
+    if (st) return st;
+    std::vector<s3r::PropParent> parents(np);
+    uint64_t map_entries = 0;
+    for (uint32_t i = 0; i < np; ++i) {
+        const Subtree& t = ds.subtrees[p0 + i];
+        if (t.depth < 1 || t.depth > S3R_MAX_DEPTH)
+            return fail(S3R_ERR_UNSUPPORTED, "subtree depth " + std::to_string(t.depth) + " outside 1..S3R_MAX_DEPTH");
+        poff[i + 1] = poff[i] + (uint64_t)t.node_count;
+        const uint64_t e = (1ull << t.depth) + 1;
+        parents[i] = {t.depth, 0u, map_entries};
+        map_entries += e * e * e;
+    }
+    std::vector<s3r::PropChild> children(nc);
+    pl.child_count.assign(np, 0);
+    for (uint32_t k = 0; k < nc; ++k) {
+        const Subtree& t = ds.subtrees[c0 + k];
+        coff[k + 1] = coff[k] + (uint64_t)t.node_count;
+        auto it = ds.level_map[level].find(loc_key(t.x >> 1, t.y >> 1, t.z >> 1));
+        if (it == ds.level_map[level].end())
+            return fail(S3R_ERR_INVALID, "a subtree of level " + std::to_string(level + 1) + " has no parent subtree");
+        const uint32_t p = it->second - p0;
+        children[k] = {p, (t.x & 1) + 2 * (t.y & 1) + 4 * (t.z & 1), (int32_t)t.depth + 1 - (int32_t)parents[p].depth, 0u};
+        ++pl.child_count[p];
+    }
+    std::vector<uint16_t> pn2i(3 * poff[np]), cn2i(3 * coff[nc]);
+    st = parallel_ranges(np + nc, thread_count(0, (np + nc) / 16 + 1), [&](uint32_t b, uint32_t e, uint32_t) {
+        WalkScratch ws;
+        for (uint32_t i = b; i < e; ++i) {
+            if (i < np) walk_nodes(ds, ds.subtrees[p0 + i], pn2i.data() + 3 * poff[i], ws);
+            else walk_nodes(ds, ds.subtrees[c0 + (i - np)], cn2i.data() + 3 * coff[i - np], ws);
+        }
+        return (int)S3R_OK;
+    });
+    if (st) return st;
+    if (coff[nc] >= (1ull << 31)) return fail(S3R_ERR_UNSUPPORTED, "more than 2^31 child nodes in one level");
+    // temporary device copies: node lists, layout, dense maps; kept: the gather indices
+    const size_t sizes[8] = {np * sizeof(s3r::PropParent) + 1, (np + 1) * sizeof(uint64_t), pn2i.size() * 2 + 2,
+                             nc * sizeof(s3r::PropChild) + 1, (nc + 1) * sizeof(uint64_t), cn2i.size() * 2 + 2,
+                             map_entries * sizeof(int32_t) + 4, sizeof(uint32_t)};
+    void* tmp[8] = {};
+    auto release = [&]() {
+        for (void*& p : tmp)
+            if (p) cudaFree(p), p = nullptr;
+    };
+    cudaError_t e = cudaMalloc((void**)&pl.src, poff[np] * 8 * sizeof(int32_t) + 32);
+    for (int i = 0; i < 8 && e == cudaSuccess; ++i) e = cudaMalloc(&tmp[i], sizes[i]);
+    if (e != cudaSuccess) {
+        release();
+        if (pl.src) cudaFree(pl.src), pl.src = nullptr;
+        return fail(S3R_ERR_NOMEM, std::string("propagation buffers: ") + cudaGetErrorString(e));
+    }
+    const void* from[6] = {parents.data(), poff.data(), pn2i.data(), children.data(), coff.data(), cn2i.data()};
+    const size_t bytes[6] = {np * sizeof(s3r::PropParent), (np + 1) * sizeof(uint64_t), pn2i.size() * 2,
+                             nc * sizeof(s3r::PropChild), (nc + 1) * sizeof(uint64_t), cn2i.size() * 2};
+    for (int i = 0; i < 6 && e == cudaSuccess; ++i)
+        if (bytes[i]) e = cudaMemcpy(tmp[i], from[i], bytes[i], cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(tmp[7], 0, sizeof(uint32_t));
+    s3r::PropArgs a{};
+    a.parents = (const s3r::PropParent*)tmp[0];
+    a.parent_node_off = (const uint64_t*)tmp[1];
+    a.parent_n2i = (const uint16_t*)tmp[2];
+    a.children = (const s3r::PropChild*)tmp[3];
+    a.child_node_off = (const uint64_t*)tmp[4];
+    a.child_n2i = (const uint16_t*)tmp[5];
+    a.map = (int32_t*)tmp[6];
+    a.src = pl.src;
+    a.error = (uint32_t*)tmp[7];
+    a.parent_nodes = poff[np];
+    a.child_nodes = coff[nc];
+    a.nparents = np;
+    a.nchildren = nc;
+    uint32_t launches = 0, err = 0;
+    if (e == cudaSuccess) e = s3r::launch_prop_index(a, nullptr, &launches);
+    if (e == cudaSuccess) e = cudaMemcpy(&err, tmp[7], sizeof err, cudaMemcpyDeviceToHost); // synchronizes
+    release();
+    if (e != cudaSuccess || err) {
+        cudaFree(pl.src);
+        pl.src = nullptr;
+        if (e != cudaSuccess) return prop_fail(nullptr, e, "propagation index");
+        return fail(S3R_ERR_INVALID, err & 2u ? "a child node lands where its parent subtree has no node"
+                                               : "a child node lands outside its parent subtree");
+    }
+    pl.parent_nodes = poff[np];
+    pl.child_nodes = coff[nc];
+    pl.ready = true;
+    return S3R_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int s3r_dataset_propagate(s3r_ctx* ctx, s3r_dataset* ds, uint32_t level, const float* child_values, float* sums,
+                          float* weights, uint8_t* child_count, void* stream)
+{
+    if (!ctx || !ds || !sums || !weights) return fail(S3R_ERR_INVALID, "null argument");
+    if (level >= ds->level_map.size()) return fail(S3R_ERR_INVALID, "level out of range");
+    if (ds->prop.size() < ds->level_map.size()) ds->prop.resize(ds->level_map.size());
+    PropLevel& pl = ds->prop[level];
+    if (!pl.ready)
+        if (int st = prop_prepare(*ds, level, pl)) return st;
+    if (pl.child_nodes && !child_values) return fail(S3R_ERR_INVALID, "null child values");
+    const cudaError_t e =
+        s3r::launch_prop_gather(pl.src, pl.child_nodes ? child_values : sums, pl.parent_nodes, sums, weights,
+                                (cudaStream_t)stream);
+    if (pl.parent_nodes) s3r::count_launches(ctx, 1);
+    if (e != cudaSuccess) return prop_fail(ctx, e, "propagation kernel");
+    if (child_count && !pl.child_count.empty()) std::memcpy(child_count, pl.child_count.data(), pl.child_count.size());
+    return S3R_OK;
+}
+
+int s3r_field_divide(s3r_ctx* ctx, const float* sums, const float* weights, uint64_t n, float* values, void* stream)
+{
+    if (!ctx || (n && (!sums || !weights || !values))) return fail(S3R_ERR_INVALID, "null argument");
+    const cudaError_t e = s3r::launch_divide(sums, weights, n, values, (cudaStream_t)stream);
+    if (n) s3r::count_launches(ctx, 1);
+    if (e != cudaSuccess) return prop_fail(ctx, e, "divide kernel");
     return S3R_OK;
 }
 

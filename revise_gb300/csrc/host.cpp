@@ -81,6 +81,10 @@ struct s3r_plan {
 };
 
 void s3r::set_thread_error(const char* msg) { g_last_error = msg; }
+void s3r::count_launches(s3r_ctx* ctx, uint32_t n)
+{
+    if (ctx) ctx->launches += n;
+}
 
 namespace {
 

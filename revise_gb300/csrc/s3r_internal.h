@@ -109,6 +109,38 @@ int record_error(int code, const char* msg);
 int record_cuda_error(cudaError_t e, const char* what);
 
 // Kernel launchers (defined in the .cu files); all return cudaGetLastError().
+// Child -> parent propagation of one metadata level (propagate.cu).
+struct PropParent {
+    uint32_t depth;   // parent subtree depth D
+    uint32_t pad;
+    uint64_t map_off; // start of its (2^D+1)^3 dense map
+};
+struct PropChild {
+    uint32_t parent;  // index of its parent subtree
+    uint32_t c;       // local position x + 2y + 4z in the parent
+    int32_t shift;    // child depth + 1 - parent depth
+    uint32_t pad;
+};
+struct PropArgs {
+    const PropParent* parents;
+    const uint64_t* parent_node_off; // nparents+1
+    const uint16_t* parent_n2i;
+    const PropChild* children;
+    const uint64_t* child_node_off;  // nchildren+1
+    const uint16_t* child_n2i;
+    int32_t* map;                    // dense vertex -> node maps (uninitialized; entries are verified)
+    int32_t* src;                    // out: 8 child-node indices per parent node, -1 = none
+    uint32_t* error;                 // bit 0: node outside the parent; bit 1: no parent node there
+    uint64_t parent_nodes, child_nodes;
+    uint32_t nparents, nchildren;
+};
+cudaError_t launch_prop_index(const PropArgs& a, cudaStream_t s, uint32_t* launches);
+cudaError_t launch_prop_gather(const int32_t* src, const float* child_values, uint64_t n, float* sums, float* weights,
+                               cudaStream_t s);
+cudaError_t launch_divide(const float* sums, const float* weights, uint64_t n, float* values, cudaStream_t s);
+// Adds n to the context's launch counter (host.cpp).
+void count_launches(s3r_ctx* ctx, uint32_t n);
+
 cudaError_t launch_fill_f32(float* p, uint64_t n, float v, cudaStream_t s);
 cudaError_t launch_fill_u32(uint32_t* p, uint64_t n, uint32_t v, cudaStream_t s);
 cudaError_t launch_scatter_nodes(float* grid, uint32_t depth, const uint16_t* n2i, const float* sparse, uint32_t n,

@@ -464,3 +464,28 @@ def write_dataset(base: str, blocks, max_subtree_depth: int, max_full_level: int
     info_path.write_text("time_steps\n%d\n\nfield\tmin\tmax\tanimated\n" % time_steps +
                          "".join((f"{name}\t{lo:.9g}\t{hi:.9g}\t{int(has_ts)}\n" if lo <= hi else
                                   f"{name}\t-\t-\t{int(has_ts)}\n") for (name, _), (lo, hi) in zip(fields, ranges)))
+
+
+# ------------------------------------------------------------------ upstream field generation
+
+def _propagate(svc: BlockTreeFieldService, ctx, level: int, child_values, sums, weights, stream=None) -> np.ndarray:
+    from .api import _stream
+    n = len(svc.metadata().level_blocks(level))
+    counts = np.zeros(max(1, n), dtype=np.uint8)
+    ctx._check(svc._lib.s3r_dataset_propagate(ctx.h, svc._h, level, ptr(child_values), ptr(sums), ptr(weights),
+                                              arr(counts, C.c_uint8), _stream(stream)))
+    return counts[:n]
+
+
+def _field_divide(ctx, sums, weights, values, stream=None) -> None:
+    from .api import _stream
+    n = int(values.numel())
+    ctx._check(ctx.lib.s3r_field_divide(ctx.h, ptr(sums), ptr(weights), n, ptr(values), _stream(stream)))
+
+
+BlockTreeFieldService.propagate = _propagate
+BlockTreeFieldService.propagate.__doc__ = """The child -> parent step of generatePropagatedField for `level` on
+the GPU: child_values (device, the field on every subtree of level+1 in level_blocks order) -> sums and
+weights (device, one float per node of every subtree of `level`).  Returns per parent subtree its number
+of child subtrees (8: divide; fewer: add the generator's contributions first)."""
+field_divide = _field_divide
