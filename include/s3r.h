@@ -28,6 +28,9 @@
  *   s3r_block_view_rect,
  *   s3r_camera_look_at         the host-side parameter set-up of renderDenseField (:317-409, :353-372)
  *   s3r_b2f_order              BackToFrontOrder<MacroBlock<3>>::range(eye) (include/BackToFrontOrder.hpp:61-359)
+ *   s3r_split_index_cube,
+ *   s3r_split_b2f              IndexCubeSplitter<3> (include/IndexCubeSplitter.hpp) and
+ *                              IndexCubeSplitStorage::getBoxesSorted (src/s3vs_lib/IndexCubeSplitStorage.hpp)
  *   s3r_bound_rect             getBoundRect (src/s3vs_worker/cuda/VsWorker_cu.cpp:51-88)
  *   s3r_blend_image_part_host,
  *   s3r_compose_parts          blendImagePart (src/s3vs_lib/BlendImagePart.hpp:61-145)
@@ -250,6 +253,18 @@ int s3r_b2f_order(const uint32_t bmin[3], const uint32_t bmax[3], const double c
                   const double eye[3], uint32_t* out, uint32_t capacity, uint32_t* count);
 
 /* World box of an index box at level (s3vs::boundingBoxOfIndexBox, src/s3vs_worker/BlockOrderUtil.hpp:29-52). */
+/* IndexCubeSplitter<3>(level, split_count, [-5,5]^3).all_blocks(add_trailing_empty)
+ * (include/IndexCubeSplitter.hpp:36-196): the (2^level)^3 block cube cut into axis-aligned index boxes for
+ * split_count workers -- slabs along x first, then y, then z, each axis into at most 2^level slabs at
+ * i*size/slabs.  boxes: count x {min x, y, z, max x, y, z} (max exclusive), x fastest; with
+ * add_trailing_empty, empty boxes (all zero) up to split_count. */
+int s3r_split_index_cube(uint32_t level, uint32_t split_count, int32_t add_trailing_empty, uint32_t* boxes,
+                         uint32_t capacity, uint32_t* count);
+/* The same boxes in back-to-front order for the eye (IndexCubeSplitStorage::getBoxesSorted,
+ * src/s3vs_lib/IndexCubeSplitStorage.hpp:54-74: BackToFrontOrder over the splitter, whose boundaries are
+ * split at the eye coordinate by NonUniformIndexRangeSplitter). */
+int s3r_split_b2f(uint32_t level, uint32_t split_count, const double eye[3], uint32_t* boxes, uint32_t capacity,
+                  uint32_t* count);
 int s3r_index_box_world(uint32_t level, const uint32_t bmin[3], const uint32_t bmax[3], double cmin[3],
                         double cmax[3]);
 

@@ -288,3 +288,24 @@ def read_blocks_per_call(path: str, offsets, counts):
     if rc != 0:
         raise IOError(f"per-block read of {path} failed")
     return out, ranges
+
+
+def ref_split_cube(level: int, count: int, trailing: bool) -> np.ndarray:
+    """The reference's IndexCubeSplitter<3>(level, count, [-5,5]^3).all_blocks(trailing): (n, 6) boxes."""
+    lib = ref()
+    cap = max(count, 1) + 8
+    out = np.zeros((cap, 6), dtype=np.uint32)
+    n = lib.ref_split_cube(C.c_uint32(level), C.c_uint32(count), C.c_int(int(trailing)), _p(out, C.c_uint32),
+                           C.c_uint32(cap))
+    return out[:n].copy()
+
+
+def ref_split_b2f(level: int, count: int, eye) -> np.ndarray:
+    """The reference's BackToFrontOrder over that splitter for `eye`: (n, 6) boxes."""
+    lib = ref()
+    cap = max(count, 1) + 8
+    out = np.zeros((cap, 6), dtype=np.uint32)
+    e = np.ascontiguousarray(eye, dtype=np.float64)
+    n = lib.ref_split_b2f(C.c_uint32(level), C.c_uint32(count), _p(e, C.c_double), _p(out, C.c_uint32),
+                          C.c_uint32(cap))
+    return out[:n].copy()

@@ -13,7 +13,12 @@
 //                         src/s3vs_lib/BlendImagePart.hpp:61-145
 //   ref_make_ctf          s3vs::makeColorTransferVector(ctmap, colorCount)
 //                         include/s3vs/ColorTransferFunction.hpp:27-69
+//   ref_split_cube        s3dmm::IndexCubeSplitter<3>(level, count, [-5,5]^3).all_blocks(trailing)
+//                         include/IndexCubeSplitter.hpp:36-196
+//   ref_split_b2f         BackToFrontOrder over that splitter for an eye
+//                         (IndexCubeSplitStorage::getBoxesSorted, src/s3vs_lib/IndexCubeSplitStorage.hpp:54-74)
 #include "s3dmm/DenseFieldInterpolator.hpp"
+#include "IndexCubeSplitter.hpp"
 #include "s3dmm/Metadata.hpp"
 #include "BackToFrontOrder.hpp"
 #include "MacroBlock.hpp"
@@ -101,6 +106,49 @@ void ref_make_ctf(const double* xs, const double* rgba, uint32_t npoints, uint32
                                               real_type(rgba[4 * i + 2]), real_type(rgba[4 * i + 3])};
     auto v = s3vs::makeColorTransferVector(ctmap, colorCount);
     std::memcpy(out, v.data(), v.size() * sizeof(float));
+}
+
+} // extern "C"
+
+extern "C" {
+
+static BoundingBox<3, real_type> ref_cube_bbox()
+{
+    return BoundingBox<3, real_type>{} << Vec<3, real_type>{-5, -5, -5} << Vec<3, real_type>{5, 5, 5};
+}
+
+// Boxes of the splitter (6 per box: min xyz, max xyz; empty boxes as zeros); returns the count.
+int ref_split_cube(uint32_t level, uint32_t count, int trailing, uint32_t* out, uint32_t capacity)
+{
+    IndexCubeSplitter<3> sp{level, count, ref_cube_bbox()};
+    auto boxes = sp.all_blocks(trailing != 0);
+    uint32_t n = 0;
+    for (auto& b : boxes) {
+        if (n < capacity)
+            for (int a = 0; a < 3; ++a) {
+                out[6 * n + a] = b.empty() ? 0u : b.min()[a];
+                out[6 * n + 3 + a] = b.empty() ? 0u : b.max()[a];
+            }
+        ++n;
+    }
+    return (int)n;
+}
+
+int ref_split_b2f(uint32_t level, uint32_t count, const double* eye, uint32_t* out, uint32_t capacity)
+{
+    IndexCubeSplitter<3> sp{level, count, ref_cube_bbox()};
+    BackToFrontOrder b2f{sp};
+    Vec<3, real_type> e{real_type(eye[0]), real_type(eye[1]), real_type(eye[2])};
+    uint32_t n = 0;
+    for (const auto& b : b2f.range(e)) {
+        if (n < capacity)
+            for (int a = 0; a < 3; ++a) {
+                out[6 * n + a] = b.min()[a];
+                out[6 * n + 3 + a] = b.max()[a];
+            }
+        ++n;
+    }
+    return (int)n;
 }
 
 } // extern "C"

@@ -62,6 +62,17 @@ inline void InitGoogleTest(int*, char**) {}
     static ::testing::shim::Registrar shim_reg_##suite##_##name(#suite, #name,               \
                                                                 SHIM_TEST_FN(suite, name)); \
     static void SHIM_TEST_FN(suite, name)()
+#define TEST_F(fixture, name)                                                                        \
+    struct shim_fixture_##fixture##_##name : fixture {                                               \
+        void TestBody();                                                                             \
+    };                                                                                               \
+    static ::testing::shim::Registrar shim_reg_##fixture##_##name(#fixture, #name, [] {              \
+        shim_fixture_##fixture##_##name t;                                                           \
+        t.SetUp();                                                                                   \
+        t.TestBody();                                                                                \
+        t.TearDown();                                                                                \
+    });                                                                                              \
+    void shim_fixture_##fixture##_##name::TestBody()
 #define EXPECT_EQ(a, b) ::testing::shim::report_eq((a), (b), true, #a, #b, __FILE__, __LINE__)
 #define EXPECT_NE(a, b) ::testing::shim::report_eq((a), (b), false, #a, #b, __FILE__, __LINE__)
 #define EXPECT_TRUE(a) ::testing::shim::report_bool(static_cast<bool>(a), true, #a, __FILE__, __LINE__)

@@ -113,6 +113,8 @@ _SIGS = {
     "s3r_blend_image_part_mip_host": (C.c_int, [f32p, C.c_int32, C.c_int32, f32p, C.c_int32, C.c_int32, C.c_int32,
                                                 C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "s3r_b2f_order": (C.c_int, [u32p, u32p, f64p, f64p, f64p, u32p, C.c_uint32, u32p]),
+    "s3r_split_index_cube": (C.c_int, [C.c_uint32, C.c_uint32, C.c_int32, u32p, C.c_uint32, u32p]),
+    "s3r_split_b2f": (C.c_int, [C.c_uint32, C.c_uint32, f64p, u32p, C.c_uint32, u32p]),
     "s3r_index_box_world": (C.c_int, [C.c_uint32, u32p, u32p, f64p, f64p]),
     "s3r_bound_rect": (C.c_int, [vp, vp, C.c_uint32, C.c_uint32, i32p, vp]),
     "s3r_crop": (C.c_int, [vp, vp, C.c_uint32, i32p, vp, vp]),

@@ -309,6 +309,18 @@ class VsWorker:
         pass
 
     def render_scene_part(self, level: int, index_box_min, index_box_max, cancelled=lambda: False):
+        part = self.render_scene_part_device(level, index_box_min, index_box_max, cancelled)
+        if part is None:
+            return None
+        origin, size, pixels = part
+        if size[0] == 0:
+            return ImagePartResult((0, 0), (0, 0), np.zeros((0, 0), dtype=np.uint32))
+        pix = pixels.cpu().numpy().view(np.uint32).reshape(size[1], size[0])
+        return ImagePartResult(origin, size, pix)
+
+    def render_scene_part_device(self, level: int, index_box_min, index_box_max, cancelled=lambda: False):
+        """renderScenePart with the cropped part left in device memory: (origin, size, int32 tensor),
+        size (0, 0) when nothing was drawn; None when cancelled."""
         torch = _torch()
         s = self.state
         W, H = s.view.W, s.view.H
@@ -325,8 +337,7 @@ class VsWorker:
             self.renderer.render_dense_field(self.viewport, level, idx, cancelled)
         rect = self.ctx.bound_rect(self.viewport, W, H)
         if rect[2] == 0:
-            return ImagePartResult((0, 0), (0, 0), np.zeros((0, 0), dtype=np.uint32))
+            return (0, 0), (0, 0), torch.zeros(1, dtype=torch.int32, device="cuda")
         crop = torch.empty(rect[2] * rect[3], dtype=torch.int32, device="cuda")
         self.ctx.crop(self.viewport, W, rect, crop)
-        pix = crop.cpu().numpy().view(np.uint32).reshape(rect[3], rect[2])
-        return ImagePartResult((rect[0], rect[1]), (rect[2], rect[3]), pix)
+        return (int(rect[0]), int(rect[1])), (int(rect[2]), int(rect[3])), crop

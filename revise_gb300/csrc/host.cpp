@@ -235,6 +235,34 @@ Split split_range(uint32_t lo, uint32_t hi, float c0, float c1, float x)
     return s;
 }
 
+// Split of the box index range [0, n) by one eye coordinate when the boxes' boundaries sit at coords[0..n]
+// (NonUniformIndexRangeSplitter, include/NonUniformIndexRangeSplitter.hpp:27-56): the first boundary not below
+// x decides, so an eye exactly on a boundary belongs to the box before it.
+Split split_boundaries(const float* coords, uint32_t n, float x)
+{
+    const float* it = std::lower_bound(coords, coords + n + 1, x);
+    Split s;
+    if (it == coords) {
+        s.before[0] = s.before[1] = 0;
+        s.at = ~0u;
+        s.after[0] = 0;
+        s.after[1] = n;
+    } else if (it == coords + n + 1) {
+        s.before[0] = 0;
+        s.before[1] = n;
+        s.at = ~0u;
+        s.after[0] = s.after[1] = 0;
+    } else {
+        const uint32_t at = (uint32_t)(it - coords) - 1;
+        s.before[0] = 0;
+        s.before[1] = at;
+        s.at = at;
+        s.after[0] = at + 1;
+        s.after[1] = n;
+    }
+    return s;
+}
+
 // Macro-block visiting order: the 27 cells of the 3x3x3 split (0 = before the
 // eye, 1 = at it, 2 = beyond it per axis) taken corners first, then edges,
 // faces and the eye's own cell (include/BackToFrontOrder.hpp:182-209).
@@ -282,6 +310,91 @@ bool next_in_box(uint32_t p[3], const uint32_t mn[3], const uint32_t mx[3])
         }
     }
     return true;
+}
+
+// Visits a 3-D index grid in back-to-front order for the per-axis splits of
+// the eye (BackToFrontOrder::iterator, include/BackToFrontOrder.hpp:79-320):
+// macro blocks in kMacroOrder, inside each the anti-diagonal sweep, mirrored on
+// axes beyond the eye.  f(pos) gets each index triple.
+template <class F> void b2f_traverse(const Split sp[3], F&& f)
+{
+    for (uint8_t ord : kMacroOrder) {
+        const uint32_t mp[3] = {ord % 3u, (ord / 3u) % 3u, ord / 9u};
+        uint32_t mn[3], mx[3];
+        bool valid = true;
+        for (int a = 0; a < 3; ++a) {
+            const Split& s = sp[a];
+            if (mp[a] == 0) {
+                mn[a] = s.before[0];
+                mx[a] = s.before[1];
+                valid &= s.before[0] != s.before[1];
+            } else if (mp[a] == 1) {
+                mn[a] = s.at;
+                mx[a] = s.at + 1;
+                valid &= s.at != ~0u;
+            } else {
+                mn[a] = s.after[0];
+                mx[a] = s.after[1];
+                valid &= s.after[0] != s.after[1];
+            }
+        }
+        if (!valid) continue;
+        uint32_t p[3] = {mn[0], mn[1], mn[2]};
+        do {
+            uint32_t q[3];
+            for (int a = 0; a < 3; ++a) q[a] = mp[a] == 2 ? mx[a] - 1 + mn[a] - p[a] : p[a];
+            f(q);
+        } while (next_in_box(p, mn, mx));
+    }
+}
+
+// IndexCubeSplitter<3> (include/IndexCubeSplitter.hpp:36-196) over the world cube [-5, 5]^3: per axis the
+// number of slabs (split_count taken greedily along x, then y, then z, each at most 2^level) and their
+// index boundaries i*size/slabs and world boundaries (the float formula of init_axis_split).
+struct CubeSplit {
+    uint32_t n[3];
+    std::vector<uint32_t> idx[3];
+    std::vector<float> coord[3];
+};
+
+CubeSplit cube_split(uint32_t level, uint32_t split_count)
+{
+    CubeSplit cs;
+    const uint32_t size = 1u << level;
+    const uint64_t max_split = 1ull << (3 * level);
+    uint32_t count = (uint32_t)std::min<uint64_t>(max_split, split_count);
+    for (int a = 0; a < 3; ++a) {
+        if (count <= size) {
+            cs.n[a] = count;
+            count = 1;
+        } else {
+            cs.n[a] = size;
+            count = std::max(1u, count / size);
+        }
+    }
+    const float origin = -5.f, length = 10.f;
+    for (int a = 0; a < 3; ++a) {
+        const uint32_t k = cs.n[a];
+        cs.idx[a].assign(k + 1, 0);
+        cs.coord[a].assign(k + 1, 0.f);
+        cs.idx[a][k] = size;
+        cs.coord[a][0] = origin;
+        cs.coord[a][k] = origin + length;
+        for (uint32_t i = 1; i < k; ++i) {
+            const uint32_t si = (uint32_t)((uint64_t)i * size / k);
+            cs.idx[a][i] = si;
+            cs.coord[a][i] = origin + length * (float)si / (float)size;
+        }
+    }
+    return cs;
+}
+
+void put_box(const CubeSplit& cs, const uint32_t q[3], uint32_t* out)
+{
+    for (int a = 0; a < 3; ++a) {
+        out[a] = cs.idx[a][q[a]];
+        out[3 + a] = cs.idx[a][q[a] + 1];
+    }
 }
 
 // ---------------------------------------------------------------- plan
@@ -767,34 +880,49 @@ int s3r_b2f_order(const uint32_t bmin[3], const uint32_t bmax[3], const double c
         sp[a] = split_range(bmin[a], bmax[a], (float)cmin[a], (float)cmax[a], (float)eye[a]);
     }
     uint32_t n = 0;
-    for (uint8_t ord : kMacroOrder) {
-        const uint32_t mp[3] = {ord % 3u, (ord / 3u) % 3u, ord / 9u};
-        uint32_t mn[3], mx[3];
-        bool valid = true;
-        for (int a = 0; a < 3; ++a) {
-            const Split& s = sp[a];
-            if (mp[a] == 0) {
-                mn[a] = s.before[0];
-                mx[a] = s.before[1];
-                valid &= s.before[0] != s.before[1];
-            } else if (mp[a] == 1) {
-                mn[a] = s.at;
-                mx[a] = s.at + 1;
-                valid &= s.at != ~0u;
-            } else {
-                mn[a] = s.after[0];
-                mx[a] = s.after[1];
-                valid &= s.after[0] != s.after[1];
+    b2f_traverse(sp, [&](const uint32_t q[3]) {
+        if (n < capacity)
+            for (int a = 0; a < 3; ++a) out[3 * n + a] = q[a];
+        ++n;
+    });
+    *count = n;
+    return S3R_OK;
+}
+
+int s3r_split_index_cube(uint32_t level, uint32_t split_count, int32_t add_trailing_empty, uint32_t* boxes,
+                         uint32_t capacity, uint32_t* count)
+{
+    if (!count || (capacity && !boxes) || split_count == 0 || level > 20)
+        return fail(nullptr, S3R_ERR_INVALID, "bad argument");
+    const CubeSplit cs = cube_split(level, split_count);
+    uint32_t n = 0;
+    for (uint32_t z = 0; z < cs.n[2]; ++z)
+        for (uint32_t y = 0; y < cs.n[1]; ++y)
+            for (uint32_t x = 0; x < cs.n[0]; ++x) {
+                const uint32_t q[3] = {x, y, z};
+                if (n < capacity) put_box(cs, q, boxes + 6 * n);
+                ++n;
             }
-        }
-        if (!valid) continue;
-        uint32_t p[3] = {mn[0], mn[1], mn[2]};
-        do {
-            if (n < capacity)
-                for (int a = 0; a < 3; ++a) out[3 * n + a] = mp[a] == 2 ? mx[a] - 1 + mn[a] - p[a] : p[a];
-            ++n;
-        } while (next_in_box(p, mn, mx));
-    }
+    if (add_trailing_empty)
+        for (; n < split_count; ++n)
+            if (n < capacity) std::fill(boxes + 6 * n, boxes + 6 * n + 6, 0u);
+    *count = n;
+    return S3R_OK;
+}
+
+int s3r_split_b2f(uint32_t level, uint32_t split_count, const double eye[3], uint32_t* boxes, uint32_t capacity,
+                  uint32_t* count)
+{
+    if (!eye || !count || (capacity && !boxes) || split_count == 0 || level > 20)
+        return fail(nullptr, S3R_ERR_INVALID, "bad argument");
+    const CubeSplit cs = cube_split(level, split_count);
+    Split sp[3];
+    for (int a = 0; a < 3; ++a) sp[a] = split_boundaries(cs.coord[a].data(), cs.n[a], (float)eye[a]);
+    uint32_t n = 0;
+    b2f_traverse(sp, [&](const uint32_t q[3]) {
+        if (n < capacity) put_box(cs, q, boxes + 6 * n);
+        ++n;
+    });
     *count = n;
     return S3R_OK;
 }

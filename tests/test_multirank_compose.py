@@ -1,7 +1,8 @@
 """Multi-rank sort-last compositing on CPU ranks (gloo, world size 2): each rank
-renders its index box with the oracle ray caster into a cropped image part,
-rank 0 gathers and blends them back to front; the result equals the same
-composition done in one process."""
+renders its box of the reference's split with the oracle ray caster into a
+cropped image part, rank 0 gathers them and evaluates the reference's render
+graph back to front; the result equals the same composition done in one
+process."""
 import os
 import socket
 
@@ -79,5 +80,20 @@ def test_two_rank_gather_and_compose_matches_single_process():
 
 def test_box_order_puts_far_box_first():
     boxes = compose.split_boxes(2, 2)
+    assert boxes == [((0, 0, 0), (2, 4, 4)), ((2, 0, 0), (4, 4, 4))]
     assert compose.box_order(2, boxes, (100.0, 0.0, 0.0)) == [0, 1]
     assert compose.box_order(2, boxes, (-100.0, 0.0, 0.0)) == [1, 0]
+
+
+def test_compose_is_the_render_graph_of_the_sorted_parts():
+    rng = np.random.default_rng(1)
+    parts = []
+    for _ in range(5):
+        h, w = int(rng.integers(1, 9)), int(rng.integers(1, 9))
+        px = rng.integers(0, 1 << 32, (h, w), dtype=np.uint64).astype(np.uint32)
+        parts.append(((int(rng.integers(0, 20)), int(rng.integers(0, 20))), px))
+    order = [3, 0, 4, 1, 2]
+    from revise_gb300 import schedule
+    g = schedule.render_graph(schedule.affinity_for(5, 2))
+    want = schedule.run_graph(g, [schedule.Part(parts[i][0], parts[i][1]) for i in order], 32, 32, 5)
+    assert np.array_equal(compose.compose(parts, order, 32, 32, 5, thread_per_node=2), want)
