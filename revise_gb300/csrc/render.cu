@@ -801,7 +801,52 @@ struct Premul {
     float r, g, b, a;
 };
 
+// The 8 texels of sample k issued as independent loads (32-bit offsets: a brick
+// holds at most 513^3 vertices) with the cell's fractions.
+template <int Fmt> struct Texels {
+    float t[8];
+    float f[3];
+};
+
+template <int Fmt>
+__device__ __forceinline__ void fetch_texels(const void* brick, const BlockRay& r, int k, Texels<Fmt>& x)
+{
+    Cell c;
+    sample_cell(r, k, c);
+    const uint32_t n = r.n;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const uint32_t xi = (q & 1) ? c.i1[0] : c.i0[0];
+        const uint32_t yi = (q & 2) ? c.i1[1] : c.i0[1];
+        const uint32_t zi = (q & 4) ? c.i1[2] : c.i0[2];
+        x.t[q] = Brick<Fmt>::get(brick, (zi * n + yi) * n + xi);
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) x.f[d] = c.f[d];
+}
+
+// Trilinear value of fetched texels; false when one of them is NaN (outside the domain).
+template <int Fmt> __device__ __forceinline__ bool filter_texels(const Texels<Fmt>& x, float& val)
+{
+    bool bad = false;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) bad |= isnan(x.t[q]);
+    if (bad) return false;
+    const float* t = x.t;
+    const float x00 = __fmaf_rn(x.f[0], t[1] - t[0], t[0]);
+    const float x10 = __fmaf_rn(x.f[0], t[3] - t[2], t[2]);
+    const float x01 = __fmaf_rn(x.f[0], t[5] - t[4], t[4]);
+    const float x11 = __fmaf_rn(x.f[0], t[7] - t[6], t[6]);
+    const float y0 = __fmaf_rn(x.f[1], x10 - x00, x00);
+    const float y1 = __fmaf_rn(x.f[1], x11 - x01, x01);
+    val = __fmaf_rn(x.f[2], y1 - y0, y0);
+    return true;
+}
+
 // March one block along a ray (premultiplied, block-local early termination).
+// Exact filter: software-pipelined -- sample k+1's texel loads are issued
+// before sample k is filtered, looked up and composited, so a ray keeps two
+// samples' loads in flight; the arithmetic and its order are unchanged.
 template <int Fmt, bool kTex>
 __device__ __forceinline__ Premul march_block(const s3r_view& v, const BlockRay& r, const void* brick, float scale,
                                               float offset, uint32_t depth, const float4* tf, float of,
@@ -810,21 +855,37 @@ __device__ __forceinline__ Premul march_block(const s3r_view& v, const BlockRay&
     const float span = v.field_max - v.field_min;
     const float il = layer_exponent(depth, v.level, v.quality);
     Premul acc{0.f, 0.f, 0.f, 0.f};
+    if constexpr (!kTex) {
+        if (r.samples < 2) return acc;
+        Texels<Fmt> cur, nxt;
+        fetch_texels<Fmt>(brick, r, 0, cur);
+        for (int i = 1; i < r.samples; ++i) {
+            ++taken;
+            if (i + 1 < r.samples) fetch_texels<Fmt>(brick, r, i, nxt);
+            float val;
+            if (filter_texels<Fmt>(cur, val)) {
+                if (Fmt != S3R_BRICK_F32) val = __fmaf_rn(scale, val, offset);
+                const float v01 = __fdiv_rn(__fsub_rn(val, v.field_min), span);
+                const float4 col = tf_lookup(tf, v.tf_n, v01).c;
+                const float a = __fsub_rn(1.f, __powf(__fmaf_rn(-col.w, of, 1.f), il));
+                const float w = __fmul_rn(__fsub_rn(1.f, acc.a), a);
+                acc.r = __fmaf_rn(w, col.x, acc.r);
+                acc.g = __fmaf_rn(w, col.y, acc.g);
+                acc.b = __fmaf_rn(w, col.z, acc.b);
+                acc.a = __fadd_rn(acc.a, w);
+                if (acc.a > kAlphaThreshold) break;
+            }
+            cur = nxt;
+        }
+        return acc;
+    }
     for (int i = 1; i < r.samples; ++i) {
         ++taken;
         float val;
-        if constexpr (kTex) {
-            if (!tex_trilinear<Fmt>(brick, r, i - 1, val)) continue;
-        } else {
-            Cell cell;
-            sample_cell(r, i - 1, cell);
-            float t[8];
-            uint64_t off[8];
-            if (!trilinear<Fmt>(brick, cell, r.n, val, t, off)) continue;
-        }
+        if (!tex_trilinear<Fmt>(brick, r, i - 1, val)) continue;
         if (Fmt != S3R_BRICK_F32) val = __fmaf_rn(scale, val, offset);
         const float v01 = __fdiv_rn(__fsub_rn(val, v.field_min), span);
-        const float4 col = kTex ? tex_tf_lookup(tf, v.tf_n, v01) : tf_lookup(tf, v.tf_n, v01).c;
+        const float4 col = tex_tf_lookup(tf, v.tf_n, v01);
         const float a = __fsub_rn(1.f, __powf(__fmaf_rn(-col.w, of, 1.f), il));
         const float w = __fmul_rn(__fsub_rn(1.f, acc.a), a);
         acc.r = __fmaf_rn(w, col.x, acc.r);
