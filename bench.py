@@ -335,6 +335,7 @@ def run_gb300(a):
     if not a.no_extras and rank == 0:
         extras = measure_extras(ctx, torch, np)
         extras["ingest"] = measure_ingest(ctx, torch, np, w, with_reference=not a.no_cpu)
+        extras["modes"] = measure_modes(ctx, torch, np, with_reference=not a.no_cpu)
 
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
@@ -519,6 +520,95 @@ def measure_ingest(ctx, torch, np, w, with_reference: bool):
         return out
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
+
+
+MODE_NAMES = {0: "isosurface", 1: "isosurfaces", 2: "max_intensity", 3: "argb", 4: "argb_light",
+              5: "domain_voxels", 6: "value_on_isosurface", 7: "value_on_isosurfaces"}
+
+
+def measure_modes(ctx, torch, np, with_reference: bool):
+    """Every field mode of the per-block renderer (s3r_render_block; texture filter, and the exact
+    filter beside it) over cfg2's 64
+    blocks of depth 6 at 1920x1080, back to front into one viewport: the summed CUDA-event times of the
+    64 render launches (each block's dense field interpolated first, not timed); beside it the same
+    measurement of the reference's own renderKernel<mode> (its kernels from cubins) when built."""
+    from revise_gb300 import _lib, host, workloads
+    from revise_gb300.api import to_device_n2i
+    w = workloads.cfg2()
+    m = 1 << w.level
+    order = host.b2f_order([0, 0, 0], [m, m, m], [-5.0] * 3, [5.0] * 3, w.eye)
+    where = {tuple(b[:3]): i for i, b in enumerate(w.blocks.tolist())}
+    oi = np.array([where[tuple(b)] for b in order.tolist()])
+    tf = torch.from_numpy(np.ascontiguousarray(w.tf)).cuda()
+    dense, dense2 = {}, {}
+    u = np.empty_like(w.sparse)
+    for b in range(w.nblocks):
+        a, c = int(w.node_off[b]), int(w.node_off[b + 1])
+        x = w.n2i[a:c].astype(np.float64) / (1 << int(w.blocks[b, 3])) + w.blocks[b, :3]
+        u[a:c] = (0.25 * x[:, 0] + 0.2 * x[:, 1] + 0.1 * x[:, 2]).astype(np.float32)
+    for b in range(w.nblocks):
+        n2i, sp = w.block_nodes(b)
+        d = int(w.blocks[b, 3])
+        dn = to_device_n2i(n2i)
+        dense[b] = ctx.interp_dense(dn, torch.from_numpy(np.ascontiguousarray(sp)).cuda(), d)
+        a, c = int(w.node_off[b]), int(w.node_off[b + 1])
+        dense2[b] = ctx.interp_dense(dn, torch.from_numpy(np.ascontiguousarray(u[a:c])).cuda(), d)
+    refcu = None
+    if with_reference:
+        try:
+            from oracle import refcu as _r
+            if _r.available():
+                refcu = _r
+                refcu.set_tf(np.ascontiguousarray(w.tf, np.float32))
+        except Exception:
+            refcu = None
+    out = {"workload": "cfg2: 4x4x4 blocks of depth 6 (17.6 M dense vertices), 1920x1080, texture filter, "
+                       "64 render launches back to front, interpolation excluded"}
+    span = w.field_max - w.field_min
+    for mode, name in MODE_NAMES.items():
+        view = host.view_for(w, filter=_lib.FILTER_TEXTURE)
+        rel = lambda r: float(np.float32(w.field_min + r * span))  # noqa: E731
+        if mode in (_lib.MODE_ISOSURFACE, _lib.MODE_VALUE_ON_ISOSURFACE):
+            view.threshold = rel(0.45)
+        elif mode in (_lib.MODE_ISOSURFACES, _lib.MODE_VALUE_ON_ISOSURFACES):
+            view.threshold = 0.0
+        levels = [rel(x) for x in (0.2, 0.35, 0.5, 0.65, 0.8)] if mode in (
+            _lib.MODE_ISOSURFACES, _lib.MODE_VALUE_ON_ISOSURFACES) else []
+        two = mode in (_lib.MODE_VALUE_ON_ISOSURFACE, _lib.MODE_VALUE_ON_ISOSURFACES)
+        pres = host.presentation(mode, view, isosurface_opacity=0.6, levels=levels,
+                                 secondary_range=(0.0, 1.1) if two else (0.0, 1.0))
+        clear = 0x7FC00000 if mode == _lib.MODE_MAX_INTENSITY else 0
+        rects = np.array([host.block_view_rect(view, w.blocks[b, :3]) for b in range(w.nblocks)], np.int32)
+        vp = torch.full((w.W * w.H,), clear, dtype=torch.int64, device="cuda").to(torch.int32)
+
+        def frame():
+            evs = []
+            for b in oi:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                ctx.render_block(view, pres, dense[b], int(w.blocks[b, 3]), [int(x) for x in w.blocks[b, :3]],
+                                 rects[b], tf, vp, brick2=dense2[b] if two else None)
+                e1.record()
+                evs.append((e0, e1))
+            torch.cuda.synchronize()
+            return sum(x.elapsed_time(y) for x, y in evs)
+
+        frame()
+        ours = statistics.median([frame() for _ in range(3)])
+        view.filter = _lib.FILTER_EXACT
+        frame()
+        ours_exact = statistics.median([frame() for _ in range(3)])
+        view.filter = _lib.FILTER_TEXTURE
+        rec = {"ms": ours, "ms_exact_filter": ours_exact}
+        if refcu is not None:
+            try:
+                rms = statistics.median([refcu.time_render(view, pres, w, oi, rects, u if two else None, clear)[0]
+                                         for _ in range(3)])
+                rec.update({"reference_kernels_ms": rms, "speedup": rms / ours})
+            except Exception as e:
+                rec["reference_kernels"] = f"unavailable: {type(e).__name__}: {e}"
+        out[name] = rec
+    return out
 
 
 def measure_extras(ctx, torch, np):

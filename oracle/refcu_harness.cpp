@@ -450,3 +450,46 @@ int ref_cuda_worker(const void* view, uint32_t nblocks, const uint32_t* blocks, 
 }
 
 } // extern "C"
+
+extern "C" {
+
+// Kernel time of the reference's renderKernel<mode> over a block set already in back-to-front order:
+// per block its dense field interpolated (not timed; the secondary field too when sparse2 is given), then
+// the render launch bracketed by CUDA events.  viewport (host, W*H) is the initial and final image;
+// *ms the sum of the render launches' event times.
+int ref_cuda_time_render(const void* view, const void* pres, uint32_t nblocks, const uint32_t* blocks,
+                         const uint64_t* node_off, const uint16_t* n2i, const float* sparse, const float* sparse2,
+                         const int32_t* rects, uint32_t* viewport, double* ms)
+{
+    const View& v = *static_cast<const View*>(view);
+    const size_t npx = (size_t)v.W * v.H;
+    uint32_t* d = nullptr;
+    CKR(cudaMalloc(&d, npx * 4));
+    CKR(cudaMemcpy(d, viewport, npx * 4, cudaMemcpyHostToDevice));
+    cudaEvent_t e0, e1;
+    CKR(cudaEventCreate(&e0));
+    CKR(cudaEventCreate(&e1));
+    double total = 0;
+    for (uint32_t i = 0; i < nblocks; ++i) {
+        const uint64_t a = node_off[i], b = node_off[i + 1];
+        const uint32_t depth = blocks[4 * i + 3];
+        if (interp_into_field(n2i + 3 * a, sparse + a, (uint32_t)(b - a), depth)) return 1;
+        if (sparse2 && interp_into(g_field2, n2i + 3 * a, sparse2 + a, (uint32_t)(b - a), depth)) return 1;
+        CKR(cudaDeviceSynchronize());
+        CKR(cudaEventRecord(e0, 0));
+        if (render_block(v, depth, blocks + 4 * i, rects + 4 * i, d, static_cast<const Pres*>(pres))) return 1;
+        CKR(cudaEventRecord(e1, 0));
+        CKR(cudaEventSynchronize(e1));
+        float t = 0;
+        CKR(cudaEventElapsedTime(&t, e0, e1));
+        total += t;
+    }
+    CKR(cudaMemcpy(viewport, d, npx * 4, cudaMemcpyDeviceToHost));
+    CKR(cudaEventDestroy(e0));
+    CKR(cudaEventDestroy(e1));
+    CKR(cudaFree(d));
+    *ms = total;
+    return 0;
+}
+
+} // extern "C"
