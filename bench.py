@@ -563,7 +563,15 @@ def measure_modes(ctx, torch, np, with_reference: bool):
         except Exception:
             refcu = None
     out = {"workload": "cfg2: 4x4x4 blocks of depth 6 (17.6 M dense vertices), 1920x1080, texture filter, "
-                       "64 render launches back to front, interpolation excluded"}
+                       "64 render launches back to front, interpolation excluded; batched_ms: the whole frame "
+                       "in one s3r_frame_render_mode launch (exact filter, FP32 compositing) on resident bricks"}
+    from revise_gb300.api import FramePlan
+    plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=16)
+    plan.interp(torch.from_numpy(w.sparse).cuda())
+    plan2 = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=16)
+    plan2.interp(torch.from_numpy(np.ascontiguousarray(u)).cuda())
+    bricks2, _ = plan2.bricks()
+    frame_img = torch.zeros(w.W * w.H * 4, device="cuda")
     span = w.field_max - w.field_min
     for mode, name in MODE_NAMES.items():
         view = host.view_for(w, filter=_lib.FILTER_TEXTURE)
@@ -598,16 +606,31 @@ def measure_modes(ctx, torch, np, with_reference: bool):
         view.filter = _lib.FILTER_EXACT
         frame()
         ours_exact = statistics.median([frame() for _ in range(3)])
+        bview = host.view_for(w, filter=_lib.FILTER_EXACT)
+        bview.threshold = view.threshold
+
+        def batched():
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            plan.render_mode(bview, pres, tf, bricks2 if two else None, frame_img)
+            e1.record()
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1)
+
+        batched()
+        bms = statistics.median([batched() for _ in range(5)])
         view.filter = _lib.FILTER_TEXTURE
-        rec = {"ms": ours, "ms_exact_filter": ours_exact}
+        rec = {"ms": ours, "ms_exact_filter": ours_exact, "batched_ms": bms}
         if refcu is not None:
             try:
                 rms = statistics.median([refcu.time_render(view, pres, w, oi, rects, u if two else None, clear)[0]
                                          for _ in range(3)])
-                rec.update({"reference_kernels_ms": rms, "speedup": rms / ours})
+                rec.update({"reference_kernels_ms": rms, "speedup": rms / ours, "speedup_batched": rms / bms})
             except Exception as e:
                 rec["reference_kernels"] = f"unavailable: {type(e).__name__}: {e}"
         out[name] = rec
+    plan.close()
+    plan2.close()
     return out
 
 

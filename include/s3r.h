@@ -367,6 +367,18 @@ int s3r_frame_interp(s3r_ctx* ctx, s3r_plan* plan, const float* sparse, void* st
 int s3r_frame_render(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* tf, float* rgba,
                      uint32_t* argb, unsigned long long* samples, void* stream);
 
+/* The batched frame in any field mode (pres, as for s3r_render_block): every ray walks the plan's blocks
+ * front to back, each block marched exactly as s3r_render_block marches it, the blocks' colours
+ * composited in FP32 (no ARGB8 rounding between blocks), for max intensity the maximum over the blocks.
+ * bricks2 (device): the secondary field's brick store in this plan's layout (s3r_plan_bricks of a second
+ * plan over the same block set), needed by the value-on-isosurface modes, else may be NULL.
+ * rgba (optional): W*H float RGBA, non-premultiplied (max intensity: t, t, t, 1 with t the relative
+ * maximum, zero where no block gave one); argb (optional): ARGB32 (max intensity: the float bits of t,
+ * NaN bits where none, as the reference's viewport holds them).  F32 plans only (else
+ * S3R_ERR_UNSUPPORTED). */
+int s3r_frame_render_mode(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const s3r_presentation* pres,
+                          const float* tf, const void* bricks2, float* rgba, uint32_t* argb, void* stream);
+
 /* s3r_frame_interp + s3r_frame_render as one CUDA graph, captured on the first
  * call for this (plan, pointers, viewport size, tf_n, filter) and replayed
  * afterwards; the view is copied to the device before each replay.  Allocates

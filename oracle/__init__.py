@@ -309,3 +309,17 @@ def ref_split_b2f(level: int, count: int, eye) -> np.ndarray:
     n = lib.ref_split_b2f(C.c_uint32(level), C.c_uint32(count), _p(e, C.c_double), _p(out, C.c_uint32),
                           C.c_uint32(cap))
     return out[:n].copy()
+
+
+def render_frame_mode(view: OrcView, pres: OrcPresentation, w, dense: np.ndarray, rects, tf: np.ndarray,
+                      alpha_stop: float, dense2=None) -> np.ndarray:
+    """Batched field-mode frame in FP32: (W*H, 4) float RGBA (see orc_render_frame_mode)."""
+    blocks, off, dense, rects, rp = _frame_args(w, dense, rects)
+    tf = np.ascontiguousarray(tf, dtype=np.float32)
+    d2 = None if dense2 is None else np.ascontiguousarray(dense2, dtype=np.float32)
+    out = np.zeros((view.W * view.H, 4), dtype=np.float32)
+    port().orc_render_frame_mode(C.byref(view), C.byref(pres), C.c_uint32(blocks.shape[0]), _p(blocks, C.c_uint32),
+                                 _p(off, C.c_uint64), _p(dense, C.c_float),
+                                 _p(d2, C.c_float) if d2 is not None else None, rp, _p(tf, C.c_float),
+                                 C.c_float(alpha_stop), _p(out, C.c_float))
+    return out

@@ -624,8 +624,10 @@ static int find_interval(float val, const float* levels, uint32_t count)
     return i2;
 }
 
-static void mode_pixel(const orc_view* v, const orc_presentation* pr, const orc_ray* r, const float* brick,
-                       const float* brick2, uint32_t depth, const float* tf, uint32_t* px)
+/* What one block contributes to one pixel in a field mode: *kind 0 nothing, 1 the colour gathered front to
+ * back in the block (acc, non-premultiplied), 2 the relative maximum (*t, max intensity), 3 clear. */
+static void mode_block(const orc_view* v, const orc_presentation* pr, const orc_ray* r, const float* brick,
+                       const float* brick2, uint32_t depth, const float* tf, int* kind, float acc[4], float* t_out)
 {
     const uint32_t n = r->n;
     const float span = v->field_max - v->field_min;
@@ -653,15 +655,14 @@ static void mode_pixel(const orc_view* v, const orc_presentation* pr, const orc_
             const float val = field_at(v, brick, n, tc);
             if (val >= v->threshold && maxv < val) maxv = val;
         }
+        *kind = 0;
         if (maxv < v->field_min) return;
-        const float t = (maxv - v->field_min) / span;
-        float prev;
-        memcpy(&prev, px, 4);
-        if (!isnan(prev) && prev > t) return;
-        memcpy(px, &t, 4);
+        *t_out = (maxv - v->field_min) / span;
+        *kind = 2;
         return;
     }
-    float acc[4] = {0.f, 0.f, 0.f, 0.f}, ex[4];
+    acc[0] = acc[1] = acc[2] = acc[3] = 0.f;
+    *kind = 1;
     if (mode == 3 || mode == 4 || mode == 5) {
         const float of = opacity_factor(v), il = layer_exponent(v, depth);
         float dom[4] = {0, 0, 0, 0};
@@ -689,15 +690,12 @@ static void mode_pixel(const orc_view* v, const orc_presentation* pr, const orc_
             blend_behind(acc, col);
             if (acc[3] > 0.996f) break;
         }
-        argb_to_rgba(*px, ex);
-        blend_above(ex, acc);
-        *px = rgba_to_argb(ex);
         return;
     }
     const int multi = mode == 1 || mode == 7, secondary = mode == 6 || mode == 7;
     const uint32_t nl = pr->level_count;
     if (multi && nl < 1) {
-        *px = 0u;
+        *kind = 3;
         return;
     }
     ORC_POS(0);
@@ -777,11 +775,30 @@ static void mode_pixel(const orc_view* v, const orc_presentation* pr, const orc_
         v1 = v2;
     }
 done:
-    argb_to_rgba(*px, ex);
-    blend_above(ex, acc);
-    *px = rgba_to_argb(ex);
+    return;
 #undef ORC_POS
 }
+
+static void mode_pixel(const orc_view* v, const orc_presentation* pr, const orc_ray* r, const float* brick,
+                       const float* brick2, uint32_t depth, const float* tf, uint32_t* px)
+{
+    int kind = 0;
+    float acc[4], t = 0.f, ex[4];
+    mode_block(v, pr, r, brick, brick2, depth, tf, &kind, acc, &t);
+    if (kind == 2) {
+        float prev;
+        memcpy(&prev, px, 4);
+        if (!isnan(prev) && prev > t) return;
+        memcpy(px, &t, 4);
+    } else if (kind == 1) {
+        argb_to_rgba(*px, ex);
+        blend_above(ex, acc);
+        *px = rgba_to_argb(ex);
+    } else if (kind == 3) {
+        *px = 0u;
+    }
+}
+
 
 void orc_render_block_mode(const orc_view* v, const orc_presentation* pr, const float* brick, const float* brick2,
                            uint32_t depth, const uint32_t idx[3], const int32_t rect[4], const float* tf,
@@ -1018,6 +1035,48 @@ void orc_render_frame_argb8(const orc_view* v, uint32_t nb, const uint32_t* bloc
                 argb_to_rgba(*px, ex);
                 blend_above(ex, rgba);
                 *px = rgba_to_argb(ex);
+            }
+        }
+    }
+    free(hits);
+}
+
+void orc_render_frame_mode(const orc_view* v, const orc_presentation* pr, uint32_t nb, const uint32_t* blocks,
+                           const uint64_t* dense_off, const float* dense, const float* dense2, const int32_t* rects,
+                           const float* tf, float alpha_stop, float* rgba)
+{
+    hit* hits = (hit*)malloc(sizeof(hit) * (nb ? nb : 1));
+    const int mip = pr->mode == 2;
+    for (uint32_t vy = 0; vy < v->H; ++vy) {
+        for (uint32_t vx = 0; vx < v->W; ++vx) {
+            int nh = collect_hits(v, nb, blocks, rects, vx, vy, hits);
+            float F[4] = {0.f, 0.f, 0.f, 0.f}, best = 0.f;
+            int have = 0;
+            for (int j = nh - 1; j >= 0; --j) { /* near first */
+                const uint32_t b = hits[j].block;
+                int kind = 0;
+                float acc[4], t = 0.f;
+                mode_block(v, pr, &hits[j].r, dense + dense_off[b], dense2 ? dense2 + dense_off[b] : NULL,
+                           blocks[4 * b + 3], tf, &kind, acc, &t);
+                if (kind == 2) {
+                    if (!have || t > best) best = t;
+                    have = 1;
+                } else if (kind == 1) {
+                    const float T = 1.f - F[3];
+                    for (int c = 0; c < 3; ++c) F[c] = fmaf(T, acc[c] * acc[3], F[c]);
+                    F[3] = fmaf(T, acc[3], F[3]);
+                } else if (kind == 3) {
+                    break;
+                }
+                if (!mip && F[3] > alpha_stop) break;
+            }
+            float* o = rgba + 4 * ((size_t)(v->H - 1 - vy) * v->W + vx);
+            if (mip) {
+                o[0] = o[1] = o[2] = have ? best : 0.f;
+                o[3] = have ? 1.f : 0.f;
+            } else {
+                o[3] = F[3];
+                for (int c = 0; c < 3; ++c) o[c] = F[3] > 0.f ? F[c] / F[3] : 0.f;
             }
         }
     }

@@ -119,6 +119,14 @@ void orc_render_frame_f64(const orc_view* v, uint32_t nb, const uint32_t* blocks
 void orc_render_frame_argb8(const orc_view* v, uint32_t nb, const uint32_t* blocks, const uint64_t* dense_off,
                             const float* dense, const int32_t* rects, const float* tf, uint32_t* viewport);
 
+/* ---- batched field modes: per pixel the blocks front to back, each marched as orc_render_block_mode marches
+ * it, their colours composited in FP32 (premultiplied, stop once alpha exceeds alpha_stop), max intensity the
+ * maximum over the blocks, a cleared pixel (multi-level mode without levels) ending the walk.  rgba: W*H*4
+ * floats, non-premultiplied (max intensity: t, t, t, 1, zero where no block gave a maximum). ---- */
+void orc_render_frame_mode(const orc_view* v, const orc_presentation* pr, uint32_t nb, const uint32_t* blocks,
+                           const uint64_t* dense_off, const float* dense, const float* dense2, const int32_t* rects,
+                           const float* tf, float alpha_stop, float* rgba);
+
 /* ---- image-part blend (src/s3vs_lib/BlendImagePart.hpp:61-145) ---- */
 void orc_blend_image_part(uint32_t* dst, int32_t dw, int32_t dh, const uint32_t* src, int32_t sw, int32_t sh,
                           int32_t ox, int32_t oy, int32_t just_copy, int32_t offx, int32_t offy);

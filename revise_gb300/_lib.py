@@ -131,6 +131,7 @@ _SIGS = {
     "s3r_plan_autotune": (C.c_int, [vp, vp, C.POINTER(View), vp, vp, C.c_uint32, vp]),
     "s3r_frame_interp": (C.c_int, [vp, vp, vp, vp]),
     "s3r_frame_render": (C.c_int, [vp, vp, C.POINTER(View), vp, vp, vp, vp, vp]),
+    "s3r_frame_render_mode": (C.c_int, [vp, vp, C.POINTER(View), C.POINTER(Presentation), vp, vp, vp, vp, vp]),
     "s3r_frame_run": (C.c_int, [vp, vp, C.POINTER(View), vp, vp, vp, vp, vp, vp]),
     "s3r_render_argb_backward": (C.c_int, [vp, vp, C.POINTER(View), vp, vp, vp, vp, vp, vp]),
     "s3r_dataset_open": (C.c_int, [C.c_char_p, C.POINTER(vp)]),

@@ -216,6 +216,12 @@ class FramePlan:
         self.ctx._check(self.lib.s3r_frame_render(self.ctx.h, self.h, C.byref(view), ptr(tf_dev), ptr(rgba),
                                                   ptr(argb), ptr(samples), _stream(stream)))
 
+    def render_mode(self, view: View, pres, tf_dev, bricks2=None, rgba=None, argb=None, stream=None):
+        """The batched frame in any field mode; bricks2: the secondary field's brick store (another plan's
+        bricks() over the same blocks) for the value-on-isosurface modes."""
+        self.ctx._check(self.lib.s3r_frame_render_mode(self.ctx.h, self.h, C.byref(view), C.byref(pres), ptr(tf_dev),
+                                                        ptr(bricks2), ptr(rgba), ptr(argb), _stream(stream)))
+
     def run(self, view: View, sparse_dev, tf_dev, rgba=None, argb=None, samples=None, stream=None):
         self.ctx._check(self.lib.s3r_frame_run(self.ctx.h, self.h, C.byref(view), ptr(sparse_dev), ptr(tf_dev),
                                                ptr(rgba), ptr(argb), ptr(samples), _stream(stream)))

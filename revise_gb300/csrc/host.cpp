@@ -1298,6 +1298,37 @@ int s3r_frame_render(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const f
     return rc;
 }
 
+int s3r_frame_render_mode(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const s3r_presentation* pres,
+                          const float* tf, const void* bricks2, float* rgba, uint32_t* argb, void* stream)
+{
+    if (!ctx || !plan || !tf || !pres) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (plan->ctx != ctx) return fail(ctx, S3R_ERR_INVALID, "plan belongs to another context");
+    int rc = check_view(ctx, view);
+    if (rc) return rc;
+    if (view->level != plan->level) return fail(ctx, S3R_ERR_INVALID, "view level differs from the plan level");
+    if (pres->mode > S3R_MODE_VALUE_ON_ISOSURFACES) return fail(ctx, S3R_ERR_INVALID, "unknown field mode");
+    if (pres->level_count > S3R_MAX_LEVELS || pres->light_count > S3R_MAX_LIGHTS)
+        return fail(ctx, S3R_ERR_INVALID, "too many levels or lights");
+    if ((pres->mode == S3R_MODE_VALUE_ON_ISOSURFACE || pres->mode == S3R_MODE_VALUE_ON_ISOSURFACES) && !bricks2)
+        return fail(ctx, S3R_ERR_INVALID, "the value-on-isosurface modes need the secondary bricks");
+    if (plan->fmt != S3R_BRICK_F32) return fail(ctx, S3R_ERR_UNSUPPORTED, "field modes need F32 bricks");
+    if ((rc = set_device(ctx))) return rc;
+    cudaStream_t s = as_stream(stream);
+    if ((rc = plan_stage_view(plan, view, s))) return rc;
+    FrameArgs fa{};
+    fa.view = plan->view_dev;
+    fa.table = plan->table_dev;
+    fa.bricks = plan->bricks;
+    fa.tf = tf;
+    fa.rgba = rgba;
+    fa.argb = argb;
+    fa.cover = plan->cover_dev;
+    S3R_CUDA(ctx, launch_frame_render_mode(fa, *pres, static_cast<const float*>(bricks2), view->W, view->H, view->tf_n,
+                                           view->filter, s));
+    ++ctx->launches;
+    return S3R_OK;
+}
+
 int s3r_frame_run(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* sparse, const float* tf,
                   float* rgba, uint32_t* argb, unsigned long long* samples, void* stream)
 {

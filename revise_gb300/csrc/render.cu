@@ -535,25 +535,24 @@ __device__ __forceinline__ int find_interval(float v, const float* levels, uint3
     return i2;
 }
 
+// What one block contributes to one pixel in a field mode.
+struct ModeOut {
+    enum : uint32_t { kNone, kBlend, kMax, kClear } kind;
+    float4 acc; // kBlend: non-premultiplied colour and alpha gathered front to back in the block
+    float t;    // kMax: (max value - field min) / span
+};
+
+// The per-pixel march of one block in a field mode (renderKernel<mode>,
+// DenseFieldRenderer_cu.cu:62-215 and render*.hpp): max intensity gives the
+// block's maximum above the threshold; the colour modes (Argb, ArgbLight,
+// DomainVoxels) and the isosurface modes the colour gathered with blendBehind;
+// multi-level modes with no level clear the pixel.
 template <bool kTex>
-__global__ void render_block_mode_kernel(const s3r_view v, const s3r_presentation pr, const float* __restrict__ brick,
-                                         const float* __restrict__ brick2, const RenderBlock rb,
-                                         const float4* __restrict__ tf_g, uint32_t* __restrict__ viewport)
+__device__ __forceinline__ ModeOut march_block_mode(const s3r_view& v, const s3r_presentation& pr,
+                                                    const float* __restrict__ brick, const float* __restrict__ brick2,
+                                                    const BlockRay& r, uint32_t depth, const float4* tf)
 {
-    extern __shared__ float4 tf[];
-    for (uint32_t i = threadIdx.y * blockDim.x + threadIdx.x; i < v.tf_n; i += blockDim.x * blockDim.y)
-        tf[i] = tf_g[i];
-    __syncthreads();
-    const int32_t xx = blockIdx.x * blockDim.x + threadIdx.x;
-    const int32_t yy = blockIdx.y * blockDim.y + threadIdx.y;
-    if (xx >= rb.rect[2] || yy >= rb.rect[3]) return;
-    const uint32_t vx = (uint32_t)(rb.rect[0] + xx), vy = (uint32_t)(rb.rect[1] + yy);
-    if (vx >= v.W || vy >= v.H) return;
-    float org[3], dir[3];
-    pixel_ray(v, vx, vy, org, dir);
-    BlockRay r;
-    if (!block_ray(v, org, dir, rb, r)) return;
-    uint32_t* px = &viewport[(size_t)(v.H - 1 - vy) * v.W + vx];
+    ModeOut out{ModeOut::kNone, make_float4(0.f, 0.f, 0.f, 0.f), 0.f};
     const uint32_t n = r.n;
     const float span = v.field_max - v.field_min;
     const F3 eye = f3(v.cam.eye);
@@ -592,17 +591,15 @@ __global__ void render_block_mode_kernel(const s3r_view v, const s3r_presentatio
             const float val = value(brick, pos_of(i - 1));
             if (val >= v.threshold && maxv < val) maxv = val;
         }
-        if (maxv < v.field_min) return;
-        const float t = (maxv - v.field_min) / span;
-        const float prev = __uint_as_float(*px);
-        if (!isnan(prev) && prev > t) return;
-        *px = __float_as_uint(t);
-        return;
+        if (maxv < v.field_min) return out;
+        out.kind = ModeOut::kMax;
+        out.t = (maxv - v.field_min) / span;
+        return out;
     }
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     if (mode == S3R_MODE_ARGB || mode == S3R_MODE_ARGB_LIGHT || mode == S3R_MODE_DOMAIN_VOXELS) {
         const float of = (v.threshold - v.field_min) / span;
-        const float il = layer_exponent(rb.depth, v.level, v.quality);
+        const float il = layer_exponent(depth, v.level, v.quality);
         float4 dom = make_float4(0.f, 0.f, 0.f, 0.f);
         if (mode == S3R_MODE_DOMAIN_VOXELS) {
             // renderDomainVoxels.hpp:41-42: one colour, the table's middle
@@ -628,8 +625,9 @@ __global__ void render_block_mode_kernel(const s3r_view v, const s3r_presentatio
             blend_behind(acc, col);
             if (acc.w > kMax) break;
         }
-        *px = blend_above_argb(*px, acc);
-        return;
+        out.kind = ModeOut::kBlend;
+        out.acc = acc;
+        return out;
     }
     // isosurface modes: v1 at the entry point, v2 at samples 1 .. sampleCount-1; the
     // crossing is placed at pos + step * t from the later sample, as the reference does
@@ -637,8 +635,8 @@ __global__ void render_block_mode_kernel(const s3r_view v, const s3r_presentatio
     const bool secondary = mode == S3R_MODE_VALUE_ON_ISOSURFACE || mode == S3R_MODE_VALUE_ON_ISOSURFACES;
     const uint32_t nl = pr.level_count;
     if (multi && nl < 1) {
-        *px = 0u; // renderIsosurfaces.hpp:36-38
-        return;
+        out.kind = ModeOut::kClear; // renderIsosurfaces.hpp:36-38
+        return out;
     }
     auto surface_colour = [&](float level, F3 xpos) {
         float4 dif;
@@ -715,7 +713,41 @@ __global__ void render_block_mode_kernel(const s3r_view v, const s3r_presentatio
             v1 = v2;
         }
     }
-    *px = blend_above_argb(*px, acc);
+    out.kind = ModeOut::kBlend;
+    out.acc = acc;
+    return out;
+}
+
+template <bool kTex>
+__global__ void render_block_mode_kernel(const s3r_view v, const s3r_presentation pr, const float* __restrict__ brick,
+                                         const float* __restrict__ brick2, const RenderBlock rb,
+                                         const float4* __restrict__ tf_g, uint32_t* __restrict__ viewport)
+{
+    extern __shared__ float4 tf[];
+    for (uint32_t i = threadIdx.y * blockDim.x + threadIdx.x; i < v.tf_n; i += blockDim.x * blockDim.y)
+        tf[i] = tf_g[i];
+    __syncthreads();
+    const int32_t xx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int32_t yy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (xx >= rb.rect[2] || yy >= rb.rect[3]) return;
+    const uint32_t vx = (uint32_t)(rb.rect[0] + xx), vy = (uint32_t)(rb.rect[1] + yy);
+    if (vx >= v.W || vy >= v.H) return;
+    float org[3], dir[3];
+    pixel_ray(v, vx, vy, org, dir);
+    BlockRay r;
+    if (!block_ray(v, org, dir, rb, r)) return;
+    uint32_t* px = &viewport[(size_t)(v.H - 1 - vy) * v.W + vx];
+    const ModeOut o = march_block_mode<kTex>(v, pr, brick, brick2, r, rb.depth, tf);
+    if (o.kind == ModeOut::kMax) {
+        // renderMaxIntensityProjection.hpp:30-50; the pixel holds float bits
+        const float prev = __uint_as_float(*px);
+        if (!isnan(prev) && prev > o.t) return;
+        *px = __float_as_uint(o.t);
+    } else if (o.kind == ModeOut::kBlend) {
+        *px = blend_above_argb(*px, o.acc);
+    } else if (o.kind == ModeOut::kClear) {
+        *px = 0u;
+    }
 }
 
 // ---------------------------------------------------------------- batched form
@@ -1010,6 +1042,87 @@ __global__ void frame_render_kernel(FrameArgs fa)
     }
 }
 
+// Non-premultiplied RGBA and ARGB32 of a composited ray, row-flipped as the reference stores pixels.
+__device__ __forceinline__ void write_pixel(const FrameArgs& fa, const s3r_view& v, uint32_t vx, uint32_t vy,
+                                            const Premul& acc)
+{
+    const size_t o = (size_t)(v.H - 1 - vy) * v.W + vx;
+    float4 out = make_float4(0.f, 0.f, 0.f, acc.a);
+    if (acc.a > 0.f) {
+        const float inv = 1.f / acc.a;
+        out.x = acc.r * inv;
+        out.y = acc.g * inv;
+        out.z = acc.b * inv;
+    }
+    if (fa.rgba) reinterpret_cast<float4*>(fa.rgba)[o] = out;
+    if (fa.argb) fa.argb[o] = rgba_to_argb(out);
+}
+
+// Batched field modes (F32 bricks): one lane per ray walks the blocks front
+// to back, each block marched as render_block_mode_kernel marches it
+// (march_block_mode), and the blocks' contributions are combined in float: the
+// colour modes' block results composited front to back (premultiplied) with
+// no ARGB8 rounding between blocks, max intensity the maximum over the
+// blocks, and a multi-level mode without levels clears the pixel (what lies
+// behind the first block it meets is erased, as the per-block path erases it).
+template <bool kTex>
+__global__ void frame_render_mode_kernel(FrameArgs fa, const s3r_presentation pr, const float* __restrict__ bricks2)
+{
+    extern __shared__ float4 tf[];
+    const s3r_view v = *fa.view;
+    const uint32_t nthreads = blockDim.x * blockDim.y;
+    const uint32_t tid = threadIdx.y * blockDim.x + threadIdx.x;
+    for (uint32_t i = tid; i < v.tf_n; i += nthreads) tf[i] = reinterpret_cast<const float4*>(fa.tf)[i];
+    __syncthreads();
+    const uint32_t vx = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t vy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (vx >= v.W || vy >= v.H) return;
+    const bool mip = pr.mode == S3R_MODE_MAX_INTENSITY;
+    Premul acc{0.f, 0.f, 0.f, 0.f};
+    bool have_max = false;
+    float best = 0.f;
+    const int4 cv = *reinterpret_cast<const int4*>(fa.cover);
+    if ((int32_t)vx >= cv.x && (int32_t)vx < cv.z && (int32_t)vy >= cv.y && (int32_t)vy < cv.w) {
+        float org[3], dir[3];
+        pixel_ray(v, vx, vy, org, dir);
+        const float* bricks = reinterpret_cast<const float*>(fa.bricks);
+        walk_blocks(org, dir, v.level, [&](uint32_t b, uint32_t, uint32_t, uint32_t) {
+            const RenderBlock* rb = &fa.table[b];
+            const uint32_t depth = rb->depth;
+            if (depth == 0xffffffffu) return true;
+            const int4 rc = *reinterpret_cast<const int4*>(rb->rect);
+            const int32_t rca[4] = {rc.x, rc.y, rc.z, rc.w};
+            if (!pixel_in_rect(rca, vx, vy)) return true;
+            BlockRay r;
+            if (!block_ray(v, org, dir, *rb, r)) return true;
+            const ModeOut o = march_block_mode<kTex>(v, pr, bricks + rb->brick_off,
+                                                     bricks2 ? bricks2 + rb->brick_off : nullptr, r, depth, tf);
+            if (o.kind == ModeOut::kMax) {
+                if (!have_max || o.t > best) best = o.t;
+                have_max = true;
+            } else if (o.kind == ModeOut::kBlend) {
+                const float T = __fsub_rn(1.f, acc.a);
+                acc.r = __fmaf_rn(T, __fmul_rn(o.acc.x, o.acc.w), acc.r);
+                acc.g = __fmaf_rn(T, __fmul_rn(o.acc.y, o.acc.w), acc.g);
+                acc.b = __fmaf_rn(T, __fmul_rn(o.acc.z, o.acc.w), acc.b);
+                acc.a = __fmaf_rn(T, o.acc.w, acc.a);
+            } else if (o.kind == ModeOut::kClear) {
+                return false;
+            }
+            return mip || !(acc.a > v.alpha_stop);
+        });
+    }
+    const size_t o = (size_t)(v.H - 1 - vy) * v.W + vx;
+    if (mip) {
+        if (fa.rgba)
+            reinterpret_cast<float4*>(fa.rgba)[o] =
+                have_max ? make_float4(best, best, best, 1.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (fa.argb) fa.argb[o] = have_max ? __float_as_uint(best) : 0x7fc00000u;
+        return;
+    }
+    write_pixel(fa, v, vx, vy, acc);
+}
+
 // ---------------------------------------------------------------- adjoint
 
 // For L = 1/2 sum (I - target)^2 with I = (C/A, A) the premultiplied composite
@@ -1252,6 +1365,17 @@ cudaError_t launch_frame_render(const FrameArgs& a, uint32_t W, uint32_t H, uint
                    : launch_frame_render_fmt<S3R_BRICK_BF16, false>(a, grid, block, smem, R, s);
     default: return cudaErrorInvalidValue;
     }
+}
+
+cudaError_t launch_frame_render_mode(const FrameArgs& a, const s3r_presentation& pres, const float* bricks2,
+                                     uint32_t W, uint32_t H, uint32_t tf_n, uint32_t filter, cudaStream_t s)
+{
+    dim3 block(16, 8);
+    dim3 grid((W + 15) / 16, (H + 7) / 8);
+    const size_t smem = tf_n * sizeof(float4);
+    if (filter == S3R_FILTER_TEXTURE) frame_render_mode_kernel<true><<<grid, block, smem, s>>>(a, pres, bricks2);
+    else frame_render_mode_kernel<false><<<grid, block, smem, s>>>(a, pres, bricks2);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_frame_backward(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, cudaStream_t s)

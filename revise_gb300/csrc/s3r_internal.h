@@ -159,6 +159,8 @@ cudaError_t launch_render_block_argb(const s3r_view* view_host, const float* bri
                                      const float* tf, uint32_t* viewport, cudaStream_t s);
 cudaError_t launch_frame_render(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, uint32_t fmt,
                                 uint32_t tile_shape, uint32_t filter, cudaStream_t s);
+cudaError_t launch_frame_render_mode(const FrameArgs& a, const s3r_presentation& pres, const float* bricks2,
+                                     uint32_t W, uint32_t H, uint32_t tf_n, uint32_t filter, cudaStream_t s);
 cudaError_t launch_frame_backward(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, cudaStream_t s);
 // dtf[i] += sum over the kDtfParts copies of part[. * n + i], n = 4 * tf_n
 cudaError_t launch_dtf_reduce(const float* part, float* dtf, uint32_t n, cudaStream_t s);
