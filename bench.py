@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the adjoint, 16-bit and reference-CUDA measurements")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--adjoint-only", action="store_true",
+                    help="only the adjoint measurement (cfg5), one JSON line; for profiling the backward kernel")
     return ap.parse_args()
 
 
@@ -634,11 +636,10 @@ def measure_modes(ctx, torch, np, with_reference: bool):
     return out
 
 
-def measure_extras(ctx, torch, np):
-    """Adjoint/forward ratio on the 8-block differentiation config and 16-bit-brick frame rates (cfg2)."""
-    from revise_gb300 import _lib, host, workloads
+def measure_adjoint(ctx, torch, np):
+    """Forward render and adjoint (backward) times on the 8-block differentiation config (cfg5)."""
+    from revise_gb300 import host, workloads
     from revise_gb300.api import FramePlan
-    out = {}
     w = workloads.cfg5()
     view = host.view_for(w)
     plan = FramePlan(ctx, w)
@@ -664,9 +665,16 @@ def measure_extras(ctx, torch, np):
 
     fwd = tm(lambda: plan.render(view, tf, rgba))
     bwd = tm(lambda: plan.backward(view, tf, rgba, dl, dtf, dd))
-    out["adjoint"] = {"workload": "cfg5: 2x2x2 blocks depth 6, 512x512", "forward_render_ms": fwd,
-                      "backward_ms": bwd, "adjoint_forward_ratio": bwd / fwd}
     plan.close()
+    return {"workload": "cfg5: 2x2x2 blocks depth 6, 512x512", "forward_render_ms": fwd, "backward_ms": bwd,
+            "adjoint_forward_ratio": bwd / fwd}
+
+
+def measure_extras(ctx, torch, np):
+    """Adjoint/forward ratio on the 8-block differentiation config and 16-bit-brick frame rates (cfg2)."""
+    from revise_gb300 import _lib, host, workloads
+    from revise_gb300.api import FramePlan
+    out = {"adjoint": measure_adjoint(ctx, torch, np)}
     w2 = workloads.cfg2()
     v2 = host.view_for(w2)
     sp2 = torch.from_numpy(w2.sparse).cuda()
@@ -686,6 +694,14 @@ def main():
     a = parse()
     if a.impl == "reference":
         return run_reference(a)
+    if a.adjoint_only:
+        import numpy as np
+        import torch
+        from revise_gb300.api import Context
+        ctx = Context(0)
+        print(json.dumps({"adjoint": measure_adjoint(ctx, torch, np)}))
+        ctx.close()
+        return 0
     return run_gb300(a)
 
 

@@ -1125,13 +1125,49 @@ __global__ void frame_render_mode_kernel(FrameArgs fa, const s3r_presentation pr
 
 // ---------------------------------------------------------------- adjoint
 
+// The 8 texels of a cell (F32 brick, 32-bit offsets), their offsets, and the trilinear value (false on a NaN).
+__device__ __forceinline__ void cell_offsets(const Cell& c, uint32_t n, uint32_t off[8])
+{
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const uint32_t x = (q & 1) ? c.i1[0] : c.i0[0];
+        const uint32_t y = (q & 2) ? c.i1[1] : c.i0[1];
+        const uint32_t z = (q & 4) ? c.i1[2] : c.i0[2];
+        off[q] = (z * n + y) * n + x;
+    }
+}
+
+__device__ __forceinline__ void fetch_cell(const float* brick, const Cell& c, uint32_t n, float t[8])
+{
+    uint32_t off[8];
+    cell_offsets(c, n, off);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) t[q] = __ldg(brick + off[q]);
+}
+
+__device__ __forceinline__ bool filter_cell(const Cell& c, const float t[8], float& val)
+{
+    bool bad = false;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) bad |= isnan(t[q]);
+    if (bad) return false;
+    const float x00 = __fmaf_rn(c.f[0], t[1] - t[0], t[0]);
+    const float x10 = __fmaf_rn(c.f[0], t[3] - t[2], t[2]);
+    const float x01 = __fmaf_rn(c.f[0], t[5] - t[4], t[4]);
+    const float x11 = __fmaf_rn(c.f[0], t[7] - t[6], t[6]);
+    const float y0 = __fmaf_rn(c.f[1], x10 - x00, x00);
+    const float y1 = __fmaf_rn(c.f[1], x11 - x01, x01);
+    val = __fmaf_rn(c.f[2], y1 - y0, y0);
+    return true;
+}
+
 // For L = 1/2 sum (I - target)^2 with I = (C/A, A) the premultiplied composite
 // of the kept samples (front to back, T_k = prod_{j<k} (1 - a_k)):
 //   dC/dc_k = T_k a_k,  dC/da_k = T_k c_k - (C - C_{<=k}) / (1 - a_k),
 //   dA/da_k = (1 - A) / (1 - a_k),
 // a_k = 1 - (1 - alpha_tf * of)^il, c_k / alpha_tf linear in the table
 // entries around v01, v01 linear in the trilinear value.
-__global__ void __launch_bounds__(128, 5) frame_backward_kernel(FrameArgs fa)
+__global__ void __launch_bounds__(128, 4) frame_backward_kernel(FrameArgs fa)
 {
     extern __shared__ float4 sm[];
     const s3r_view v = *fa.view;
@@ -1171,6 +1207,7 @@ __global__ void __launch_bounds__(128, 5) frame_backward_kernel(FrameArgs fa)
             float org[3], dir[3];
             pixel_ray(v, vx, vy, org, dir);
             const float span = v.field_max - v.field_min;
+            const float inv_span = 1.f / span;
             const float of = (v.threshold - v.field_min) / span;
             float T = 1.f, Cpre[3] = {0.f, 0.f, 0.f};
             float accA = 0.f;
@@ -1199,24 +1236,27 @@ __global__ void __launch_bounds__(128, 5) frame_backward_kernel(FrameArgs fa)
                 float* gdense = fa.ddense + rb->brick_off;
                 const float il = layer_exponent(depth, v.level, v.quality);
                 float Ab = 0.f;
-                for (int i = 1; i < r.samples; ++i) {
-                    Cell cell;
-                    sample_cell(r, i - 1, cell);
-                    float t[8], val;
-                    uint64_t off[8];
-                    if (!trilinear<S3R_BRICK_F32>(brick, cell, r.n, val, t, off)) continue;
-                    const float v01 = __fdiv_rn(__fsub_rn(val, v.field_min), span);
+                // one sample's gradients from its cell and texels; false once the block is opaque
+                auto step_sample = [&](const Cell& cell, const float* tcur) -> bool {
+                    float val;
+                    if (!filter_cell(cell, tcur, val)) return true;
+                    uint32_t off[8];
+                    cell_offsets(cell, r.n, off);
+                    const float fx = cell.f[0], fy = cell.f[1], fz = cell.f[2];
+                    // the forward's v01 up to the last ulp (a reciprocal instead of the division)
+                    const float v01 = __fmul_rn(__fsub_rn(val, v.field_min), inv_span);
                     const TfSample ts = tf_lookup(tf, v.tf_n, v01);
                     const float base = __fmaf_rn(-ts.c.w, of, 1.f);
                     const float pw = __powf(base, il);
                     const float a = __fsub_rn(1.f, pw);
-                    const float dadc = base > 0.f ? il * pw / base * of : 0.f;
+                    // derivatives need no correctly rounded divisions: fast reciprocals
+                    const float dadc = base > 0.f ? __fdividef(il * pw, base) * of : 0.f;
                     const float wa = T * a;
                     const float col[3] = {ts.c.x, ts.c.y, ts.c.z};
                     float g_col[4];
                     float g_a = 0.f;
                     const float om = 1.f - a;
-                    const float inv_om = om > 1e-12f ? 1.f / om : 0.f;
+                    const float inv_om = om > 1e-12f ? __fdividef(1.f, om) : 0.f;
 #pragma unroll
                     for (int ch = 0; ch < 3; ++ch) {
                         const float cpost = __fmaf_rn(wa, col[ch], Cpre[ch]);
@@ -1265,9 +1305,8 @@ __global__ void __launch_bounds__(128, 5) frame_backward_kernel(FrameArgs fa)
                         const float g_v01 = (g_col[0] * (q.x - p.x) + g_col[1] * (q.y - p.y) +
                                              g_col[2] * (q.z - p.z) + g_col[3] * (q.w - p.w)) *
                                             (float)v.tf_n;
-                        const float g_val = g_v01 / span;
+                        const float g_val = g_v01 * inv_span;
                         if (g_val != 0.f) {
-                            const float fx = cell.f[0], fy = cell.f[1], fz = cell.f[2];
 #pragma unroll
                             for (int qn = 0; qn < 8; ++qn) {
                                 const float w = ((qn & 1) ? fx : 1.f - fx) * ((qn & 2) ? fy : 1.f - fy) *
@@ -1278,7 +1317,28 @@ __global__ void __launch_bounds__(128, 5) frame_backward_kernel(FrameArgs fa)
                     }
                     T *= om;
                     Ab = __fadd_rn(Ab, __fmul_rn(__fsub_rn(1.f, Ab), a));
-                    if (Ab > kAlphaThreshold) break;
+                    return !(Ab > kAlphaThreshold);
+                };
+                // software-pipelined as the forward march, unrolled by two with two
+                // buffers: sample i's texels load while sample i-1's gradients form
+                Cell ca, cb;
+                float ta[8], tb[8];
+                if (r.samples > 1) {
+                    sample_cell(r, 0, ca);
+                    fetch_cell(brick, ca, r.n, ta);
+                }
+                for (int i = 1; i < r.samples; i += 2) {
+                    if (i + 1 < r.samples) {
+                        sample_cell(r, i, cb);
+                        fetch_cell(brick, cb, r.n, tb);
+                    }
+                    if (!step_sample(ca, ta)) break;
+                    if (i + 1 >= r.samples) break;
+                    if (i + 2 < r.samples) {
+                        sample_cell(r, i + 1, ca);
+                        fetch_cell(brick, ca, r.n, ta);
+                    }
+                    if (!step_sample(cb, tb)) break;
                 }
                 // block composite exactly as the forward kernel forms it
                 accA = __fmaf_rn(__fsub_rn(1.f, accA), Ab, accA);
@@ -1380,8 +1440,8 @@ cudaError_t launch_frame_render_mode(const FrameArgs& a, const s3r_presentation&
 
 cudaError_t launch_frame_backward(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, cudaStream_t s)
 {
-    dim3 block(16, 8);
-    dim3 grid((W + 15) / 16, (H + 7) / 8);
+    dim3 block(32, 4);
+    dim3 grid((W + 31) / 32, (H + 3) / 4);
     const size_t smem = tf_n * sizeof(float4);
     if (smem > 48 * 1024) {
         cudaError_t err =
