@@ -338,6 +338,7 @@ def run_gb300(a):
         extras = measure_extras(ctx, torch, np)
         extras["ingest"] = measure_ingest(ctx, torch, np, w, with_reference=not a.no_cpu)
         extras["modes"] = measure_modes(ctx, torch, np, with_reference=not a.no_cpu)
+        extras["worker_loop"] = measure_worker_loop(ctx, torch, np, w)
 
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
@@ -668,6 +669,52 @@ def measure_adjoint(ctx, torch, np):
     plan.close()
     return {"workload": "cfg5: 2x2x2 blocks depth 6, 512x512", "forward_render_ms": fwd, "backward_ms": bwd,
             "adjoint_forward_ratio": bwd / fwd}
+
+
+def measure_worker_loop(ctx, torch, np, w):
+    """The per-block drop-in path over the whole frame: s3r_render_scene_part (the native
+    VsWorker_cu::renderScenePart) on the full block cube as one index box, texture filter as the
+    reference samples -- per block interpolation from resident nodes and render, back to front --
+    wall time per frame including the bounding-rectangle read back."""
+    import time
+    from revise_gb300 import _lib
+    from revise_gb300.api import RenderSharedState, VsWorker
+    st = RenderSharedState(w, filter=_lib.FILTER_TEXTURE)
+    wk = VsWorker(ctx)
+    wk.set_render_shared_state(st)
+    m = 1 << w.level
+    wk.render_scene_part_native(w.level, (0, 0, 0), (m, m, m))
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(3):
+        t = time.perf_counter()
+        wk.render_scene_part_native(w.level, (0, 0, 0), (m, m, m))
+        torch.cuda.synchronize()
+        ts.append((time.perf_counter() - t) * 1e3)
+    launches0 = ctx.launches
+    wk.render_scene_part_native(w.level, (0, 0, 0), (m, m, m))
+    launches = int(ctx.launches - launches0)
+    # the same loop rendering from the batched plan's bricks: one interpolation launch per frame
+    from revise_gb300.api import FramePlan
+    plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=16)
+    sparse = torch.from_numpy(w.sparse).cuda()
+
+    def planned():
+        plan.interp(sparse)
+        wk.render_scene_part_plan(plan, w.level, (0, 0, 0), (m, m, m))
+
+    planned()
+    torch.cuda.synchronize()
+    tp = []
+    for _ in range(3):
+        t = time.perf_counter()
+        planned()
+        torch.cuda.synchronize()
+        tp.append((time.perf_counter() - t) * 1e3)
+    plan.close()
+    return {"workload": f"{w.name}: {w.nblocks} blocks as one box, {w.W}x{w.H}, Argb, texture filter, nodes resident",
+            "ms_per_frame": statistics.median(ts), "launches_per_frame": launches,
+            "from_plan_bricks_ms_per_frame": statistics.median(tp)}
 
 
 def measure_extras(ctx, torch, np):

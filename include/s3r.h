@@ -32,6 +32,7 @@
  *   s3r_split_b2f              IndexCubeSplitter<3> (include/IndexCubeSplitter.hpp) and
  *                              IndexCubeSplitStorage::getBoxesSorted (src/s3vs_lib/IndexCubeSplitStorage.hpp)
  *   s3r_bound_rect             getBoundRect (src/s3vs_worker/cuda/VsWorker_cu.cpp:51-88)
+ *   s3r_render_scene_part      VsWorker_cu::renderScenePart (src/s3vs_worker/cuda/VsWorker_cu.cpp:225-313)
  *   s3r_blend_image_part_host,
  *   s3r_compose_parts          blendImagePart (src/s3vs_lib/BlendImagePart.hpp:61-145)
  *   s3r_blend_image_part_mip_host  blendImagePartMaxIntensity (src/s3vs_lib/BlendImagePart.hpp:148-191)
@@ -298,6 +299,38 @@ typedef struct s3r_image_part {
  * each exactly as blendImagePart would (parts[0] first; just_copy_first copies it). */
 int s3r_compose_parts(s3r_ctx* ctx, const s3r_image_part* parts, uint32_t nparts, int32_t just_copy_first,
                       uint32_t* dst, int32_t dw, int32_t dh, int32_t offx, int32_t offy, void* stream);
+
+/* ------------------------------------------------------------- worker loop */
+
+/* The blocks of one level a worker renders: per block {ix, iy, iz, depth} and its nodes. */
+typedef struct s3r_worker_blocks {
+    uint32_t nblocks;
+    const uint32_t* blocks;    /* host: nblocks x {ix, iy, iz, depth} */
+    const uint64_t* node_off;  /* host: nblocks+1 prefix offsets into n2i / sparse */
+    const uint16_t* n2i;       /* device: node_off[nblocks] x {x, y, z} */
+    const float* sparse;       /* device: node_off[nblocks] values (S3R_NO_FIELD_VALUE where masked) */
+    const float* sparse2;      /* device, optional: the secondary field on the same nodes */
+} s3r_worker_blocks;
+
+/* VsWorker_cu::renderScenePart (src/s3vs_worker/cuda/VsWorker_cu.cpp:225-313) natively, for the index box
+ * [box_min, box_max) of view->level: the viewport (device, W*H ARGB32) cleared as clearViewport clears it,
+ * the box's blocks visited back to front for the view's eye (BackToFrontOrder over the box, blocks missing
+ * from wb skipped), each block's dense field interpolated from its nodes into the context's scratch
+ * (s3r_interp_dense; the secondary field too for the value-on-isosurface modes) and ray-cast into the
+ * viewport (s3r_render_block, or s3r_render_block_argb when pres is NULL); then rect = the bounding
+ * rectangle of the non-transparent pixels (s3r_bound_rect; {0,0,0,0} when empty) -- the part s3r_crop
+ * cuts out.  Allocates the scratch on the first call for a depth; synchronizes the stream at the end. */
+int s3r_render_scene_part(s3r_ctx* ctx, const s3r_view* view, const s3r_presentation* pres,
+                          const s3r_worker_blocks* wb, const uint32_t box_min[3], const uint32_t box_max[3],
+                          const float* tf, uint32_t* viewport, int32_t rect[4], void* stream);
+
+/* s3r_render_scene_part with the blocks' dense fields taken from a plan's brick store (F32; interpolated
+ * for all of the plan's blocks at once by s3r_frame_interp) instead of interpolated block by block:
+ * per block of the box (back to front) only the render launch.  bricks2: the secondary field's brick
+ * store in the plan's layout (value-on-isosurface modes). */
+int s3r_render_scene_part_bricks(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const s3r_presentation* pres,
+                                 const void* bricks2, const uint32_t box_min[3], const uint32_t box_max[3],
+                                 const float* tf, uint32_t* viewport, int32_t rect[4], void* stream);
 
 /* ------------------------------------------------ transfer-function table */
 

@@ -79,6 +79,11 @@ class ImagePart(C.Structure):
     _fields_ = [("pixels", vp), ("origin", C.c_int32 * 2), ("size", C.c_int32 * 2)]
 
 
+class WorkerBlocks(C.Structure):
+    _fields_ = [("nblocks", C.c_uint32), ("blocks", u32p), ("node_off", u64p), ("n2i", vp), ("sparse", vp),
+                ("sparse2", vp)]
+
+
 class DatasetInfo(C.Structure):
     _fields_ = [("format_version", C.c_uint32), ("time_steps", C.c_uint32), ("field_count", C.c_uint32),
                 ("max_subtree_depth", C.c_uint32), ("max_full_level", C.c_uint32), ("level_count", C.c_uint32),
@@ -122,6 +127,10 @@ _SIGS = {
                                             C.c_int32, C.c_int32, C.c_int32, C.c_int32]),
     "s3r_compose_parts": (C.c_int, [vp, C.POINTER(ImagePart), C.c_uint32, C.c_int32, vp, C.c_int32, C.c_int32,
                                     C.c_int32, C.c_int32, vp]),
+    "s3r_render_scene_part": (C.c_int, [vp, C.POINTER(View), C.POINTER(Presentation), C.POINTER(WorkerBlocks), u32p,
+                                        u32p, vp, vp, i32p, vp]),
+    "s3r_render_scene_part_bricks": (C.c_int, [vp, vp, C.POINTER(View), C.POINTER(Presentation), vp, u32p, u32p,
+                                               vp, vp, i32p, vp]),
     "s3r_make_color_transfer": (C.c_int, [f64p, f64p, C.c_uint32, C.c_uint32, f32p]),
     "s3r_frame_plan": (C.c_int, [vp, C.POINTER(FrameDesc), C.POINTER(vp)]),
     "s3r_plan_destroy": (C.c_int, [vp]),

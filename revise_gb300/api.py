@@ -17,7 +17,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib, host
-from ._lib import FrameDesc, ImagePart, PlanInfo, View, arr, check, ptr
+from ._lib import FrameDesc, ImagePart, PlanInfo, View, WorkerBlocks, arr, check, ptr
 
 
 def _torch():
@@ -286,6 +286,17 @@ class RenderSharedState:
         self.block_index = {(int(b[0]), int(b[1]), int(b[2])): i for i, b in enumerate(workload.blocks)}
         self._dev = {}
 
+    def device_all(self):
+        """All blocks' nodes and values as single device arrays (n2i as int16 bits, values float32),
+        with the host block table and node offsets: the s3r_worker_blocks of s3r_render_scene_part."""
+        if "all" not in self._dev:
+            torch = _torch()
+            w = self.w
+            self._dev["all"] = (np.ascontiguousarray(w.blocks, dtype=np.uint32),
+                                np.ascontiguousarray(w.node_off, dtype=np.uint64), to_device_n2i(w.n2i),
+                                torch.from_numpy(np.ascontiguousarray(w.sparse, dtype=np.float32)).cuda())
+        return self._dev["all"]
+
     def device_nodes(self, b: int):
         if b not in self._dev:
             torch = _torch()
@@ -300,6 +311,7 @@ class VsWorker:
 
     def __init__(self, ctx: Context):
         self.ctx = ctx
+        self.lib = ctx.lib
         self.renderer = DenseFieldRenderer(ctx)
         self.state = None
         self.viewport = None
@@ -323,6 +335,61 @@ class VsWorker:
             return ImagePartResult((0, 0), (0, 0), np.zeros((0, 0), dtype=np.uint32))
         pix = pixels.cpu().numpy().view(np.uint32).reshape(size[1], size[0])
         return ImagePartResult(origin, size, pix)
+
+    def render_scene_part_native(self, level: int, index_box_min, index_box_max, pres=None, sparse2_dev=None):
+        """renderScenePart as one native call (s3r_render_scene_part): clear, back-to-front block loop
+        (interpolate + render per block), bounding rectangle; the cropped part stays in device memory:
+        (origin, size, int32 tensor), size (0, 0) when nothing was drawn."""
+        torch = _torch()
+        s = self.state
+        W, H = s.view.W, s.view.H
+        if self.viewport is None or self.viewport.numel() != W * H:
+            self.viewport = torch.empty(W * H, dtype=torch.int32, device="cuda")
+        blocks, node_off, n2i_dev, sparse_dev = s.device_all()
+        wb = WorkerBlocks()
+        wb.nblocks = blocks.shape[0]
+        wb.blocks = arr(blocks, C.c_uint32)
+        wb.node_off = arr(node_off, C.c_uint64)
+        wb.n2i = ptr(n2i_dev)
+        wb.sparse = ptr(sparse_dev)
+        wb.sparse2 = ptr(sparse2_dev)
+        bmin = (C.c_uint32 * 3)(*[int(x) for x in index_box_min])
+        bmax = (C.c_uint32 * 3)(*[int(x) for x in index_box_max])
+        rect = (C.c_int32 * 4)()
+        if self.renderer._tf is None:
+            self.renderer._tf = torch.from_numpy(np.ascontiguousarray(s.tf, dtype=np.float32)).cuda()
+        self.ctx._check(self.lib.s3r_render_scene_part(self.ctx.h, C.byref(s.view),
+                                                       C.byref(pres) if pres is not None else None, C.byref(wb),
+                                                       bmin, bmax, ptr(self.renderer._tf), ptr(self.viewport), rect,
+                                                       None))
+        if rect[2] == 0:
+            return (0, 0), (0, 0), torch.zeros(1, dtype=torch.int32, device="cuda")
+        crop = torch.empty(rect[2] * rect[3], dtype=torch.int32, device="cuda")
+        self.ctx.crop(self.viewport, W, list(rect), crop)
+        return (int(rect[0]), int(rect[1])), (int(rect[2]), int(rect[3])), crop
+
+    def render_scene_part_plan(self, plan, level: int, index_box_min, index_box_max, pres=None, bricks2=None):
+        """renderScenePart from a FramePlan's brick store (interpolated with plan.interp for all blocks):
+        one render launch per block of the box, back to front; the cropped part in device memory."""
+        torch = _torch()
+        s = self.state
+        W, H = s.view.W, s.view.H
+        if self.viewport is None or self.viewport.numel() != W * H:
+            self.viewport = torch.empty(W * H, dtype=torch.int32, device="cuda")
+        if self.renderer._tf is None:
+            self.renderer._tf = torch.from_numpy(np.ascontiguousarray(s.tf, dtype=np.float32)).cuda()
+        bmin = (C.c_uint32 * 3)(*[int(x) for x in index_box_min])
+        bmax = (C.c_uint32 * 3)(*[int(x) for x in index_box_max])
+        rect = (C.c_int32 * 4)()
+        self.ctx._check(self.lib.s3r_render_scene_part_bricks(self.ctx.h, plan.h, C.byref(s.view),
+                                                              C.byref(pres) if pres is not None else None,
+                                                              ptr(bricks2), bmin, bmax, ptr(self.renderer._tf),
+                                                              ptr(self.viewport), rect, None))
+        if rect[2] == 0:
+            return (0, 0), (0, 0), torch.zeros(1, dtype=torch.int32, device="cuda")
+        crop = torch.empty(rect[2] * rect[3], dtype=torch.int32, device="cuda")
+        self.ctx.crop(self.viewport, W, list(rect), crop)
+        return (int(rect[0]), int(rect[1])), (int(rect[2]), int(rect[3])), crop
 
     def render_scene_part_device(self, level: int, index_box_min, index_box_max, cancelled=lambda: False):
         """renderScenePart with the cropped part left in device memory: (origin, size, int32 tensor),

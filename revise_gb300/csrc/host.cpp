@@ -14,6 +14,7 @@
 #include <new>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 using namespace s3r;
@@ -34,6 +35,8 @@ struct s3r_ctx {
     s3r_image_part* parts_dev = nullptr;
     size_t parts_cap = 0;
     cudaStream_t capture = nullptr;
+    float* worker_dense[2] = {nullptr, nullptr}; // s3r_render_scene_part: primary / secondary dense field
+    size_t worker_cap[2] = {0, 0};
     uint64_t launches = 0;
     int sms = 152;
 };
@@ -737,6 +740,8 @@ int s3r_ctx_destroy(s3r_ctx* ctx)
     if (ctx->rect_host) cudaFreeHost(ctx->rect_host);
     if (ctx->parts_dev) cudaFree(ctx->parts_dev);
     if (ctx->capture) cudaStreamDestroy(ctx->capture);
+    for (float* d : ctx->worker_dense)
+        if (d) cudaFree(d);
     delete ctx;
     return S3R_OK;
 }
@@ -1484,6 +1489,135 @@ int s3r_render_argb_backward(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view,
     S3R_CUDA(ctx, launch_dtf_reduce(plan->dtf_part, dtf, 4 * view->tf_n, s));
     ctx->launches += 2;
     return S3R_OK;
+}
+
+} // extern "C"
+
+extern "C" {
+
+int s3r_render_scene_part(s3r_ctx* ctx, const s3r_view* view, const s3r_presentation* pres,
+                          const s3r_worker_blocks* wb, const uint32_t box_min[3], const uint32_t box_max[3],
+                          const float* tf, uint32_t* viewport, int32_t rect[4], void* stream)
+{
+    if (!ctx) return fail(nullptr, S3R_ERR_INVALID, "ctx is null");
+    int rc = check_view(ctx, view);
+    if (rc) return rc;
+    if (!wb || !box_min || !box_max || !tf || !viewport || !rect) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (wb->nblocks && (!wb->blocks || !wb->node_off || !wb->n2i || !wb->sparse))
+        return fail(ctx, S3R_ERR_INVALID, "null block data");
+    const bool secondary = pres && (pres->mode == S3R_MODE_VALUE_ON_ISOSURFACE ||
+                                    pres->mode == S3R_MODE_VALUE_ON_ISOSURFACES);
+    if (secondary && !wb->sparse2) return fail(ctx, S3R_ERR_INVALID, "this mode needs the secondary field");
+    if ((rc = set_device(ctx))) return rc;
+    const cudaStream_t s = as_stream(stream);
+    const uint32_t clear = pres && pres->mode == S3R_MODE_MAX_INTENSITY ? 0x7fc00000u : 0u;
+    if ((rc = s3r_clear_viewport(ctx, viewport, view->W, view->H, clear, stream))) return rc;
+    // the box's blocks back to front (MacroBlock over the box, the view's eye)
+    double cmin[3], cmax[3];
+    if ((rc = s3r_index_box_world(view->level, box_min, box_max, cmin, cmax))) return rc;
+    Split sp[3];
+    for (int a = 0; a < 3; ++a)
+        sp[a] = split_range(box_min[a], box_max[a], (float)cmin[a], (float)cmax[a], view->cam.eye[a]);
+    std::unordered_map<uint64_t, uint32_t> where;
+    where.reserve(wb->nblocks * 2 + 1);
+    for (uint32_t b = 0; b < wb->nblocks; ++b) {
+        const uint32_t* bl = wb->blocks + 4 * b;
+        where[(uint64_t)bl[0] | ((uint64_t)bl[1] << 21) | ((uint64_t)bl[2] << 42)] = b;
+    }
+    b2f_traverse(sp, [&](const uint32_t q[3]) {
+        if (rc) return;
+        auto it = where.find((uint64_t)q[0] | ((uint64_t)q[1] << 21) | ((uint64_t)q[2] << 42));
+        if (it == where.end()) return; // not a block of this set
+        const uint32_t b = it->second;
+        const uint32_t depth = wb->blocks[4 * b + 3];
+        if (depth > S3R_MAX_DEPTH) {
+            rc = fail(ctx, S3R_ERR_INVALID, "depth exceeds S3R_MAX_DEPTH");
+            return;
+        }
+        const uint64_t e = (1ull << depth) + 1, count = e * e * e;
+        for (int f = 0; f < (secondary ? 2 : 1); ++f)
+            if (ctx->worker_cap[f] < count) {
+                if (ctx->worker_dense[f]) cudaFree(ctx->worker_dense[f]);
+                ctx->worker_dense[f] = nullptr;
+                ctx->worker_cap[f] = 0;
+                const cudaError_t err = cudaMalloc(&ctx->worker_dense[f], count * sizeof(float));
+                if (err != cudaSuccess) {
+                    rc = cuda_fail(ctx, err, "cudaMalloc(worker dense field)");
+                    return;
+                }
+                ctx->worker_cap[f] = count;
+            }
+        const uint64_t o = wb->node_off[b], n = wb->node_off[b + 1] - o;
+        // DeviceField::makeField: the block's dense field from its nodes
+        if ((rc = s3r_interp_dense(ctx, wb->n2i + 3 * o, wb->sparse + o, (uint32_t)n, depth, ctx->worker_dense[0],
+                                   stream)))
+            return;
+        if (secondary && (rc = s3r_interp_dense(ctx, wb->n2i + 3 * o, wb->sparse2 + o, (uint32_t)n, depth,
+                                                ctx->worker_dense[1], stream)))
+            return;
+        int32_t r[4];
+        view_rect(*view, wb->blocks + 4 * b, r);
+        if (r[2] <= 0 || r[3] <= 0) return;
+        rc = pres ? s3r_render_block(ctx, view, pres, ctx->worker_dense[0], secondary ? ctx->worker_dense[1] : nullptr,
+                                     depth, wb->blocks + 4 * b, r, tf, viewport, stream)
+                  : s3r_render_block_argb(ctx, view, ctx->worker_dense[0], depth, wb->blocks + 4 * b, r, tf, viewport,
+                                          stream);
+    });
+    if (rc) return rc;
+    (void)s;
+    return s3r_bound_rect(ctx, viewport, view->W, view->H, rect, stream);
+}
+
+} // extern "C"
+
+extern "C" {
+
+int s3r_render_scene_part_bricks(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const s3r_presentation* pres,
+                                 const void* bricks2, const uint32_t box_min[3], const uint32_t box_max[3],
+                                 const float* tf, uint32_t* viewport, int32_t rect[4], void* stream)
+{
+    if (!ctx || !plan) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (plan->ctx != ctx) return fail(ctx, S3R_ERR_INVALID, "plan belongs to another context");
+    int rc = check_view(ctx, view);
+    if (rc) return rc;
+    if (view->level != plan->level) return fail(ctx, S3R_ERR_INVALID, "view level differs from the plan level");
+    if (!box_min || !box_max || !tf || !viewport || !rect) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (plan->fmt != S3R_BRICK_F32) return fail(ctx, S3R_ERR_UNSUPPORTED, "the per-block renderer reads F32 bricks");
+    const bool secondary = pres && (pres->mode == S3R_MODE_VALUE_ON_ISOSURFACE ||
+                                    pres->mode == S3R_MODE_VALUE_ON_ISOSURFACES);
+    if (secondary && !bricks2) return fail(ctx, S3R_ERR_INVALID, "this mode needs the secondary bricks");
+    if ((rc = set_device(ctx))) return rc;
+    const uint32_t clear = pres && pres->mode == S3R_MODE_MAX_INTENSITY ? 0x7fc00000u : 0u;
+    if ((rc = s3r_clear_viewport(ctx, viewport, view->W, view->H, clear, stream))) return rc;
+    double cmin[3], cmax[3];
+    if ((rc = s3r_index_box_world(view->level, box_min, box_max, cmin, cmax))) return rc;
+    Split sp[3];
+    for (int a = 0; a < 3; ++a)
+        sp[a] = split_range(box_min[a], box_max[a], (float)cmin[a], (float)cmax[a], view->cam.eye[a]);
+    const uint32_t m = 1u << plan->level;
+    std::vector<int32_t> where((size_t)m * m * m, -1);
+    for (uint32_t b = 0; b < plan->nblocks; ++b) {
+        const uint32_t* bl = &plan->blocks[4 * b];
+        where[bl[0] + m * (bl[1] + (size_t)m * bl[2])] = (int32_t)b;
+    }
+    const float* bricks = static_cast<const float*>(plan->bricks);
+    const float* b2 = static_cast<const float*>(bricks2);
+    b2f_traverse(sp, [&](const uint32_t q[3]) {
+        if (rc) return;
+        if (q[0] >= m || q[1] >= m || q[2] >= m) return;
+        const int32_t b = where[q[0] + m * (q[1] + (size_t)m * q[2])];
+        if (b < 0) return;
+        const uint32_t* bl = &plan->blocks[4 * b];
+        int32_t r[4];
+        view_rect(*view, bl, r);
+        if (r[2] <= 0 || r[3] <= 0) return;
+        const uint64_t o = plan->vertex_off[b];
+        rc = pres ? s3r_render_block(ctx, view, pres, bricks + o, secondary ? b2 + o : nullptr, bl[3], bl, r, tf,
+                                     viewport, stream)
+                  : s3r_render_block_argb(ctx, view, bricks + o, bl[3], bl, r, tf, viewport, stream);
+    });
+    if (rc) return rc;
+    return s3r_bound_rect(ctx, viewport, view->W, view->H, rect, stream);
 }
 
 } // extern "C"

@@ -1,0 +1,101 @@
+"""The native worker loop (s3r_render_scene_part) against the Python worker loop over the same
+per-block calls (bit for bit), in the Argb and the field modes, for whole and partial boxes."""
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from revise_gb300 import _lib, host, workloads
+
+sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+import mode_scenes as ms  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _img(part, W, H):
+    (ox, oy), (w, h), px = part
+    out = np.zeros((H, W), np.uint32)
+    if w:
+        out[oy:oy + h, ox:ox + w] = px.cpu().numpy().view(np.uint32).reshape(h, w)
+    return out
+
+
+@pytest.mark.parametrize("box", [((0, 0, 0), (2, 2, 2)), ((0, 1, 0), (2, 2, 1)), ((1, 0, 1), (2, 2, 2))])
+@pytest.mark.parametrize("filt", [_lib.FILTER_EXACT, _lib.FILTER_TEXTURE])
+def test_native_argb_equals_python_loop(ctx, box, filt):
+    from revise_gb300.api import RenderSharedState, VsWorker
+    w = workloads.small(seed=6, level=1, depths=(2, 3, 4), W=96, H=72)
+    st = RenderSharedState(w, filter=filt)
+    wk = VsWorker(ctx)
+    wk.set_render_shared_state(st)
+    a = wk.render_scene_part_device(1, *box)
+    b = wk.render_scene_part_native(1, *box)
+    assert a[0] == b[0] and a[1] == b[1]
+    assert np.array_equal(_img(a, w.W, w.H), _img(b, w.W, w.H))
+    if box[1] == (2, 2, 2) and box[0] == (0, 0, 0):
+        assert a[1][0] > 0
+
+
+@pytest.mark.parametrize("name", list(ms.MODES))
+def test_native_modes_equal_per_block_calls(ctx, name):
+    import torch
+    from revise_gb300.api import RenderSharedState, VsWorker
+    w, view, pres, sparse2 = ms.scene(name, _lib.FILTER_TEXTURE)
+    st = RenderSharedState(w, filter=_lib.FILTER_TEXTURE)
+    st.view = view
+    wk = VsWorker(ctx)
+    wk.set_render_shared_state(st)
+    s2 = torch.from_numpy(np.ascontiguousarray(sparse2)).cuda() if sparse2 is not None else None
+    m = 1 << w.level
+    got = wk.render_scene_part_native(w.level, (0, 0, 0), (m, m, m), pres=pres, sparse2_dev=s2)
+    # the same calls one by one from Python
+    from revise_gb300.api import to_device_n2i
+    clear = ms.clear_value(pres)
+    vp = torch.full((w.W * w.H,), clear, dtype=torch.int64, device="cuda").to(torch.int32)
+    tf = torch.from_numpy(w.tf).cuda()
+    order = host.b2f_order([0, 0, 0], [m, m, m], *host.index_box_world(w.level, [0, 0, 0], [m, m, m]), view.cam.eye[:])
+    where = {tuple(b[:3]): i for i, b in enumerate(w.blocks.tolist())}
+    for idx in order.tolist():
+        b = where[tuple(idx)]
+        n2i, sp = w.block_nodes(b)
+        d = int(w.blocks[b, 3])
+        dn = to_device_n2i(n2i)
+        dense = ctx.interp_dense(dn, torch.from_numpy(sp).cuda(), d)
+        dense2 = None
+        if sparse2 is not None:
+            a0, a1 = int(w.node_off[b]), int(w.node_off[b + 1])
+            dense2 = ctx.interp_dense(dn, torch.from_numpy(np.ascontiguousarray(sparse2[a0:a1])).cuda(), d)
+        r = host.block_view_rect(view, idx)
+        if r[2] > 0 and r[3] > 0:
+            ctx.render_block(view, pres, dense, d, idx, r, tf, vp, brick2=dense2)
+    torch.cuda.synchronize()
+    want = vp.cpu().numpy().view(np.uint32).reshape(w.H, w.W)
+    gimg = _img(got, w.W, w.H)
+    if pres.mode == _lib.MODE_MAX_INTENSITY:
+        # the native part is cropped to non-transparent pixels (alpha byte != 0), as getBoundRect crops
+        (ox, oy), (ww, hh), _ = got
+        assert np.array_equal(gimg[oy:oy + hh, ox:ox + ww], want[oy:oy + hh, ox:ox + ww])
+    else:
+        assert np.array_equal(gimg, want)
+
+
+@pytest.mark.parametrize("filt", [_lib.FILTER_EXACT, _lib.FILTER_TEXTURE])
+def test_scene_part_from_plan_bricks_equals_native_loop(ctx, filt):
+    """Rendering from the plan's bricks (interpolated in one launch) gives the native per-block
+    loop's image: the bricks are bit-identical to the per-block interpolation."""
+    import torch
+    from revise_gb300.api import FramePlan, RenderSharedState, VsWorker
+    w = workloads.small(seed=8, level=1, depths=(2, 3, 5), W=96, H=72)
+    st = RenderSharedState(w, filter=filt)
+    wk = VsWorker(ctx)
+    wk.set_render_shared_state(st)
+    plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=8)
+    plan.interp(torch.from_numpy(w.sparse).cuda())
+    for box in [((0, 0, 0), (2, 2, 2)), ((1, 0, 0), (2, 2, 2))]:
+        a = wk.render_scene_part_native(1, *box)
+        b = wk.render_scene_part_plan(plan, 1, *box)
+        assert a[0] == b[0] and a[1] == b[1]
+        assert np.array_equal(_img(a, w.W, w.H), _img(b, w.W, w.H))
+    plan.close()
