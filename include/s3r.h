@@ -58,7 +58,7 @@
 extern "C" {
 #endif
 
-#define S3R_ABI_VERSION 4
+#define S3R_ABI_VERSION 5
 
 /* status codes */
 #define S3R_OK 0
@@ -361,7 +361,7 @@ typedef struct s3r_frame_desc {
 typedef struct s3r_plan_info {
     uint64_t nodes;          /* sparse nodes over all blocks */
     uint64_t vertices;       /* dense vertices over all blocks */
-    uint64_t brick_bytes;    /* bytes of the brick store */
+    uint64_t brick_bytes;    /* bytes of the brick store (rows padded to the brick pitch) */
     uint64_t tiles;          /* interpolation work items */
     uint64_t tile_entries;   /* binned node entries (nodes on tile boundaries repeat) */
     uint32_t tile_cells;
@@ -375,8 +375,13 @@ typedef struct s3r_plan_info {
 int s3r_frame_plan(s3r_ctx* ctx, const s3r_frame_desc* desc, s3r_plan** out);
 int s3r_plan_destroy(s3r_plan* plan);
 int s3r_plan_info_get(const s3r_plan* plan, s3r_plan_info* out);
-/* Device pointer to the brick store and, per block, its vertex offset (host, nblocks+1 entries). */
+/* Device pointer to the brick store and, per block, the offset of its first element (host, nblocks+1
+ * entries).  Block b's vertex (x, y, z) is element vertex_off[b] + (z (2^d+1) + y) pitch[b] + x, with the
+ * row pitch from s3r_plan_brick_pitches: 2^d+1 rounded up to whole 32-byte sectors (elements between
+ * 2^d+1 and the pitch are never written nor read). */
 int s3r_plan_bricks(const s3r_plan* plan, void** bricks, const uint64_t** vertex_off);
+/* Per block: the brick row pitch in elements (host, nblocks entries). */
+int s3r_plan_brick_pitches(const s3r_plan* plan, const uint32_t** pitch);
 /* Per-brick {scale, offset} pairs (device, 2 floats per block; F16/BF16 only, else NULL). */
 int s3r_plan_brick_scales(const s3r_plan* plan, const float** scale_offset);
 
@@ -422,7 +427,8 @@ int s3r_frame_run(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const floa
 /* Adjoint of s3r_frame_render (F32 bricks) for L = 1/2 sum (I - target)^2:
  * given the forward image rgba (device) and dl_drgba = I - target (device,
  * W*H*4), accumulates dL/dtf (device, tf_n*4 floats) and dL/ddense (device,
- * one float per brick vertex).  Sample positions are recomputed per ray.
+ * one float per brick-store element, in the store's layout; padding elements
+ * stay untouched).  Sample positions are recomputed per ray.
  * view->filter must be S3R_FILTER_EXACT (else S3R_ERR_UNSUPPORTED).
  * Allocates its scratch (512 copies of the table gradient) on the first call. */
 int s3r_render_argb_backward(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* tf,

@@ -22,7 +22,7 @@ MAX_DEPTH = 9
 
 BRICK_F32, BRICK_F16, BRICK_BF16 = 0, 1, 2
 FILTER_EXACT, FILTER_TEXTURE = 0, 1
-ABI_VERSION = 4
+ABI_VERSION = 5
 
 u8p = C.POINTER(C.c_uint8)
 u16p = C.POINTER(C.c_uint16)
@@ -136,6 +136,7 @@ _SIGS = {
     "s3r_plan_destroy": (C.c_int, [vp]),
     "s3r_plan_info_get": (C.c_int, [vp, C.POINTER(PlanInfo)]),
     "s3r_plan_bricks": (C.c_int, [vp, C.POINTER(vp), C.POINTER(u64p)]),
+    "s3r_plan_brick_pitches": (C.c_int, [vp, C.POINTER(u32p)]),
     "s3r_plan_brick_scales": (C.c_int, [vp, C.POINTER(vp)]),
     "s3r_plan_autotune": (C.c_int, [vp, vp, C.POINTER(View), vp, vp, C.c_uint32, vp]),
     "s3r_frame_interp": (C.c_int, [vp, vp, vp, vp]),

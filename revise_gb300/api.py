@@ -202,6 +202,40 @@ class FramePlan:
         dt = "f4" if self.fmt == _lib.BRICK_F32 else ("f2" if self.fmt == _lib.BRICK_F16 else "u2")
         return device_array(p.value, (int(offs[-1]),), dt, self), offs
 
+    def pitches(self) -> np.ndarray:
+        """Per block: the brick row pitch in elements (rows padded to whole 32-byte sectors)."""
+        p = _lib.u32p()
+        check(self.lib.s3r_plan_brick_pitches(self.h, C.byref(p)))
+        return np.ctypeslib.as_array(p, shape=(self.blocks.shape[0],)).copy()
+
+    def block_dense(self, b: int, store=None):
+        """Block b's (2^d+1)^3 vertices (x fastest) from the brick store, or from a tensor in the store's
+        layout such as the adjoint's dL/ddense."""
+        if store is None:
+            store, offs = self.bricks()
+        else:
+            offs = self.bricks()[1]
+        e = (1 << int(self.blocks[b, 3])) + 1
+        pitch = int(self.pitches()[b])
+        a = int(offs[b])
+        return store[a:a + e * e * pitch].view(e, e, pitch)[:, :, :e].reshape(-1)
+
+    def dense(self, store=None):
+        """The brick store (or a tensor in its layout) without the row padding: every block's (2^d+1)^3
+        vertices, blocks in order -- the concatenation the single-block interpolator produces."""
+        torch = _torch()
+        if store is None:
+            store, offs = self.bricks()
+        else:
+            offs = self.bricks()[1]
+        pit = self.pitches()
+        parts = []
+        for b in range(self.blocks.shape[0]):
+            e = (1 << int(self.blocks[b, 3])) + 1
+            a = int(offs[b])
+            parts.append(store[a:a + e * e * int(pit[b])].view(e, e, int(pit[b]))[:, :, :e].reshape(-1))
+        return torch.cat(parts)
+
     def brick_scales(self):
         p = C.c_void_p()
         check(self.lib.s3r_plan_brick_scales(self.h, C.byref(p)))

@@ -52,12 +52,16 @@ struct s3r_plan {
     std::vector<uint16_t> n2i;         // host copy (re-binning by the autotuner)
     std::vector<uint64_t> vertex_off;  // nblocks+1
     uint64_t vertices = 0, nodes = 0, tiles = 0, entries = 0;
+    uint64_t brick_elems = 0;          // elements of the brick store (rows padded to the pitch)
+    std::vector<uint32_t> pitch;       // per block: brick row pitch in elements
     // device
     PlanBlock* blocks_dev = nullptr;
     uint2* items_dev = nullptr;
     uint64_t* entry_off_dev = nullptr;
     uint16_t* entry_local_dev = nullptr;
     uint32_t* entry_node_dev = nullptr;
+    uint32_t* flags_dev = nullptr;
+    uint32_t flag_words = 1;
     uint32_t* queue_dev = nullptr;
     uint64_t* node_off_dev = nullptr;
     float2* scale_offset_dev = nullptr;
@@ -412,11 +416,13 @@ void plan_free_device(s3r_plan* p)
     f(p->entry_off_dev);
     f(p->entry_local_dev);
     f(p->entry_node_dev);
+    f(p->flags_dev);
     p->blocks_dev = nullptr;
     p->items_dev = nullptr;
     p->entry_off_dev = nullptr;
     p->entry_local_dev = nullptr;
     p->entry_node_dev = nullptr;
+    p->flags_dev = nullptr;
 }
 
 void plan_drop_graph(s3r_plan* p)
@@ -457,6 +463,7 @@ int plan_bin(s3r_plan* p, uint32_t tile_log2)
         pb[b].coarse_log2 = L;
         pb[b].node_base = p->node_off[b];
         pb[b].dense_off = p->vertex_off[b];
+        pb[b].pitch = p->pitch[b];
         const uint64_t m = 1ull << L;
         tiles_off[b + 1] = tiles_off[b] + m * m * m;
         coarse_off[b + 1] = coarse_off[b] + (m + 1) * (m + 1) * (m + 1);
@@ -554,6 +561,32 @@ int plan_bin(s3r_plan* p, uint32_t tile_log2)
     const uint64_t nentries = entry_off[ntiles];
     std::vector<uint16_t> local(nentries);
     std::vector<uint32_t> node(nentries);
+    // per item: one bit per finest 2x2x2 cube of the tile, set when one of the cube's midpoints holds
+    // a node (the cube along each odd axis of the node, both neighbours along each even one)
+    const uint32_t hmax = std::max(1u, (1u << tile_log2) / 2);
+    const uint32_t fwords = std::max(1u, (hmax * hmax * hmax + 31) / 32);
+    std::vector<uint32_t> flags(ntiles * fwords, 0u);
+    auto flag_node = [&](uint32_t* f, uint32_t H, uint32_t x, uint32_t y, uint32_t z) {
+        if (!((x | y | z) & 1)) return;
+        auto span = [H](uint32_t v, uint32_t& lo, uint32_t& hi) {
+            if (v & 1) {
+                lo = hi = v >> 1;
+            } else {
+                lo = v ? (v >> 1) - 1 : 0;
+                hi = std::min(v >> 1, H - 1);
+            }
+        };
+        uint32_t x0, x1, y0, y1, z0, z1;
+        span(x, x0, x1);
+        span(y, y0, y1);
+        span(z, z0, z1);
+        for (uint32_t k = z0; k <= z1; ++k)
+            for (uint32_t j = y0; j <= y1; ++j)
+                for (uint32_t i = x0; i <= x1; ++i) {
+                    const uint32_t c = i + H * (j + H * k);
+                    f[c >> 5] |= 1u << (c & 31);
+                }
+    };
     std::vector<uint64_t> cursor(ntiles);
     for (uint64_t t = 0; t < ntiles; ++t) cursor[t] = entry_off[slot[t]];
     // pass 2: fill (tiles of one block are only touched by that block's thread)
@@ -575,6 +608,8 @@ int plan_bin(s3r_plan* p, uint32_t tile_log2)
                         const uint64_t e = cursor[t]++;
                         local[e] = (uint16_t)tile_offset(T, x - tx * T, y - ty * T, z - tz * T);
                         node[e] = (uint32_t)(i - p->node_off[b]);
+                        if (T >= 2)
+                            flag_node(&flags[slot[t] * fwords], T / 2, x - tx * T, y - ty * T, z - tz * T);
                     }
         }
         const uint32_t E3 = E * E * E;
@@ -591,6 +626,8 @@ int plan_bin(s3r_plan* p, uint32_t tile_log2)
     if ((rc = upload(ctx, &p->entry_off_dev, entry_off))) return rc;
     if ((rc = upload(ctx, &p->entry_local_dev, local))) return rc;
     if ((rc = upload(ctx, &p->entry_node_dev, node))) return rc;
+    if ((rc = upload(ctx, &p->flags_dev, flags))) return rc;
+    p->flag_words = fwords;
     p->tile_log2 = tile_log2;
     p->tiles = ntiles;
     p->entries = nentries;
@@ -651,6 +688,8 @@ int plan_launch_interp(s3r_plan* p, const float* sparse, cudaStream_t s, uint32_
     a.entry_off = p->entry_off_dev;
     a.entry_local = p->entry_local_dev;
     a.entry_node = p->entry_node_dev;
+    a.flags = p->flags_dev;
+    a.flag_words = p->flag_words;
     a.sparse = sparse;
     a.queue = p->queue_dev;
     a.scale_offset = p->fmt == S3R_BRICK_F32 ? nullptr : p->scale_offset_dev;
@@ -836,9 +875,10 @@ int s3r_clear_viewport(s3r_ctx* ctx, uint32_t* viewport, uint32_t W, uint32_t H,
     return S3R_OK;
 }
 
-int s3r_render_block_argb(s3r_ctx* ctx, const s3r_view* view, const float* brick, uint32_t depth,
-                          const uint32_t idx[3], const int32_t rect[4], const float* tf, uint32_t* viewport,
-                          void* stream)
+// pitch: the brick's row pitch in elements (0: a plain (2^depth+1)^3 grid)
+static int render_block_argb_pitched(s3r_ctx* ctx, const s3r_view* view, const float* brick, uint32_t depth,
+                                     uint32_t pitch, const uint32_t idx[3], const int32_t rect[4], const float* tf,
+                                     uint32_t* viewport, void* stream)
 {
     if (!ctx) return fail(nullptr, S3R_ERR_INVALID, "ctx is null");
     int rc = check_view(ctx, view);
@@ -851,10 +891,18 @@ int s3r_render_block_argb(s3r_ctx* ctx, const s3r_view* view, const float* brick
     if ((rc = set_device(ctx))) return rc;
     RenderBlock rb{};
     block_sampling(view->level, idx, depth, rb);
+    rb.pitch = pitch;
     for (int i = 0; i < 4; ++i) rb.rect[i] = rect[i];
     S3R_CUDA(ctx, launch_render_block_argb(view, brick, rb, tf, viewport, as_stream(stream)));
     if (rect[2] > 0 && rect[3] > 0) ++ctx->launches;
     return S3R_OK;
+}
+
+int s3r_render_block_argb(s3r_ctx* ctx, const s3r_view* view, const float* brick, uint32_t depth,
+                          const uint32_t idx[3], const int32_t rect[4], const float* tf, uint32_t* viewport,
+                          void* stream)
+{
+    return render_block_argb_pitched(ctx, view, brick, depth, 0, idx, rect, tf, viewport, stream);
 }
 
 int s3r_index_box_world(uint32_t level, const uint32_t bmin[3], const uint32_t bmax[3], double cmin[3], double cmax[3])
@@ -982,9 +1030,10 @@ int s3r_default_light(const s3r_view* view, s3r_light* out)
     return S3R_OK;
 }
 
-int s3r_render_block(s3r_ctx* ctx, const s3r_view* view, const s3r_presentation* pres, const float* brick,
-                     const float* brick2, uint32_t depth, const uint32_t idx[3], const int32_t rect[4],
-                     const float* tf, uint32_t* viewport, void* stream)
+static int render_block_pitched(s3r_ctx* ctx, const s3r_view* view, const s3r_presentation* pres,
+                                const float* brick, const float* brick2, uint32_t depth, uint32_t pitch,
+                                const uint32_t idx[3], const int32_t rect[4], const float* tf, uint32_t* viewport,
+                                void* stream)
 {
     if (!ctx) return fail(nullptr, S3R_ERR_INVALID, "ctx is null");
     int rc = check_view(ctx, view);
@@ -1007,10 +1056,18 @@ int s3r_render_block(s3r_ctx* ctx, const s3r_view* view, const s3r_presentation*
     if ((rc = set_device(ctx))) return rc;
     RenderBlock rb{};
     block_sampling(view->level, idx, depth, rb);
+    rb.pitch = pitch;
     for (int i = 0; i < 4; ++i) rb.rect[i] = rect[i];
     S3R_CUDA(ctx, launch_render_block_mode(view, pres, brick, brick2, rb, tf, viewport, as_stream(stream)));
     if (rect[2] > 0 && rect[3] > 0) ++ctx->launches;
     return S3R_OK;
+}
+
+int s3r_render_block(s3r_ctx* ctx, const s3r_view* view, const s3r_presentation* pres, const float* brick,
+                     const float* brick2, uint32_t depth, const uint32_t idx[3], const int32_t rect[4],
+                     const float* tf, uint32_t* viewport, void* stream)
+{
+    return render_block_pitched(ctx, view, pres, brick, brick2, depth, 0, idx, rect, tf, viewport, stream);
 }
 
 int s3r_blend_image_part_mip_host(float* dst, int32_t dw, int32_t dh, const float* src, int32_t sw, int32_t sh,
@@ -1161,6 +1218,9 @@ int s3r_frame_plan(s3r_ctx* ctx, const s3r_frame_desc* desc, s3r_plan** out)
     p->nodes = p->node_off[desc->nblocks];
     p->n2i.assign(desc->n2i, desc->n2i + 3 * p->nodes);
     p->vertex_off.assign(desc->nblocks + 1, 0);
+    p->pitch.assign(desc->nblocks, 0);
+    p->vertices = 0;
+    const uint32_t elem_bytes = p->fmt == S3R_BRICK_F32 ? 4u : 2u;
     p->table_host.assign((size_t)m * m * m, RenderBlock{});
     for (auto& t : p->table_host) {
         t.depth = 0xffffffffu;
@@ -1179,21 +1239,25 @@ int s3r_frame_plan(s3r_ctx* ctx, const s3r_frame_desc* desc, s3r_plan** out)
         if (p->node_off[b + 1] - p->node_off[b] > 0xffffffffull)
             return bail(fail(ctx, S3R_ERR_INVALID, "too many nodes in one block"));
         const uint64_t e = (1ull << bl[3]) + 1;
-        p->vertex_off[b + 1] = p->vertex_off[b] + e * e * e;
+        const uint32_t pitch = plan_brick_pitch(bl[3], elem_bytes);
+        p->pitch[b] = pitch;
+        p->vertex_off[b + 1] = p->vertex_off[b] + e * e * pitch;
+        p->vertices += e * e * e;
         RenderBlock& t = p->table_host[bl[0] + m * (bl[1] + m * bl[2])];
         if (t.depth != 0xffffffffu) return bail(fail(ctx, S3R_ERR_INVALID, "duplicate block index"));
         block_sampling(p->level, bl, bl[3], t);
         t.brick_off = p->vertex_off[b];
+        t.pitch = pitch;
         t.block = b;
         const uint32_t lim = (uint32_t)(e - 1);
         for (uint64_t i = p->node_off[b]; i < p->node_off[b + 1]; ++i)
             if (p->n2i[3 * i] > lim || p->n2i[3 * i + 1] > lim || p->n2i[3 * i + 2] > lim)
                 return bail(fail(ctx, S3R_ERR_INVALID, "node index outside its block"));
     }
-    p->vertices = p->vertex_off[desc->nblocks];
-    const size_t esz = p->fmt == S3R_BRICK_F32 ? 4 : 2;
+    p->brick_elems = p->vertex_off[desc->nblocks];
+    const size_t esz = elem_bytes;
     cudaError_t e;
-    if ((e = cudaMalloc(&p->bricks, std::max<uint64_t>(p->vertices, 1) * esz)) != cudaSuccess)
+    if ((e = cudaMalloc(&p->bricks, std::max<uint64_t>(p->brick_elems, 1) * esz)) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "cudaMalloc(bricks)"));
     if ((rc = upload(ctx, &p->node_off_dev, p->node_off))) return bail(rc);
     if ((e = cudaMalloc(&p->queue_dev, sizeof(uint32_t))) != cudaSuccess)
@@ -1249,7 +1313,7 @@ int s3r_plan_info_get(const s3r_plan* p, s3r_plan_info* out)
     if (!p || !out) return fail(nullptr, S3R_ERR_INVALID, "null pointer");
     out->nodes = p->nodes;
     out->vertices = p->vertices;
-    out->brick_bytes = p->vertices * (p->fmt == S3R_BRICK_F32 ? 4 : 2);
+    out->brick_bytes = p->brick_elems * (p->fmt == S3R_BRICK_F32 ? 4 : 2);
     out->tiles = p->tiles;
     out->tile_entries = p->entries;
     out->tile_cells = 1u << p->tile_log2;
@@ -1264,6 +1328,13 @@ int s3r_plan_bricks(const s3r_plan* p, void** bricks, const uint64_t** vertex_of
     if (!p || !bricks || !vertex_off) return fail(nullptr, S3R_ERR_INVALID, "null pointer");
     *bricks = p->bricks;
     *vertex_off = p->vertex_off.data();
+    return S3R_OK;
+}
+
+int s3r_plan_brick_pitches(const s3r_plan* p, const uint32_t** pitch)
+{
+    if (!p || !pitch) return fail(nullptr, S3R_ERR_INVALID, "null pointer");
+    *pitch = p->pitch.data();
     return S3R_OK;
 }
 
@@ -1612,9 +1683,10 @@ int s3r_render_scene_part_bricks(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* v
         view_rect(*view, bl, r);
         if (r[2] <= 0 || r[3] <= 0) return;
         const uint64_t o = plan->vertex_off[b];
-        rc = pres ? s3r_render_block(ctx, view, pres, bricks + o, secondary ? b2 + o : nullptr, bl[3], bl, r, tf,
-                                     viewport, stream)
-                  : s3r_render_block_argb(ctx, view, bricks + o, bl[3], bl, r, tf, viewport, stream);
+        const uint32_t pitch = plan->pitch[b];
+        rc = pres ? render_block_pitched(ctx, view, pres, bricks + o, secondary ? b2 + o : nullptr, bl[3], pitch, bl,
+                                         r, tf, viewport, stream)
+                  : render_block_argb_pitched(ctx, view, bricks + o, bl[3], pitch, bl, r, tf, viewport, stream);
     });
     if (rc) return rc;
     return s3r_bound_rect(ctx, viewport, view->W, view->H, rect, stream);

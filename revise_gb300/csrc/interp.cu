@@ -27,6 +27,8 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <type_traits>
+
 namespace s3r {
 namespace {
 
@@ -328,15 +330,15 @@ template <bool kSlots> __device__ __forceinline__ void fill_cube(float v[27])
 // NaN as +inf gives +inf); flagged cubes test their slots for NaN ("no sparse
 // value") before any slot is overwritten, then turn masked sparse values to NaN.
 template <uint32_t T, typename OutT>
-__device__ __forceinline__ void finest_store(const float* s, const uint32_t* flags, OutT* out, uint64_t e,
-                                             uint32_t ox, uint32_t oy, uint32_t oz, bool far_x, bool far_y,
-                                             bool far_z, float inv_scale, float offset)
+__device__ __forceinline__ void finest_store(const float* s, const uint32_t* flags, OutT* out, uint32_t e,
+                                             uint32_t pitch, uint32_t ox, uint32_t oy, uint32_t oz, bool far_x,
+                                             bool far_y, bool far_z, float inv_scale, float offset)
 {
     using S = SplitTile<T>;
     constexpr uint32_t H = S::H;
     constexpr uint32_t lh = (H >= 2) ? (31 - __builtin_clz(H)) : 0;
     constexpr uint32_t ncubes = H * H * H;
-    const uint64_t e2 = e * e;
+    const uint32_t e2 = e * pitch; // slab stride (a brick holds fewer than 2^32 elements)
 #pragma unroll 1
     for (uint32_t c = threadIdx.x; c < ncubes; c += blockDim.x) {
         const uint32_t ci = c & (H - 1), cj = (c >> lh) & (H - 1), ck = c >> (2 * lh);
@@ -361,19 +363,31 @@ __device__ __forceinline__ void finest_store(const float* s, const uint32_t* fla
         } else {
             fill_cube<false>(v);
         }
-        OutT* base = out + ((uint64_t)(oz + 2 * ck) * e + (oy + 2 * cj)) * e + (ox + 2 * ci);
+        OutT* base = out + (((oz + 2 * ck) * e + (oy + 2 * cj)) * pitch + (ox + 2 * ci));
 #pragma unroll
         for (int p = 0; p < 27; ++p) {
             const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
-            if (a < 2 && b < 2 && cc < 2) Store<OutT>::put_nan(base, (uint64_t)a + b * e + cc * e2, v[p], inv_scale, offset);
+            if (a < 2 && b < 2 && cc < 2) Store<OutT>::put_nan(base, a + b * pitch + cc * e2, v[p], inv_scale, offset);
         }
         const bool lx = far_x && ci == H - 1, ly = far_y && cj == H - 1, lz = far_z && ck == H - 1;
         if (lx || ly || lz) {
 #pragma unroll
             for (int p = 0; p < 27; ++p) {
                 const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
-                if ((a == 2 || b == 2 || cc == 2) && (a < 2 || lx) && (b < 2 || ly) && (cc < 2 || lz))
-                    Store<OutT>::put_nan(base, (uint64_t)a + b * e + cc * e2, v[p], inv_scale, offset);
+                if ((a == 2 || b == 2 || cc == 2) && (a < 2 || lx) && (b < 2 || ly) && (cc < 2 || lz)) {
+                    if constexpr (std::is_same<OutT, float>::value && T >= 8) {
+                        if (a == 2 && pitch >= e + 7) {
+                            // a padded brick (plan layout, d >= 3): x = 2^d starts a sector of its own
+                            // (rows are 32-byte aligned, 2^d is a multiple of 8, the pitch is 2^d + 8):
+                            // write the whole sector, the padding as NaN
+                            float4* q = reinterpret_cast<float4*>(base + a + b * pitch + cc * e2);
+                            q[0] = make_float4(v[p], qnan(), qnan(), qnan());
+                            q[1] = make_float4(qnan(), qnan(), qnan(), qnan());
+                            continue;
+                        }
+                    }
+                    Store<OutT>::put_nan(base, a + b * pitch + cc * e2, v[p], inv_scale, offset);
+                }
             }
         }
     }
@@ -385,6 +399,7 @@ __device__ __forceinline__ void finest_store(const float* s, const uint32_t* fla
 constexpr uint32_t kPrefetch = 2; // entries per thread held in registers
 struct Prefetch {
     uint32_t item;
+    uint32_t flag; // word threadIdx.x of the item's cube flags
     uint64_t node_base, e0, e1;
     uint32_t loc[kPrefetch];
     float val[kPrefetch];
@@ -399,6 +414,7 @@ __device__ __forceinline__ void prefetch_entries(Prefetch& pf, const TileArgs& a
     pf.node_base = a.blocks[blk].node_base;
     pf.e0 = a.entry_off[item];
     pf.e1 = a.entry_off[item + 1];
+    if (threadIdx.x < a.flag_words) pf.flag = a.flags[(uint64_t)item * a.flag_words + threadIdx.x];
 #pragma unroll
     for (uint32_t q = 0; q < kPrefetch; ++q) {
         const uint64_t i = pf.e0 + threadIdx.x + q * blockDim.x;
@@ -410,7 +426,7 @@ __device__ __forceinline__ void prefetch_entries(Prefetch& pf, const TileArgs& a
 }
 
 struct TileItem {
-    uint32_t d, k, L, tx, ty, tz, blk;
+    uint32_t d, k, L, tx, ty, tz, blk, pitch;
     uint64_t node_base, dense_off;
     uint32_t item;
 };
@@ -431,7 +447,11 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
     const uint32_t ox = t.tx * T, oy = t.ty * T, oz = t.tz * T;
     const uint32_t e = (1u << d) + 1u;
     constexpr uint32_t nflags = T >= 2 ? (S::H * S::H * S::H + 31) / 32 : 0;
-    for (uint32_t q = threadIdx.x; q < nflags; q += blockDim.x) flags[q] = 0u;
+    if constexpr (kGrid) {
+        for (uint32_t q = threadIdx.x; q < nflags; q += blockDim.x) flags[q] = 0u;
+    } else {
+        if (threadIdx.x < nflags) flags[threadIdx.x] = pf.flag; // the plan's flags, prefetched
+    }
     // 1. the tile's sparse values (NaN elsewhere) and the descent's
     if constexpr (kGrid) {
         __syncthreads(); // flags cleared
@@ -460,23 +480,8 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
         for (uint32_t q = threadIdx.x; q < 27 * L; q += blockDim.x) desc[q] = qnan();
         __syncthreads();
         auto place = [&](uint32_t loc, float v) {
-            if (loc < E3) {
-                s[loc] = v;
-                if constexpr (T >= 2) {
-                    // tile position of the split offset: class, then (i, j, k) inside it
-                    uint32_t c = 0;
-#pragma unroll
-                    for (uint32_t q = 1; q < 8; ++q) c += loc >= S::base(q) ? 1u : 0u;
-                    if (c) {
-                        const uint32_t r = loc - S::base(c);
-                        const uint32_t nx = S::n(c & 1), ny = S::n((c >> 1) & 1);
-                        const uint32_t ii = r % nx, rr = r / nx, jj = rr % ny, kk = rr / ny;
-                        flag_cubes(flags, S::H, 2 * ii + (c & 1), 2 * jj + ((c >> 1) & 1), 2 * kk + (c >> 2));
-                    }
-                }
-            } else {
-                desc[loc - E3] = v;
-            }
+            if (loc < E3) s[loc] = v;
+            else desc[loc - E3] = v;
         };
         // the prefetched entries, then any beyond what the registers held
 #pragma unroll
@@ -522,13 +527,13 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
     OutT* out = reinterpret_cast<OutT*>(a.out) + t.dense_off;
     const bool far_x = t.tx == mL - 1, far_y = t.ty == mL - 1, far_z = t.tz == mL - 1;
     if constexpr (T >= 2) {
-        finest_store<T, OutT>(s, flags, out, e, ox, oy, oz, far_x, far_y, far_z, inv_scale, offset);
+        finest_store<T, OutT>(s, flags, out, e, t.pitch, ox, oy, oz, far_x, far_y, far_z, inv_scale, offset);
     } else {
         // depth-0 block: its 8 root corners
         for (uint32_t q = threadIdx.x; q < 8; q += blockDim.x) {
             const uint32_t x = q & 1, y = (q >> 1) & 1, z = q >> 2;
-            Store<OutT>::put(out, ((uint64_t)(oz + z) * e + (oy + y)) * e + ox + x, s[at(x, y, z)], inv_scale,
-                             offset);
+            Store<OutT>::put(out, ((uint64_t)(oz + z) * e + (oy + y)) * t.pitch + ox + x, s[at(x, y, z)],
+                             inv_scale, offset);
         }
     }
 }
@@ -567,6 +572,7 @@ __global__ void __launch_bounds__(kInterpThreads, 8) interp_tiles_kernel(TileArg
             t.d = a.grid_depth;
             t.k = a.grid_tile_log2 < t.d ? a.grid_tile_log2 : t.d;
             t.L = t.d - t.k;
+            t.pitch = (1u << t.d) + 1u;
             tile = item;
         } else {
             const uint2 it = a.items[item];
@@ -578,6 +584,7 @@ __global__ void __launch_bounds__(kInterpThreads, 8) interp_tiles_kernel(TileArg
             t.L = b.coarse_log2;
             t.node_base = b.node_base;
             t.dense_off = b.dense_off;
+            t.pitch = b.pitch;
         }
         const uint32_t mL = 1u << t.L;
         t.tx = tile & (mL - 1);

@@ -46,8 +46,15 @@ struct BlockRay {
     float step[3];
     float origin[3];
     float factor;
-    uint32_t n;
+    uint32_t n;     // vertices per axis, 2^depth+1
+    uint32_t pitch; // row pitch of the brick in elements (>= n)
 };
+
+// A brick's extent and row pitch: vertex (x, y, z) is element (z n + y) pitch + x.
+struct Dim {
+    uint32_t n, pitch;
+};
+__device__ __forceinline__ Dim dim_of(const BlockRay& r) { return Dim{r.n, r.pitch}; }
 
 __device__ __forceinline__ void pixel_ray(const s3r_view& v, uint32_t vx, uint32_t vy, float org[3], float dir[3])
 {
@@ -116,6 +123,7 @@ __device__ __forceinline__ bool block_ray(const s3r_view& v, const float org[3],
     for (int d = 0; d < 3; ++d) r.origin[d] = rb.origin[d];
     r.factor = rb.factor;
     r.n = n;
+    r.pitch = rb.pitch ? rb.pitch : n;
     r.samples = s;
     return true;
 }
@@ -160,16 +168,16 @@ template <> struct Brick<S3R_BRICK_BF16> {
 };
 
 template <int Fmt>
-__device__ __forceinline__ bool trilinear(const void* brick, const Cell& c, uint32_t n, float& val, float t[8],
+__device__ __forceinline__ bool trilinear(const void* brick, const Cell& c, Dim g, float& val, float t[8],
                                           uint64_t off[8])
 {
-    const uint64_t n64 = n;
+    const uint64_t n64 = g.n, p64 = g.pitch;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const uint64_t x = (q & 1) ? c.i1[0] : c.i0[0];
         const uint64_t y = (q & 2) ? c.i1[1] : c.i0[1];
         const uint64_t z = (q & 4) ? c.i1[2] : c.i0[2];
-        off[q] = (z * n64 + y) * n64 + x;
+        off[q] = (z * n64 + y) * p64 + x;
         t[q] = Brick<Fmt>::get(brick, off[q]);
     }
     bool bad = false;
@@ -229,10 +237,10 @@ __device__ __forceinline__ float sample_tc(const BlockRay& r, int k, int d)
 template <int Fmt> struct Brick;
 
 template <int Fmt>
-__device__ __forceinline__ bool tex_trilinear_at(const void* brick, uint32_t n, float tcx, float tcy, float tcz,
+__device__ __forceinline__ bool tex_trilinear_at(const void* brick, Dim g, float tcx, float tcy, float tcz,
                                                  float& val)
 {
-    const int hi = (int)n - 1;
+    const int hi = (int)g.n - 1;
     const TexAxis x = tex_axis(tcx, hi);
     const TexAxis y = tex_axis(tcy, hi);
     const TexAxis z = tex_axis(tcz, hi);
@@ -247,14 +255,14 @@ __device__ __forceinline__ bool tex_trilinear_at(const void* brick, uint32_t n, 
         w[hz << 2] = yll;
         w[2 | (hz << 2)] = xl - yll;
     }
-    const uint64_t n64 = n;
+    const uint64_t n64 = g.n, p64 = g.pitch;
     float t[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const uint64_t xi = (q & 1) ? x.i1 : x.i0;
         const uint64_t yi = (q & 2) ? y.i1 : y.i0;
         const uint64_t zi = (q & 4) ? z.i1 : z.i0;
-        t[q] = Brick<Fmt>::get(brick, (zi * n64 + yi) * n64 + xi);
+        t[q] = Brick<Fmt>::get(brick, (zi * n64 + yi) * p64 + xi);
     }
     // per-axis factor nonzero: the low texel needs a < 256, the high one a > 0
     const bool lx = x.a < 256, hx = x.a > 0, ly = y.a < 256, hy = y.a > 0, lz = z.a < 256, hz = z.a > 0;
@@ -274,7 +282,7 @@ __device__ __forceinline__ bool tex_trilinear_at(const void* brick, uint32_t n, 
 template <int Fmt>
 __device__ __forceinline__ bool tex_trilinear(const void* brick, const BlockRay& r, int k, float& val)
 {
-    return tex_trilinear_at<Fmt>(brick, r.n, sample_tc(r, k, 0), sample_tc(r, k, 1), sample_tc(r, k, 2), val);
+    return tex_trilinear_at<Fmt>(brick, dim_of(r), sample_tc(r, k, 0), sample_tc(r, k, 1), sample_tc(r, k, 2), val);
 }
 
 struct TfSample {
@@ -368,13 +376,13 @@ __global__ void render_block_argb_kernel(const s3r_view v, const float* __restri
             const float tcz = __fmul_rn(__fsub_rn(tp[2], r.origin[2]), r.factor);
 #pragma unroll
             for (int d = 0; d < 3; ++d) tp[d] = __fadd_rn(tp[d], r.step[d]);
-            if (!tex_trilinear_at<S3R_BRICK_F32>(brick, r.n, tcx, tcy, tcz, val)) continue;
+            if (!tex_trilinear_at<S3R_BRICK_F32>(brick, dim_of(r), tcx, tcy, tcz, val)) continue;
         } else {
             Cell cell;
             sample_cell(r, i - 1, cell);
             float t[8];
             uint64_t off[8];
-            if (!trilinear<S3R_BRICK_F32>(brick, cell, r.n, val, t, off)) continue;
+            if (!trilinear<S3R_BRICK_F32>(brick, cell, dim_of(r), val, t, off)) continue;
         }
         const float v01 = (val - v.field_min) / span;
         float4 col = tex ? tex_tf_lookup(tf, v.tf_n, v01) : tf_lookup(tf, v.tf_n, v01).c;
@@ -414,7 +422,7 @@ __global__ void render_block_argb_kernel(const s3r_view v, const float* __restri
 // Field value at texel coordinate (x, y, z) -- the reference's fetch
 // coordinate -- filtered as kTex says; NaN where the filter gives NaN.
 template <bool kTex>
-__device__ __forceinline__ float field_at(const float* brick, uint32_t n, float x, float y, float z)
+__device__ __forceinline__ float field_at(const float* brick, Dim n, float x, float y, float z)
 {
     float val;
     if constexpr (kTex) {
@@ -422,7 +430,7 @@ __device__ __forceinline__ float field_at(const float* brick, uint32_t n, float 
         return val;
     } else {
         Cell c;
-        const int hi = (int)n - 1;
+        const int hi = (int)n.n - 1;
         const float tc[3] = {x, y, z};
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
@@ -472,7 +480,7 @@ __device__ __forceinline__ F3 blinn(F3 N, F3 V, F3 L, const s3r_light& light, F3
 // computeFragColor (cuda_lighting.hpp:52-95): normal from central differences
 // of the field at +-0.1 texel, double-sided lighting, colour clamped to [0, 1].
 template <bool kTex>
-__device__ __forceinline__ float4 frag_color(const float* brick, uint32_t n, float4 diffuse, F3 eye, F3 surf, F3 tc,
+__device__ __forceinline__ float4 frag_color(const float* brick, Dim n, float4 diffuse, F3 eye, F3 surf, F3 tc,
                                              const s3r_presentation& pr)
 {
     constexpr float d = 0.1f;
@@ -553,7 +561,7 @@ __device__ __forceinline__ ModeOut march_block_mode(const s3r_view& v, const s3r
                                                     const BlockRay& r, uint32_t depth, const float4* tf)
 {
     ModeOut out{ModeOut::kNone, make_float4(0.f, 0.f, 0.f, 0.f), 0.f};
-    const uint32_t n = r.n;
+    const Dim n = dim_of(r);
     const float span = v.field_max - v.field_min;
     const F3 eye = f3(v.cam.eye);
     const F3 step{r.step[0], r.step[1], r.step[2]};
@@ -851,7 +859,7 @@ __device__ __forceinline__ void fetch_texels(const void* brick, const BlockRay& 
         const uint32_t xi = (q & 1) ? c.i1[0] : c.i0[0];
         const uint32_t yi = (q & 2) ? c.i1[1] : c.i0[1];
         const uint32_t zi = (q & 4) ? c.i1[2] : c.i0[2];
-        x.t[q] = Brick<Fmt>::get(brick, (zi * n + yi) * n + xi);
+        x.t[q] = Brick<Fmt>::get(brick, (zi * n + yi) * r.pitch + xi);
     }
 #pragma unroll
     for (int d = 0; d < 3; ++d) x.f[d] = c.f[d];
@@ -1126,21 +1134,21 @@ __global__ void frame_render_mode_kernel(FrameArgs fa, const s3r_presentation pr
 // ---------------------------------------------------------------- adjoint
 
 // The 8 texels of a cell (F32 brick, 32-bit offsets), their offsets, and the trilinear value (false on a NaN).
-__device__ __forceinline__ void cell_offsets(const Cell& c, uint32_t n, uint32_t off[8])
+__device__ __forceinline__ void cell_offsets(const Cell& c, Dim g, uint32_t off[8])
 {
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const uint32_t x = (q & 1) ? c.i1[0] : c.i0[0];
         const uint32_t y = (q & 2) ? c.i1[1] : c.i0[1];
         const uint32_t z = (q & 4) ? c.i1[2] : c.i0[2];
-        off[q] = (z * n + y) * n + x;
+        off[q] = (z * g.n + y) * g.pitch + x;
     }
 }
 
-__device__ __forceinline__ void fetch_cell(const float* brick, const Cell& c, uint32_t n, float t[8])
+__device__ __forceinline__ void fetch_cell(const float* brick, const Cell& c, Dim g, float t[8])
 {
     uint32_t off[8];
-    cell_offsets(c, n, off);
+    cell_offsets(c, g, off);
 #pragma unroll
     for (int q = 0; q < 8; ++q) t[q] = __ldg(brick + off[q]);
 }
@@ -1241,7 +1249,7 @@ __global__ void __launch_bounds__(128, 4) frame_backward_kernel(FrameArgs fa)
                     float val;
                     if (!filter_cell(cell, tcur, val)) return true;
                     uint32_t off[8];
-                    cell_offsets(cell, r.n, off);
+                    cell_offsets(cell, dim_of(r), off);
                     const float fx = cell.f[0], fy = cell.f[1], fz = cell.f[2];
                     // the forward's v01 up to the last ulp (a reciprocal instead of the division)
                     const float v01 = __fmul_rn(__fsub_rn(val, v.field_min), inv_span);
@@ -1325,18 +1333,18 @@ __global__ void __launch_bounds__(128, 4) frame_backward_kernel(FrameArgs fa)
                 float ta[8], tb[8];
                 if (r.samples > 1) {
                     sample_cell(r, 0, ca);
-                    fetch_cell(brick, ca, r.n, ta);
+                    fetch_cell(brick, ca, dim_of(r), ta);
                 }
                 for (int i = 1; i < r.samples; i += 2) {
                     if (i + 1 < r.samples) {
                         sample_cell(r, i, cb);
-                        fetch_cell(brick, cb, r.n, tb);
+                        fetch_cell(brick, cb, dim_of(r), tb);
                     }
                     if (!step_sample(ca, ta)) break;
                     if (i + 1 >= r.samples) break;
                     if (i + 2 < r.samples) {
                         sample_cell(r, i + 1, ca);
-                        fetch_cell(brick, ca, r.n, ta);
+                        fetch_cell(brick, ca, dim_of(r), ta);
                     }
                     if (!step_sample(cb, tb)) break;
                 }

@@ -21,8 +21,20 @@ struct PlanBlock {
     uint32_t coarse_log2; // L = d - k: tiles per axis 2^L
     uint32_t coarse_off;  // first entry of this block's coarse index grid ((2^L+1)^3 int32)
     uint64_t node_base;   // first node of this block in the sparse value array
-    uint64_t dense_off;   // first vertex of this block's brick
+    uint64_t dense_off;   // first element of this block's brick
+    uint32_t pitch;       // brick row pitch in elements (>= 2^d+1): vertex (x, y, z) at (z (2^d+1) + y) pitch + x
+    uint32_t pad;
 };
+
+// Row pitch of a batched plan's brick of depth d: 2^d+1 rounded up to whole
+// 32-byte sectors, so that every row -- and with it every block, whose size is
+// a whole number of rows times 2^d+1 -- starts on a sector boundary and tiles
+// that split a row never share a sector.
+inline __host__ __device__ uint32_t plan_brick_pitch(uint32_t depth, uint32_t elem_bytes)
+{
+    const uint32_t per = 32u / elem_bytes;
+    return (((1u << depth) + 1u + per - 1u) / per) * per;
+}
 
 // Arguments of the tile interpolation kernel.  Two node sources:
 //   grid   != nullptr: one block whose sparse values were scattered into a
@@ -36,6 +48,8 @@ struct TileArgs {
     const uint16_t* entry_local;  // node position inside its tile (tile_offset)
     const uint32_t* entry_node;   // node index within its block
     // entry_local >= (2^k+1)^3 addresses descent slot 27*level + point instead of the tile
+    const uint32_t* flags;        // per item flag_words words: bit c set when finest cube c of the tile
+    uint32_t flag_words;          // holds a sparse value at one of its midpoints (plan form only)
     const float* sparse;          // node values
     const float2* scale_offset;   // per block {scale, offset} for 16-bit bricks
     void* out;                    // brick store
@@ -73,7 +87,8 @@ struct RenderBlock {
     float factor;      // world -> texel scale n / (2 (half + texel/2))     (:181)
     float texel;       // 2 half / n                                         (:169)
     uint32_t block;    // index into the plan's block list (per-brick scale/offset)
-    uint32_t pad[2];
+    uint32_t pitch;    // brick row pitch in elements; 0: 2^depth+1 (a plain dense grid)
+    uint32_t pad;
 };
 
 // Per-block sampling constants of DenseFieldRenderer_cu.cu:168-181, with the

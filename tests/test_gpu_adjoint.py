@@ -38,6 +38,7 @@ def _gpu_grad(ctx, w, target_img, keep=None):
     plan.backward(view, tf, rgba, dl, dtf, dd)
     torch.cuda.synchronize()
     loss = 0.5 * float((dl.double() ** 2).sum())
+    dd = plan.dense(dd)
     plan.close()
     return view, loss, dtf.cpu().numpy().reshape(-1, 4), dd.cpu().numpy()
 

@@ -65,8 +65,7 @@ def test_level_plan_interp_matches_oracle(ctx, shell):
             plan = FramePlan(ctx, fr, _lib.BRICK_F32, tile_cells=tile)
             plan.interp(dev)
             torch.cuda.synchronize()
-            bricks, _ = plan.bricks()
-            assert _same(bricks.cpu().numpy(), oracle.interp_workload(fr)), (level, tile)
+            assert _same(plan.dense().cpu().numpy(), oracle.interp_workload(fr)), (level, tile)
             plan.close()
 
 

@@ -102,10 +102,12 @@ def test_batched_plan_bit_exact_with_oracle(ctx, tile):
     plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=tile)
     plan.interp(torch.from_numpy(w.sparse).cuda())
     torch.cuda.synchronize()
-    bricks, offs = plan.bricks()
-    got = bricks.cpu().numpy()
+    got = plan.dense().cpu().numpy()
     want = oracle.interp_workload(w)
     assert _same(got, want)
+    # rows start on 32-byte sectors: pitch = 2^d+1 rounded up to 8 floats
+    e = (1 << w.blocks[:, 3].astype(np.int64)) + 1
+    assert np.array_equal(plan.pitches(), (e + 7) // 8 * 8)
     plan.close()
 
 
@@ -117,13 +119,16 @@ def test_batched_16bit_bricks_decode_within_quantization(ctx, fmt):
     plan = FramePlan(ctx, w, fmt, tile_cells=16)
     plan.interp(torch.from_numpy(w.sparse).cuda())
     torch.cuda.synchronize()
-    bricks, offs = plan.bricks()
+    dense = plan.dense()
+    offs = w.vertex_off
     so = plan.brick_scales().cpu().numpy()
+    e = (1 << w.blocks[:, 3].astype(np.int64)) + 1
+    assert np.array_equal(plan.pitches(), (e + 15) // 16 * 16)
     if fmt == _lib.BRICK_F16:
-        h = bricks.cpu().numpy().astype(np.float32)
+        h = dense.cpu().numpy().astype(np.float32)
         rel = 2.0 ** -11
     else:
-        h = (bricks.cpu().numpy().astype(np.uint32) << 16).view(np.float32)
+        h = (dense.cpu().numpy().astype(np.uint32) << 16).view(np.float32)
         rel = 2.0 ** -8
     want = oracle.interp_workload(w)
     for b in range(w.nblocks):
@@ -144,14 +149,12 @@ def test_cfg3_full_size_plan_sampled_blocks(ctx):
     plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=16)
     plan.interp(torch.from_numpy(w.sparse).cuda())
     torch.cuda.synchronize()
-    bricks, offs = plan.bricks()
     rng = np.random.default_rng(0)
     deep = np.flatnonzero(w.blocks[:, 3] == 7)[:3]
     sample = np.concatenate([rng.choice(w.nblocks, 40, replace=False), deep])
     for b in sample:
-        a, c = int(offs[b]), int(offs[b + 1])
         n2i, sp = w.block_nodes(int(b))
-        assert _same(bricks[a:c].cpu().numpy(), oracle.interp_f32(n2i, sp, int(w.blocks[b, 3]))), b
+        assert _same(plan.block_dense(int(b)).cpu().numpy(), oracle.interp_f32(n2i, sp, int(w.blocks[b, 3]))), b
     # every vertex was written: NaN only where the oracle says so (checked above) and none left uninitialised
     assert plan.info.vertices == w.vertices
     plan.close()
@@ -177,12 +180,15 @@ def test_cfg3_every_block_matches_single_block_path(ctx, tile):
     assert torch.equal(first, bricks.view(torch.int32))
     no = w.node_off
     n2i_all = to_device_n2i(w.n2i)
+    pit = plan.pitches()
     bad = []
     for b in range(w.nblocks):
         d = int(w.blocks[b, 3])
+        e = (1 << d) + 1
         n0, n1 = int(no[b]), int(no[b + 1])
         one = ctx.interp_dense(n2i_all[n0:n1], sp[n0:n1], d)
-        if not torch.equal(one.view(torch.int32), first[int(offs[b]):int(offs[b + 1])]):
+        mine = first[int(offs[b]):int(offs[b]) + e * e * int(pit[b])].view(e, e, int(pit[b]))[:, :, :e].reshape(-1)
+        if not torch.equal(one.view(torch.int32), mine):
             bad.append(b)
     assert not bad, bad[:10]
     plan.close()
