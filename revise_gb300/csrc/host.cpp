@@ -559,6 +559,7 @@ int plan_bin(s3r_plan* p, uint32_t tile_log2)
         entry_off[it + 1] = entry_off[it] + count[t];
     }
     const uint64_t nentries = entry_off[ntiles];
+    if (nentries > 0xffffffffull) return fail(ctx, S3R_ERR_INVALID, "too many tile entries (2^32 or more)");
     std::vector<uint16_t> local(nentries);
     std::vector<uint32_t> node(nentries);
     // per item: one bit per finest 2x2x2 cube of the tile, set when one of the cube's midpoints holds
@@ -1216,6 +1217,10 @@ int s3r_frame_plan(s3r_ctx* ctx, const s3r_frame_desc* desc, s3r_plan** out)
     p->blocks.assign(desc->blocks, desc->blocks + 4 * (size_t)desc->nblocks);
     p->node_off.assign(desc->node_off, desc->node_off + desc->nblocks + 1);
     p->nodes = p->node_off[desc->nblocks];
+    if (p->nodes > 0xffffffffull) {
+        s3r_plan_destroy(p);
+        return fail(ctx, S3R_ERR_INVALID, "a plan holds fewer than 2^32 nodes");
+    }
     p->n2i.assign(desc->n2i, desc->n2i + 3 * p->nodes);
     p->vertex_off.assign(desc->nblocks + 1, 0);
     p->pitch.assign(desc->nblocks, 0);

@@ -393,36 +393,53 @@ __device__ __forceinline__ void finest_store(const float* s, const uint32_t* fla
     }
 }
 
-// Entries of the next work item, loaded into registers while the current
-// item's finest level runs (their chain of dependent global loads -- item,
-// block, entry, node value -- would otherwise stall the CTA at every tile).
+// Entries of the next work item, loaded into registers in three stages, each
+// issued one phase of the current tile ahead of its use, so that the chain of
+// dependent global loads -- item and block, then entry positions and node
+// indices, then node values -- completes behind the current tile's work
+// instead of stalling the CTA at every tile.
 constexpr uint32_t kPrefetch = 2; // entries per thread held in registers
 struct Prefetch {
     uint32_t item;
     uint32_t flag; // word threadIdx.x of the item's cube flags
-    uint64_t node_base, e0, e1;
+    uint32_t node_base, e0, e1; // a plan holds fewer than 2^32 nodes and entries
     uint32_t loc[kPrefetch];
+    uint32_t node[kPrefetch];
     float val[kPrefetch];
 };
 
-__device__ __forceinline__ void prefetch_entries(Prefetch& pf, const TileArgs& a, uint32_t item)
+// stage 1: the item's block, entry range and flag word
+__device__ __forceinline__ void prefetch_head(Prefetch& pf, const TileArgs& a, uint32_t item)
 {
     pf.item = item;
     pf.e0 = pf.e1 = 0;
     if (item >= a.nitems) return;
     const uint32_t blk = a.items[item].x;
-    pf.node_base = a.blocks[blk].node_base;
-    pf.e0 = a.entry_off[item];
-    pf.e1 = a.entry_off[item + 1];
+    pf.node_base = (uint32_t)a.blocks[blk].node_base;
+    pf.e0 = (uint32_t)a.entry_off[item];
+    pf.e1 = (uint32_t)a.entry_off[item + 1];
     if (threadIdx.x < a.flag_words) pf.flag = a.flags[(uint64_t)item * a.flag_words + threadIdx.x];
+}
+
+// stage 2: positions and node indices of the first kPrefetch * blockDim.x entries
+__device__ __forceinline__ void prefetch_index(Prefetch& pf, const TileArgs& a)
+{
 #pragma unroll
     for (uint32_t q = 0; q < kPrefetch; ++q) {
-        const uint64_t i = pf.e0 + threadIdx.x + q * blockDim.x;
+        const uint32_t i = pf.e0 + threadIdx.x + q * blockDim.x;
         if (i < pf.e1) {
             pf.loc[q] = a.entry_local[i];
-            pf.val[q] = a.sparse[pf.node_base + a.entry_node[i]];
+            pf.node[q] = a.entry_node[i];
         }
     }
+}
+
+// stage 3: their node values
+__device__ __forceinline__ void prefetch_values(Prefetch& pf, const TileArgs& a)
+{
+#pragma unroll
+    for (uint32_t q = 0; q < kPrefetch; ++q)
+        if (pf.e0 + threadIdx.x + q * blockDim.x < pf.e1) pf.val[q] = a.sparse[pf.node_base + pf.node[q]];
 }
 
 struct TileItem {
@@ -487,8 +504,9 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
 #pragma unroll
         for (uint32_t q = 0; q < kPrefetch; ++q)
             if (pf.e0 + threadIdx.x + q * blockDim.x < pf.e1) place(pf.loc[q], to_internal(pf.val[q]));
-        for (uint64_t i = pf.e0 + threadIdx.x + kPrefetch * blockDim.x; i < pf.e1; i += blockDim.x)
+        for (uint32_t i = pf.e0 + threadIdx.x + kPrefetch * blockDim.x; i < pf.e1; i += blockDim.x)
             place(a.entry_local[i], to_internal(a.sparse[t.node_base + a.entry_node[i]]));
+        prefetch_head(pf, a, *next_item); // the current item's entries are placed
     }
     __syncthreads();
     // 2. tile corners from the coarse levels, then the tile cube's own midpoints
@@ -505,6 +523,7 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
         }
         __syncthreads();
     }
+    if constexpr (!kGrid) prefetch_index(pf, a);
     // 3. the remaining coarser levels on the even sub-array (a tile of T/2 cells)
     if constexpr (T >= 8) {
         constexpr uint32_t kk = 31 - __builtin_clz(T);
@@ -514,7 +533,7 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
         }
     }
     // 4. the finest level, straight to HBM, while the next item's entries load
-    if constexpr (!kGrid) prefetch_entries(pf, a, *next_item);
+    if constexpr (!kGrid) prefetch_values(pf, a);
     float inv_scale = 1.f, offset = 0.f;
     if constexpr (!kGrid) {
         if (a.scale_offset) {
@@ -557,7 +576,11 @@ __global__ void __launch_bounds__(kInterpThreads, 8) interp_tiles_kernel(TileArg
     __syncthreads();
     uint32_t item = item_s;
     Prefetch pf;
-    if constexpr (!kGrid) prefetch_entries(pf, a, item);
+    if constexpr (!kGrid) {
+        prefetch_head(pf, a, item);
+        prefetch_index(pf, a);
+        prefetch_values(pf, a);
+    }
     for (uint32_t iter = 0;; ++iter) {
         if (item >= nitems) break;
         uint32_t* next_p = &next_s[iter & 1];
