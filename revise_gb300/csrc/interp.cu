@@ -192,7 +192,7 @@ __device__ __forceinline__ void cube_level(float* s, uint32_t E, uint32_t T, uin
     const uint32_t st0 = hs, st1 = E * hs, st2 = E * E * hs;
     const uint32_t ncubes = 1u << (3 * j);
 #pragma unroll 1
-    for (uint32_t c = threadIdx.x; c < ncubes; c += blockDim.x) {
+    for (uint32_t c = threadIdx.x; c < ncubes; c += kInterpThreads) {
         const uint32_t ci = c & (m - 1), cj = (c >> j) & (m - 1), ck = c >> (2 * j);
         const uint32_t base = ci * sz + E * (cj * sz + E * (ck * sz));
         float v[27];
@@ -340,7 +340,7 @@ __device__ __forceinline__ void finest_store(const float* s, const uint32_t* fla
     constexpr uint32_t ncubes = H * H * H;
     const uint32_t e2 = e * pitch; // slab stride (a brick holds fewer than 2^32 elements)
 #pragma unroll 1
-    for (uint32_t c = threadIdx.x; c < ncubes; c += blockDim.x) {
+    for (uint32_t c = threadIdx.x; c < ncubes; c += kInterpThreads) {
         const uint32_t ci = c & (H - 1), cj = (c >> lh) & (H - 1), ck = c >> (2 * lh);
         float v[27];
         const bool has = (flags[c >> 5] >> (c & 31)) & 1u;
@@ -421,12 +421,12 @@ __device__ __forceinline__ void prefetch_head(Prefetch& pf, const TileArgs& a, u
     if (threadIdx.x < a.flag_words) pf.flag = a.flags[(uint64_t)item * a.flag_words + threadIdx.x];
 }
 
-// stage 2: positions and node indices of the first kPrefetch * blockDim.x entries
+// stage 2: positions and node indices of the first kPrefetch * kInterpThreads entries
 __device__ __forceinline__ void prefetch_index(Prefetch& pf, const TileArgs& a)
 {
 #pragma unroll
     for (uint32_t q = 0; q < kPrefetch; ++q) {
-        const uint32_t i = pf.e0 + threadIdx.x + q * blockDim.x;
+        const uint32_t i = pf.e0 + threadIdx.x + q * kInterpThreads;
         if (i < pf.e1) {
             pf.loc[q] = a.entry_local[i];
             pf.node[q] = a.entry_node[i];
@@ -439,7 +439,7 @@ __device__ __forceinline__ void prefetch_values(Prefetch& pf, const TileArgs& a)
 {
 #pragma unroll
     for (uint32_t q = 0; q < kPrefetch; ++q)
-        if (pf.e0 + threadIdx.x + q * blockDim.x < pf.e1) pf.val[q] = a.sparse[pf.node_base + pf.node[q]];
+        if (pf.e0 + threadIdx.x + q * kInterpThreads < pf.e1) pf.val[q] = a.sparse[pf.node_base + pf.node[q]];
 }
 
 struct TileItem {
@@ -465,7 +465,7 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
     const uint32_t e = (1u << d) + 1u;
     constexpr uint32_t nflags = T >= 2 ? (S::H * S::H * S::H + 31) / 32 : 0;
     if constexpr (kGrid) {
-        for (uint32_t q = threadIdx.x; q < nflags; q += blockDim.x) flags[q] = 0u;
+        for (uint32_t q = threadIdx.x; q < nflags; q += kInterpThreads) flags[q] = 0u;
     } else {
         if (threadIdx.x < nflags) flags[threadIdx.x] = pf.flag; // the plan's flags, prefetched
     }
@@ -473,14 +473,14 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
     if constexpr (kGrid) {
         __syncthreads(); // flags cleared
 #pragma unroll 1
-        for (uint32_t p = threadIdx.x; p < E3; p += blockDim.x) {
+        for (uint32_t p = threadIdx.x; p < E3; p += kInterpThreads) {
             const uint32_t lx = p % E, r = p / E, ly = r % E, lz = r / E;
             const float v = to_internal(a.grid[((uint64_t)(oz + lz) * e + (oy + ly)) * e + (ox + lx)]);
             s[at(lx, ly, lz)] = v;
             if constexpr (T >= 2)
                 if (!isnan(v)) flag_cubes(flags, S::H, lx, ly, lz);
         }
-        for (uint32_t q = threadIdx.x; q < 27 * L; q += blockDim.x) {
+        for (uint32_t q = threadIdx.x; q < 27 * L; q += kInterpThreads) {
             const uint32_t l = q / 27, p = q % 27;
             const uint32_t size = 1u << (d - l), hs = size >> 1;
             const uint32_t bx = ox & ~(size - 1), by = oy & ~(size - 1), bz = oz & ~(size - 1);
@@ -492,9 +492,9 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
             const float4 nan4 = make_float4(qnan(), qnan(), qnan(), qnan());
             float4* s4 = reinterpret_cast<float4*>(s);
 #pragma unroll 1
-            for (uint32_t p = threadIdx.x; p < (E3 + 3) / 4; p += blockDim.x) s4[p] = nan4;
+            for (uint32_t p = threadIdx.x; p < (E3 + 3) / 4; p += kInterpThreads) s4[p] = nan4;
         }
-        for (uint32_t q = threadIdx.x; q < 27 * L; q += blockDim.x) desc[q] = qnan();
+        for (uint32_t q = threadIdx.x; q < 27 * L; q += kInterpThreads) desc[q] = qnan();
         __syncthreads();
         auto place = [&](uint32_t loc, float v) {
             if (loc < E3) s[loc] = v;
@@ -503,8 +503,8 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
         // the prefetched entries, then any beyond what the registers held
 #pragma unroll
         for (uint32_t q = 0; q < kPrefetch; ++q)
-            if (pf.e0 + threadIdx.x + q * blockDim.x < pf.e1) place(pf.loc[q], to_internal(pf.val[q]));
-        for (uint32_t i = pf.e0 + threadIdx.x + kPrefetch * blockDim.x; i < pf.e1; i += blockDim.x)
+            if (pf.e0 + threadIdx.x + q * kInterpThreads < pf.e1) place(pf.loc[q], to_internal(pf.val[q]));
+        for (uint32_t i = pf.e0 + threadIdx.x + kPrefetch * kInterpThreads; i < pf.e1; i += kInterpThreads)
             place(a.entry_local[i], to_internal(a.sparse[t.node_base + a.entry_node[i]]));
         prefetch_head(pf, a, *next_item); // the current item's entries are placed
     }
@@ -549,7 +549,7 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
         finest_store<T, OutT>(s, flags, out, e, t.pitch, ox, oy, oz, far_x, far_y, far_z, inv_scale, offset);
     } else {
         // depth-0 block: its 8 root corners
-        for (uint32_t q = threadIdx.x; q < 8; q += blockDim.x) {
+        for (uint32_t q = threadIdx.x; q < 8; q += kInterpThreads) {
             const uint32_t x = q & 1, y = (q >> 1) & 1, z = q >> 2;
             Store<OutT>::put(out, ((uint64_t)(oz + z) * e + (oy + y)) * t.pitch + ox + x, s[at(x, y, z)],
                              inv_scale, offset);
