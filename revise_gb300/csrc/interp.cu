@@ -370,25 +370,42 @@ __device__ __forceinline__ void finest_store(const float* s, const uint32_t* fla
             if (a < 2 && b < 2 && cc < 2) Store<OutT>::put_nan(base, a + b * pitch + cc * e2, v[p], inv_scale, offset);
         }
         const bool lx = far_x && ci == H - 1, ly = far_y && cj == H - 1, lz = far_z && ck == H - 1;
-        if (lx || ly || lz) {
-#pragma unroll
-            for (int p = 0; p < 27; ++p) {
-                const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
-                if ((a == 2 || b == 2 || cc == 2) && (a < 2 || lx) && (b < 2 || ly) && (cc < 2 || lz)) {
-                    if constexpr (std::is_same<OutT, float>::value && T >= 8) {
-                        if (a == 2 && pitch >= e + 7) {
-                            // a padded brick (plan layout, d >= 3): x = 2^d starts a sector of its own
-                            // (rows are 32-byte aligned, 2^d is a multiple of 8, the pitch is 2^d + 8):
-                            // write the whole sector, the padding as NaN
-                            float4* q = reinterpret_cast<float4*>(base + a + b * pitch + cc * e2);
-                            q[0] = make_float4(v[p], qnan(), qnan(), qnan());
-                            q[1] = make_float4(qnan(), qnan(), qnan(), qnan());
-                            continue;
-                        }
-                    }
-                    Store<OutT>::put_nan(base, a + b * pitch + cc * e2, v[p], inv_scale, offset);
+        // the far side where this is the block's last cube along an axis: the x = 2 face (with its
+        // y = 2 / z = 2 edges where those are far too), then y = 2 (x < 2), then z = 2 (x, y < 2)
+        auto far_put = [&](int p) {
+            const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
+            if constexpr (std::is_same<OutT, float>::value && T >= 8) {
+                if (a == 2 && pitch >= e + 7) {
+                    // a padded brick (plan layout, d >= 3): x = 2^d starts a sector of its own
+                    // (rows are 32-byte aligned, 2^d is a multiple of 8, the pitch is 2^d + 8):
+                    // write the whole sector, the padding as NaN
+                    float4* q = reinterpret_cast<float4*>(base + a + b * pitch + cc * e2);
+                    q[0] = make_float4(v[p], qnan(), qnan(), qnan());
+                    q[1] = make_float4(qnan(), qnan(), qnan(), qnan());
+                    return;
                 }
             }
+            Store<OutT>::put_nan(base, a + b * pitch + cc * e2, v[p], inv_scale, offset);
+        };
+        if (lx) {
+#pragma unroll
+            for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+                for (int c2 = 0; c2 < 3; ++c2)
+                    if ((bb < 2 || ly) && (c2 < 2 || lz)) far_put(2 + 3 * bb + 9 * c2);
+        }
+        if (ly) {
+#pragma unroll
+            for (int a2 = 0; a2 < 2; ++a2)
+#pragma unroll
+                for (int c2 = 0; c2 < 3; ++c2)
+                    if (c2 < 2 || lz) far_put(a2 + 6 + 9 * c2);
+        }
+        if (lz) {
+#pragma unroll
+            for (int a2 = 0; a2 < 2; ++a2)
+#pragma unroll
+                for (int b2 = 0; b2 < 2; ++b2) far_put(a2 + 3 * b2 + 18);
         }
     }
 }
