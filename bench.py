@@ -637,6 +637,19 @@ def measure_modes(ctx, torch, np, with_reference: bool):
     return out
 
 
+def event_ms(torch, fn, k=10):
+    """Mean ms of fn over k runs after 3 warm-up runs, CUDA events on the current stream."""
+    for _ in range(3):
+        fn()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(k):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / k
+
+
 def measure_adjoint(ctx, torch, np):
     """Forward render and adjoint (backward) times on the 8-block differentiation config (cfg5)."""
     from revise_gb300 import host, workloads
@@ -653,19 +666,8 @@ def measure_adjoint(ctx, torch, np):
     bricks, _ = plan.bricks()
     dd = torch.zeros(bricks.numel(), device="cuda")
 
-    def tm(fn, k=10):
-        for _ in range(3):
-            fn()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(k):
-            fn()
-        e1.record()
-        torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / k
-
-    fwd = tm(lambda: plan.render(view, tf, rgba))
-    bwd = tm(lambda: plan.backward(view, tf, rgba, dl, dtf, dd))
+    fwd = event_ms(torch, lambda: plan.render(view, tf, rgba))
+    bwd = event_ms(torch, lambda: plan.backward(view, tf, rgba, dl, dtf, dd))
     plan.close()
     return {"workload": "cfg5: 2x2x2 blocks depth 6, 512x512", "forward_render_ms": fwd, "backward_ms": bwd,
             "adjoint_forward_ratio": bwd / fwd}
@@ -730,7 +732,7 @@ def measure_extras(ctx, torch, np):
     prec = {}
     for name, fmt in (("f32", _lib.BRICK_F32), ("f16", _lib.BRICK_F16), ("bf16", _lib.BRICK_BF16)):
         p = FramePlan(ctx, w2, fmt)
-        ms = tm(lambda: p.run(v2, sp2, tf2, img))
+        ms = event_ms(torch, lambda: p.run(v2, sp2, tf2, img))
         prec[name] = {"ms_per_frame": ms, "frames_per_s": 1e3 / ms}
         p.close()
     out["precision_cfg2"] = prec
