@@ -424,6 +424,17 @@ int s3r_frame_render_mode(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, co
 int s3r_frame_run(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* sparse, const float* tf,
                   float* rgba, uint32_t* argb, unsigned long long* samples, void* stream);
 
+/* s3r_frame_run from host buffers, pipelined across frames: sparse_host (pinned, one float per node) is
+ * copied to the device on a copy stream while the previous frame renders, the frame runs on `stream`,
+ * and its ARGB8 image goes to argb_host (pinned, W*H) on a second copy stream while the next frame
+ * renders.  Two device slots alternate (each with its own captured graph).  Asynchronous: argb_host
+ * holds frame k once s3r_frame_host_sync returns; both host buffers must stay valid until then (a
+ * caller reusing one host image buffer for every frame reads the last frame's image). */
+int s3r_frame_run_host(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* sparse_host,
+                       const float* tf, uint32_t* argb_host, void* stream);
+/* Waits until every frame submitted with s3r_frame_run_host has been copied back. */
+int s3r_frame_host_sync(s3r_ctx* ctx, s3r_plan* plan);
+
 /* Adjoint of s3r_frame_render (F32 bricks) for L = 1/2 sum (I - target)^2:
  * given the forward image rgba (device) and dl_drgba = I - target (device,
  * W*H*4), accumulates dL/dtf (device, tf_n*4 floats) and dL/ddense (device,

@@ -137,6 +137,8 @@ _SIGS = {
     "s3r_plan_info_get": (C.c_int, [vp, C.POINTER(PlanInfo)]),
     "s3r_plan_bricks": (C.c_int, [vp, C.POINTER(vp), C.POINTER(u64p)]),
     "s3r_plan_brick_pitches": (C.c_int, [vp, C.POINTER(u32p)]),
+    "s3r_frame_run_host": (C.c_int, [vp, vp, C.POINTER(View), vp, vp, vp, vp]),
+    "s3r_frame_host_sync": (C.c_int, [vp, vp]),
     "s3r_plan_brick_scales": (C.c_int, [vp, C.POINTER(vp)]),
     "s3r_plan_autotune": (C.c_int, [vp, vp, C.POINTER(View), vp, vp, C.c_uint32, vp]),
     "s3r_frame_interp": (C.c_int, [vp, vp, vp, vp]),

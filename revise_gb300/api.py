@@ -260,6 +260,19 @@ class FramePlan:
         self.ctx._check(self.lib.s3r_frame_run(self.ctx.h, self.h, C.byref(view), ptr(sparse_dev), ptr(tf_dev),
                                                ptr(rgba), ptr(argb), ptr(samples), _stream(stream)))
 
+    def run_host(self, view: View, sparse_host, tf_dev, argb_host, stream=None):
+        """One frame from host buffers (pinned torch tensors: the sparse values, the W*H int32 ARGB image),
+        pipelined with the frames before and after it (s3r_frame_run_host); call host_sync() before
+        reading argb_host."""
+        for t in (sparse_host, argb_host):
+            if t.is_cuda or not t.is_pinned():
+                raise ValueError("run_host takes pinned host tensors")
+        self.ctx._check(self.lib.s3r_frame_run_host(self.ctx.h, self.h, C.byref(view), ptr(sparse_host), ptr(tf_dev),
+                                                    ptr(argb_host), _stream(stream)))
+
+    def host_sync(self):
+        self.ctx._check(self.lib.s3r_frame_host_sync(self.ctx.h, self.h))
+
     def autotune(self, view: View, sparse_dev, tf_dev, reps: int = 3, stream=None):
         self.ctx._check(self.lib.s3r_plan_autotune(self.ctx.h, self.h, C.byref(view), ptr(sparse_dev), ptr(tf_dev),
                                                    reps, _stream(stream)))

@@ -41,6 +41,14 @@ struct s3r_ctx {
     int sms = 152;
 };
 
+// One captured frame (interpolation + render) and the arguments it was captured for.
+struct FrameGraph {
+    cudaGraphExec_t exec = nullptr;
+    const void* key[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    uint32_t dims[4] = {0, 0, 0, 0}; // W, H, tf_n, filter the launches were sized for
+    uint32_t kernels = 0;
+};
+
 struct s3r_plan {
     s3r_ctx* ctx = nullptr;
     s3r_frame_desc desc{};
@@ -78,13 +86,18 @@ struct s3r_plan {
     cudaEvent_t staged = nullptr;
     bool have_view = false;
     s3r_view last_view{};
-    // graph of s3r_frame_run
-    cudaGraphExec_t exec = nullptr;
+    // frame graphs: slot 0 for s3r_frame_run, slots 1 and 2 for the two buffers of s3r_frame_run_host
+    FrameGraph graphs[3];
     float* dtf_part = nullptr; // adjoint: kDtfParts copies of the transfer-function gradient
     size_t dtf_part_floats = 0;
-    const void* g_key[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    uint32_t g_dims[4] = {0, 0, 0, 0}; // W, H, tf_n, filter the graph's launches were sized for
-    uint32_t graph_kernels = 0;
+    // s3r_frame_run_host: per slot a device copy of the frame's sparse values and its image, and the
+    // streams and events that overlap frame k's copies with frames k-1 and k+1
+    float* hs_sparse[2] = {nullptr, nullptr};
+    uint32_t* hs_argb[2] = {nullptr, nullptr};
+    uint64_t hs_pixels = 0;
+    uint64_t hs_frames = 0;
+    cudaStream_t hs_h2d = nullptr, hs_d2h = nullptr;
+    cudaEvent_t hs_copied[2] = {nullptr, nullptr}, hs_rendered[2] = {nullptr, nullptr}, hs_read[2] = {nullptr, nullptr};
 };
 
 void s3r::set_thread_error(const char* msg) { g_last_error = msg; }
@@ -427,9 +440,10 @@ void plan_free_device(s3r_plan* p)
 
 void plan_drop_graph(s3r_plan* p)
 {
-    if (p->exec) cudaGraphExecDestroy(p->exec);
-    p->exec = nullptr;
-    for (auto& k : p->g_key) k = nullptr;
+    for (auto& g : p->graphs) {
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g = FrameGraph{};
+    }
 }
 
 template <class T> int upload(s3r_ctx* ctx, T** dst, const std::vector<T>& src)
@@ -1288,10 +1302,13 @@ int s3r_frame_plan(s3r_ctx* ctx, const s3r_frame_desc* desc, s3r_plan** out)
     return S3R_OK;
 }
 
+static void plan_destroy_host_pipeline(s3r_plan* p);
+
 int s3r_plan_destroy(s3r_plan* p)
 {
     if (!p) return S3R_OK;
     if (p->ctx) cudaSetDevice(p->ctx->device);
+    plan_destroy_host_pipeline(p);
     plan_drop_graph(p);
     plan_free_device(p);
     auto f = [](void* q) {
@@ -1410,6 +1427,9 @@ int s3r_frame_render_mode(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, co
     return S3R_OK;
 }
 
+static int plan_launch_frame(s3r_plan* plan, int slot, const s3r_view* view, const float* sparse, const float* tf,
+                             float* rgba, uint32_t* argb, unsigned long long* samples, cudaStream_t s);
+
 int s3r_frame_run(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* sparse, const float* tf,
                   float* rgba, uint32_t* argb, unsigned long long* samples, void* stream)
 {
@@ -1421,12 +1441,21 @@ int s3r_frame_run(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const floa
     if ((rc = set_device(ctx))) return rc;
     cudaStream_t s = as_stream(stream);
     if ((rc = plan_stage_view(plan, view, s))) return rc;
+    return plan_launch_frame(plan, 0, view, sparse, tf, rgba, argb, samples, s);
+}
+
+// The frame as a CUDA graph in cache slot `slot`, captured again when its arguments change.
+static int plan_launch_frame(s3r_plan* plan, int slot, const s3r_view* view, const float* sparse, const float* tf,
+                      float* rgba, uint32_t* argb, unsigned long long* samples, cudaStream_t s)
+{
+    s3r_ctx* ctx = plan->ctx;
+    FrameGraph& G = plan->graphs[slot];
     const void* key[5] = {sparse, tf, rgba, argb, samples};
     const uint32_t dims[4] = {view->W, view->H, view->tf_n, view->filter};
-    const bool same = plan->exec && std::memcmp(key, plan->g_key, sizeof(key)) == 0 &&
-                      std::memcmp(dims, plan->g_dims, sizeof(dims)) == 0;
+    const bool same = G.exec && std::memcmp(key, G.key, sizeof(key)) == 0 && std::memcmp(dims, G.dims, sizeof(dims)) == 0;
     if (!same) {
-        plan_drop_graph(plan);
+        if (G.exec) cudaGraphExecDestroy(G.exec);
+        G = FrameGraph{};
         cudaStream_t cs = ctx->capture;
         S3R_CUDA(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
         uint32_t k = 0;
@@ -1439,18 +1468,113 @@ int s3r_frame_run(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const floa
             return r3;
         }
         if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaStreamEndCapture");
-        e = cudaGraphInstantiate(&plan->exec, graph, 0);
+        e = cudaGraphInstantiate(&G.exec, graph, 0);
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) {
-            plan->exec = nullptr;
+            G.exec = nullptr;
             return cuda_fail(ctx, e, "cudaGraphInstantiate");
         }
-        std::memcpy(plan->g_key, key, sizeof(key));
-        std::memcpy(plan->g_dims, dims, sizeof(dims));
-        plan->graph_kernels = k;
+        std::memcpy(G.key, key, sizeof(key));
+        std::memcpy(G.dims, dims, sizeof(dims));
+        G.kernels = k;
     }
-    S3R_CUDA(ctx, cudaGraphLaunch(plan->exec, s));
-    ctx->launches += plan->graph_kernels;
+    S3R_CUDA(ctx, cudaGraphLaunch(G.exec, s));
+    ctx->launches += G.kernels;
+    return S3R_OK;
+}
+
+// Releases the host-buffer pipeline's device buffers (after its copies have finished).
+static void plan_free_host_slots(s3r_plan* p)
+{
+    if (p->hs_h2d) cudaStreamSynchronize(p->hs_h2d);
+    if (p->hs_d2h) cudaStreamSynchronize(p->hs_d2h);
+    for (int b = 0; b < 2; ++b) {
+        if (p->hs_sparse[b]) cudaFree(p->hs_sparse[b]);
+        if (p->hs_argb[b]) cudaFree(p->hs_argb[b]);
+        p->hs_sparse[b] = nullptr;
+        p->hs_argb[b] = nullptr;
+    }
+    p->hs_pixels = 0;
+}
+
+static void plan_destroy_host_pipeline(s3r_plan* p)
+{
+    plan_free_host_slots(p);
+    for (int b = 0; b < 2; ++b) {
+        for (cudaEvent_t* ev : {&p->hs_copied[b], &p->hs_rendered[b], &p->hs_read[b]}) {
+            if (*ev) cudaEventDestroy(*ev);
+            *ev = nullptr;
+        }
+    }
+    if (p->hs_h2d) cudaStreamDestroy(p->hs_h2d);
+    if (p->hs_d2h) cudaStreamDestroy(p->hs_d2h);
+    p->hs_h2d = p->hs_d2h = nullptr;
+}
+
+int s3r_frame_run_host(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* sparse_host, const float* tf,
+                       uint32_t* argb_host, void* stream)
+{
+    if (!ctx || !plan || !tf || !argb_host || (!sparse_host && plan->nodes))
+        return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (plan->ctx != ctx) return fail(ctx, S3R_ERR_INVALID, "plan belongs to another context");
+    int rc = check_view(ctx, view);
+    if (rc) return rc;
+    if (view->level != plan->level) return fail(ctx, S3R_ERR_INVALID, "view level differs from the plan level");
+    if ((rc = set_device(ctx))) return rc;
+    cudaError_t e;
+    if (!plan->hs_h2d) {
+        if ((e = cudaStreamCreateWithFlags(&plan->hs_h2d, cudaStreamNonBlocking)) != cudaSuccess ||
+            (e = cudaStreamCreateWithFlags(&plan->hs_d2h, cudaStreamNonBlocking)) != cudaSuccess)
+            return cuda_fail(ctx, e, "cudaStreamCreate(host frames)");
+        for (int b = 0; b < 2; ++b)
+            for (cudaEvent_t* ev : {&plan->hs_copied[b], &plan->hs_rendered[b], &plan->hs_read[b]})
+                if ((e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming)) != cudaSuccess)
+                    return cuda_fail(ctx, e, "cudaEventCreate(host frames)");
+    }
+    const uint64_t pixels = (uint64_t)view->W * view->H;
+    if (pixels != plan->hs_pixels || !plan->hs_sparse[0]) {
+        plan_free_host_slots(plan);
+        for (int b = 0; b < 2; ++b) {
+            if ((e = cudaMalloc(&plan->hs_sparse[b], std::max<uint64_t>(plan->nodes, 1) * sizeof(float))) != cudaSuccess ||
+                (e = cudaMalloc(&plan->hs_argb[b], pixels * sizeof(uint32_t))) != cudaSuccess) {
+                plan_free_host_slots(plan);
+                return cuda_fail(ctx, e, "cudaMalloc(host frames)");
+            }
+        }
+        plan->hs_pixels = pixels;
+    }
+    cudaStream_t s = as_stream(stream);
+    const int b = (int)(plan->hs_frames & 1);
+    // H2D into slot b once the frame two back no longer reads it
+    S3R_CUDA(ctx, cudaStreamWaitEvent(plan->hs_h2d, plan->hs_rendered[b], 0));
+    if (plan->nodes)
+        S3R_CUDA(ctx, cudaMemcpyAsync(plan->hs_sparse[b], sparse_host, plan->nodes * sizeof(float),
+                                      cudaMemcpyHostToDevice, plan->hs_h2d));
+    S3R_CUDA(ctx, cudaEventRecord(plan->hs_copied[b], plan->hs_h2d));
+    // the frame, once its input has landed and the image two frames back has been read out
+    S3R_CUDA(ctx, cudaStreamWaitEvent(s, plan->hs_copied[b], 0));
+    S3R_CUDA(ctx, cudaStreamWaitEvent(s, plan->hs_read[b], 0));
+    if ((rc = plan_stage_view(plan, view, s))) return rc;
+    if ((rc = plan_launch_frame(plan, 1 + b, view, plan->hs_sparse[b], tf, nullptr, plan->hs_argb[b], nullptr, s)))
+        return rc;
+    S3R_CUDA(ctx, cudaEventRecord(plan->hs_rendered[b], s));
+    // D2H of the image while the next frame runs
+    S3R_CUDA(ctx, cudaStreamWaitEvent(plan->hs_d2h, plan->hs_rendered[b], 0));
+    S3R_CUDA(ctx, cudaMemcpyAsync(argb_host, plan->hs_argb[b], pixels * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                  plan->hs_d2h));
+    S3R_CUDA(ctx, cudaEventRecord(plan->hs_read[b], plan->hs_d2h));
+    ++plan->hs_frames;
+    return S3R_OK;
+}
+
+int s3r_frame_host_sync(s3r_ctx* ctx, s3r_plan* plan)
+{
+    if (!ctx || !plan) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (!plan->hs_d2h) return S3R_OK;
+    int rc = set_device(ctx);
+    if (rc) return rc;
+    S3R_CUDA(ctx, cudaStreamSynchronize(plan->hs_h2d));
+    S3R_CUDA(ctx, cudaStreamSynchronize(plan->hs_d2h));
     return S3R_OK;
 }
 

@@ -99,3 +99,32 @@ def test_scene_part_from_plan_bricks_equals_native_loop(ctx, filt):
         assert a[0] == b[0] and a[1] == b[1]
         assert np.array_equal(_img(a, w.W, w.H), _img(b, w.W, w.H))
     plan.close()
+
+
+def test_frame_run_host_pipeline_matches_device_frames(ctx):
+    """s3r_frame_run_host over several frames with changing sparse values: every image equals the one
+    s3r_frame_run makes from device buffers (the two slots alternate and never mix frames)."""
+    import torch
+    from revise_gb300 import host
+    from revise_gb300.api import FramePlan
+    w = workloads.small(seed=21, level=1, depths=(2, 3, 4), W=80, H=64)
+    view = host.view_for(w)
+    plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=8)
+    tf = torch.from_numpy(np.ascontiguousarray(w.tf)).cuda()
+    rng = np.random.default_rng(3)
+    frames = [(w.sparse * np.float32(1 + 0.1 * k) + np.float32(rng.normal())).astype(np.float32) for k in range(5)]
+    frames = [np.where(w.sparse == np.float32(1e30), np.float32(1e30), f).astype(np.float32) for f in frames]
+    want = []
+    for f in frames:
+        argb = torch.zeros(w.W * w.H, dtype=torch.int32, device="cuda")
+        plan.run(view, torch.from_numpy(f).cuda(), tf, None, argb)
+        want.append(argb.cpu().numpy())
+    hosts = [torch.from_numpy(f).pin_memory() for f in frames]
+    imgs = [torch.zeros(w.W * w.H, dtype=torch.int32).pin_memory() for _ in frames]
+    for f, im in zip(hosts, imgs):
+        plan.run_host(view, f, tf, im)
+    plan.host_sync()
+    for k in range(len(frames)):
+        assert np.array_equal(imgs[k].numpy(), want[k]), k
+    assert len({x.tobytes() for x in want}) == len(want)  # the frames differ
+    plan.close()
