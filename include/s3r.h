@@ -427,9 +427,10 @@ int s3r_frame_run(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const floa
 /* s3r_frame_run from host buffers, pipelined across frames: sparse_host (pinned, one float per node) is
  * copied to the device on a copy stream while the previous frame renders, the frame runs on `stream`,
  * and its ARGB8 image goes to argb_host (pinned, W*H) on a second copy stream while the next frame
- * renders.  Two device slots alternate (each with its own captured graph).  Asynchronous: argb_host
- * holds frame k once s3r_frame_host_sync returns; both host buffers must stay valid until then (a
- * caller reusing one host image buffer for every frame reads the last frame's image). */
+ * renders.  Two device slots alternate (each with its own captured graph).  On return sparse_host may be
+ * refilled, and the image of the previous call is complete in its argb_host; this call's image is
+ * complete after the next call or s3r_frame_host_sync.  Two host image buffers used alternately let
+ * the caller read each frame while the next one renders. */
 int s3r_frame_run_host(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* sparse_host,
                        const float* tf, uint32_t* argb_host, void* stream);
 /* Waits until every frame submitted with s3r_frame_run_host has been copied back. */

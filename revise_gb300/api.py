@@ -262,8 +262,8 @@ class FramePlan:
 
     def run_host(self, view: View, sparse_host, tf_dev, argb_host, stream=None):
         """One frame from host buffers (pinned torch tensors: the sparse values, the W*H int32 ARGB image),
-        pipelined with the frames before and after it (s3r_frame_run_host); call host_sync() before
-        reading argb_host."""
+        pipelined with the frames before and after it (s3r_frame_run_host).  On return sparse_host may be
+        refilled and the previous call's image is complete; this call's after the next call or host_sync()."""
         for t in (sparse_host, argb_host):
             if t.is_cuda or not t.is_pinned():
                 raise ValueError("run_host takes pinned host tensors")

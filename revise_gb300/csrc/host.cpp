@@ -1564,6 +1564,10 @@ int s3r_frame_run_host(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const
                                   plan->hs_d2h));
     S3R_CUDA(ctx, cudaEventRecord(plan->hs_read[b], plan->hs_d2h));
     ++plan->hs_frames;
+    // on return this frame's input buffer is free and the previous frame's image is in host memory; the GPU
+    // meanwhile renders the previous frame and then this one
+    S3R_CUDA(ctx, cudaEventSynchronize(plan->hs_copied[b]));
+    if (plan->hs_frames > 1) S3R_CUDA(ctx, cudaEventSynchronize(plan->hs_read[b ^ 1]));
     return S3R_OK;
 }
 
