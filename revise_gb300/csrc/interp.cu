@@ -94,6 +94,33 @@ template <> struct Store<__nv_bfloat16> {
     }
 };
 
+// Two vertices adjacent along x, already NaN where masked, in one aligned store
+// (the pair starts at an even x of a row whose pitch keeps it aligned).
+template <typename OutT> struct Store2;
+template <> struct Store2<float> {
+    __device__ static void put_nan(float* out, float v0, float v1, float, float)
+    {
+        *reinterpret_cast<float2*>(out) = make_float2(v0, v1);
+    }
+};
+template <> struct Store2<__half> {
+    __device__ static void put_nan(__half* out, float v0, float v1, float inv_scale, float offset)
+    {
+        const __half2 h = __floats2half2_rn((v0 - offset) * inv_scale, (v1 - offset) * inv_scale);
+        const __half nan = __ushort_as_half((unsigned short)0x7e00);
+        *reinterpret_cast<__half2*>(out) = __halves2half2(isnan(v0) ? nan : __low2half(h), isnan(v1) ? nan : __high2half(h));
+    }
+};
+template <> struct Store2<__nv_bfloat16> {
+    __device__ static void put_nan(__nv_bfloat16* out, float v0, float v1, float inv_scale, float offset)
+    {
+        const __nv_bfloat162 h = __floats2bfloat162_rn((v0 - offset) * inv_scale, (v1 - offset) * inv_scale);
+        const __nv_bfloat16 nan = __ushort_as_bfloat16((unsigned short)0x7fc0);
+        *reinterpret_cast<__nv_bfloat162*>(out) =
+            __halves2bfloat162(isnan(v0) ? nan : __low2bfloat16(h), isnan(v1) ? nan : __high2bfloat16(h));
+    }
+};
+
 // +inf -> NaN in one FFMA, every other value (-0 included) unchanged:
 // 0 * v is +-0 for finite v (the sign of v, so v + 0 * v == v exactly) and NaN
 // for infinite v.
@@ -329,7 +356,9 @@ template <bool kSlots> __device__ __forceinline__ void fill_cube(float v[27])
 // loaded, so unflagged cubes produce NaN directly (a NaN in a stencil sum gives
 // NaN as +inf gives +inf); flagged cubes test their slots for NaN ("no sparse
 // value") before any slot is overwritten, then turn masked sparse values to NaN.
-template <uint32_t T, typename OutT>
+// kPairs: plan bricks, whose rows are padded to whole sectors (aligned rows, even pitch): a row's two
+// vertices of a cube go out as one store.  A plain (2^d+1)^3 grid (odd pitch) stores them one by one.
+template <uint32_t T, typename OutT, bool kPairs>
 __device__ __forceinline__ void finest_store(const float* s, const uint32_t* flags, OutT* out, uint32_t e,
                                              uint32_t pitch, uint32_t ox, uint32_t oy, uint32_t oz, bool far_x,
                                              bool far_y, bool far_z, float inv_scale, float offset)
@@ -364,10 +393,20 @@ __device__ __forceinline__ void finest_store(const float* s, const uint32_t* fla
             fill_cube<false>(v);
         }
         OutT* base = out + (((oz + 2 * ck) * e + (oy + 2 * cj)) * pitch + (ox + 2 * ci));
+        if constexpr (kPairs) {
 #pragma unroll
-        for (int p = 0; p < 27; ++p) {
-            const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
-            if (a < 2 && b < 2 && cc < 2) Store<OutT>::put_nan(base, a + b * pitch + cc * e2, v[p], inv_scale, offset);
+            for (int r = 0; r < 4; ++r) {
+                const uint32_t b = r & 1, cc = r >> 1;
+                Store2<OutT>::put_nan(base + b * pitch + cc * e2, v[3 * b + 9 * cc], v[1 + 3 * b + 9 * cc], inv_scale,
+                                      offset);
+            }
+        } else {
+#pragma unroll
+            for (int p = 0; p < 27; ++p) {
+                const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
+                if (a < 2 && b < 2 && cc < 2)
+                    Store<OutT>::put_nan(base, a + b * pitch + cc * e2, v[p], inv_scale, offset);
+            }
         }
         const bool lx = far_x && ci == H - 1, ly = far_y && cj == H - 1, lz = far_z && ck == H - 1;
         // the far side where this is the block's last cube along an axis: the x = 2 face (with its
@@ -563,7 +602,7 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
     OutT* out = reinterpret_cast<OutT*>(a.out) + t.dense_off;
     const bool far_x = t.tx == mL - 1, far_y = t.ty == mL - 1, far_z = t.tz == mL - 1;
     if constexpr (T >= 2) {
-        finest_store<T, OutT>(s, flags, out, e, t.pitch, ox, oy, oz, far_x, far_y, far_z, inv_scale, offset);
+        finest_store<T, OutT, !kGrid>(s, flags, out, e, t.pitch, ox, oy, oz, far_x, far_y, far_z, inv_scale, offset);
     } else {
         // depth-0 block: its 8 root corners
         for (uint32_t q = threadIdx.x; q < 8; q += kInterpThreads) {
