@@ -103,21 +103,21 @@ template <> struct Store2<float> {
         *reinterpret_cast<float2*>(out) = make_float2(v0, v1);
     }
 };
+// 16-bit pairs: (v - offset) / scale as one FMA per value and one paired conversion;
+// a NaN stays NaN through both.
 template <> struct Store2<__half> {
     __device__ static void put_nan(__half* out, float v0, float v1, float inv_scale, float offset)
     {
-        const __half2 h = __floats2half2_rn((v0 - offset) * inv_scale, (v1 - offset) * inv_scale);
-        const __half nan = __ushort_as_half((unsigned short)0x7e00);
-        *reinterpret_cast<__half2*>(out) = __halves2half2(isnan(v0) ? nan : __low2half(h), isnan(v1) ? nan : __high2half(h));
+        const float c = -offset * inv_scale;
+        *reinterpret_cast<__half2*>(out) = __floats2half2_rn(__fmaf_rn(v0, inv_scale, c), __fmaf_rn(v1, inv_scale, c));
     }
 };
 template <> struct Store2<__nv_bfloat16> {
     __device__ static void put_nan(__nv_bfloat16* out, float v0, float v1, float inv_scale, float offset)
     {
-        const __nv_bfloat162 h = __floats2bfloat162_rn((v0 - offset) * inv_scale, (v1 - offset) * inv_scale);
-        const __nv_bfloat16 nan = __ushort_as_bfloat16((unsigned short)0x7fc0);
+        const float c = -offset * inv_scale;
         *reinterpret_cast<__nv_bfloat162*>(out) =
-            __halves2bfloat162(isnan(v0) ? nan : __low2bfloat16(h), isnan(v1) ? nan : __high2bfloat16(h));
+            __floats2bfloat162_rn(__fmaf_rn(v0, inv_scale, c), __fmaf_rn(v1, inv_scale, c));
     }
 };
 
