@@ -435,16 +435,27 @@ __device__ __forceinline__ void finest_store(const float* s, const uint32_t* fla
         }
         if (ly) {
 #pragma unroll
-            for (int a2 = 0; a2 < 2; ++a2)
-#pragma unroll
-                for (int c2 = 0; c2 < 3; ++c2)
-                    if (c2 < 2 || lz) far_put(a2 + 6 + 9 * c2);
+            for (int c2 = 0; c2 < 3; ++c2) {
+                if (c2 == 2 && !lz) continue;
+                if constexpr (kPairs) {
+                    Store2<OutT>::put_nan(base + 2 * pitch + c2 * e2, v[6 + 9 * c2], v[7 + 9 * c2], inv_scale, offset);
+                } else {
+                    far_put(6 + 9 * c2);
+                    far_put(7 + 9 * c2);
+                }
+            }
         }
         if (lz) {
 #pragma unroll
-            for (int a2 = 0; a2 < 2; ++a2)
-#pragma unroll
-                for (int b2 = 0; b2 < 2; ++b2) far_put(a2 + 3 * b2 + 18);
+            for (int b2 = 0; b2 < 2; ++b2) {
+                if constexpr (kPairs) {
+                    Store2<OutT>::put_nan(base + b2 * pitch + 2 * e2, v[3 * b2 + 18], v[1 + 3 * b2 + 18], inv_scale,
+                                          offset);
+                } else {
+                    far_put(3 * b2 + 18);
+                    far_put(1 + 3 * b2 + 18);
+                }
+            }
         }
     }
 }
