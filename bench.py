@@ -408,8 +408,8 @@ def run_gb300(a):
                     "h2d_bytes_per_step": int(sparse.numel() * 4), "d2h_bytes_per_step": int(W * H * 4),
                     "how": f"s3r_frame_run_host, {K} frames back to back from pinned host buffers, copies "
                            "overlapped with the neighbouring frames, first submit to last image in host memory; "
-                           "no L2 flush between frames: every frame writes the 2.5 GB brick store, far more "
-                           "than the 129 MB L2"},
+                           f"no L2 flush between frames: every frame writes the {info.brick_bytes / 1e9:.2f} GB "
+                           "brick store (the L2 holds 129 MB)"},
             "e2e_serial": {"value": V / (t_e2e_serial * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": t_e2e_serial,
                            "how": "per step: H2D, frame (s3r_frame_run), D2H in series on one stream, L2 flushed "
                                   "between steps"},
