@@ -199,15 +199,30 @@ class Clocks:
         self.device = device
         self.proc = None
         self.f = None
+        self.start_line = 0
+
+    def mark(self):
+        """The timed region starts now: samples written so far are not reported (but the last of them, taken
+        under the warm-up's load, stands in when the region is shorter than one sampling interval)."""
+        if self.f is not None:
+            with open(self.f.name) as fh:
+                self.start_line = len(fh.read().splitlines())
 
     def start(self):
         try:
             self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                          "--format=csv,noheader,nounits", "-lms", "50"], stdout=self.f,
                                          stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        # the timed region starts once the sampler runs (its first line is written)
+        t_end = time.time() + 5.0
+        while time.time() < t_end and self.proc.poll() is None:
+            if os.path.getsize(self.f.name) > 0:
+                break
+            time.sleep(0.01)
 
     def stop(self):
         if not self.proc:
@@ -221,7 +236,8 @@ class Clocks:
         self.f.seek(0)
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.f.read().splitlines():
+        lines = self.f.read().splitlines()
+        for line in lines[self.start_line:] or lines[-1:]:
             p = [x.strip() for x in line.split(",")]
             if len(p) < 9:
                 continue
@@ -293,10 +309,12 @@ def run_gb300(a):
         return [x.elapsed_time(y) for x, y in ts]
 
     frame = lambda: plan.run(view, sparse, tf, rgba, argb)  # noqa: E731
+    clocks = Clocks(dev)
+    clocks.start()  # sampling runs through the warm-up; only samples after mark() are reported
     for _ in range(max(3, a.warmup)):
         frame()
-    clocks = Clocks(dev)
-    clocks.start()
+    torch.cuda.synchronize()
+    clocks.mark()
     barrier()
     l0 = ctx.launches
     step_ms = timed(frame, a.steps)
