@@ -634,6 +634,14 @@ int plan_bin(s3r_plan* p, uint32_t tile_log2)
             node[e] = (uint32_t)nd;
         });
     });
+    // items whose tile holds no node at an odd position have no flagged cube, so nothing reads their
+    // midpoint slots: the top bit of the tile field says "fill the slots"
+    for (uint64_t it = 0; it < ntiles; ++it)
+        for (uint32_t w = 0; w < fwords; ++w)
+            if (flags[it * fwords + w]) {
+                items[it].y |= 0x80000000u;
+                break;
+            }
     plan_free_device(p);
     int rc;
     if ((rc = upload(ctx, &p->blocks_dev, pb))) return rc;

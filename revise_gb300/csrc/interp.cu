@@ -511,6 +511,7 @@ __device__ __forceinline__ void prefetch_values(Prefetch& pf, const TileArgs& a)
 
 struct TileItem {
     uint32_t d, k, L, tx, ty, tz, blk, pitch;
+    uint32_t slots; // the tile has flagged cubes, which read its midpoint slots
     uint64_t node_base, dense_off;
     uint32_t item;
 };
@@ -559,7 +560,14 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
             const float4 nan4 = make_float4(qnan(), qnan(), qnan(), qnan());
             float4* s4 = reinterpret_cast<float4*>(s);
 #pragma unroll 1
-            for (uint32_t p = threadIdx.x; p < (E3 + 3) / 4; p += kInterpThreads) s4[p] = nan4;
+            // the even sub-array always (the coarse levels test it for NaN); the midpoint slots only
+            // where a flagged cube will read them
+            uint32_t n4 = (E3 + 3) / 4;
+            if constexpr (T >= 2) {
+                constexpr uint32_t G3 = S::G * S::G * S::G;
+                if (!t.slots) n4 = (G3 + 3) / 4;
+            }
+            for (uint32_t p = threadIdx.x; p < n4; p += kInterpThreads) s4[p] = nan4;
         }
         for (uint32_t q = threadIdx.x; q < 27 * L; q += kInterpThreads) desc[q] = qnan();
         __syncthreads();
@@ -656,6 +664,7 @@ __global__ void __launch_bounds__(kInterpThreads, 8) interp_tiles_kernel(TileArg
         uint32_t tile;
         t.item = item;
         t.blk = 0;
+        t.slots = 1;
         t.node_base = 0;
         t.dense_off = 0;
         if constexpr (kGrid) {
@@ -667,7 +676,8 @@ __global__ void __launch_bounds__(kInterpThreads, 8) interp_tiles_kernel(TileArg
         } else {
             const uint2 it = a.items[item];
             t.blk = it.x;
-            tile = it.y;
+            tile = it.y & 0x7fffffffu;
+            t.slots = it.y >> 31;
             const PlanBlock b = a.blocks[t.blk];
             t.d = b.depth;
             t.k = b.tile_log2;
