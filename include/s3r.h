@@ -430,7 +430,10 @@ int s3r_frame_run(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const floa
  * renders.  Two device slots alternate (each with its own captured graph).  On return sparse_host may be
  * refilled, and the image of the previous call is complete in its argb_host; this call's image is
  * complete after the next call or s3r_frame_host_sync.  Two host image buffers used alternately let
- * the caller read each frame while the next one renders. */
+ * the caller read each frame while the next one renders.  The two slots also hold their own brick
+ * stores and run on their own streams (after the work already queued on `stream`), so that frame k
+ * and frame k+1 overlap on the GPU; slot 0 is the plan's brick store, so s3r_frame_run and friends
+ * on the same plan wait for s3r_frame_host_sync. */
 int s3r_frame_run_host(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* sparse_host,
                        const float* tf, uint32_t* argb_host, void* stream);
 /* Waits until every frame submitted with s3r_frame_run_host has been copied back. */

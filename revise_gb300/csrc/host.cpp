@@ -73,6 +73,10 @@ struct s3r_plan {
     uint32_t* queue_dev = nullptr;
     uint64_t* node_off_dev = nullptr;
     float2* scale_offset_dev = nullptr;
+    // the second data slot of s3r_frame_run_host (slot 0 is the brick store above): its own bricks and
+    // per-brick 16-bit scales, so that two frames can be on the GPU at once
+    void* bricks_1 = nullptr;
+    float2* scale_offset_1 = nullptr;
     void* bricks = nullptr;
     RenderBlock* table_dev = nullptr;
     s3r_view* view_dev = nullptr;
@@ -97,7 +101,9 @@ struct s3r_plan {
     uint64_t hs_pixels = 0;
     uint64_t hs_frames = 0;
     cudaStream_t hs_h2d = nullptr, hs_d2h = nullptr;
+    cudaStream_t hs_comp[2] = {nullptr, nullptr}; // one compute stream per slot: frames k and k+1 overlap
     cudaEvent_t hs_copied[2] = {nullptr, nullptr}, hs_rendered[2] = {nullptr, nullptr}, hs_read[2] = {nullptr, nullptr};
+    cudaEvent_t hs_entry = nullptr; // work queued on the caller's stream before a frame
 };
 
 void s3r::set_thread_error(const char* msg) { g_last_error = msg; }
@@ -697,11 +703,13 @@ int plan_stage_view(s3r_plan* p, const s3r_view* view, cudaStream_t s)
     return S3R_OK;
 }
 
-int plan_launch_interp(s3r_plan* p, const float* sparse, cudaStream_t s, uint32_t* kernels)
+// slot 1: the second data slot of the host-buffer pipeline (its bricks, scales and work-queue counter)
+int plan_launch_interp(s3r_plan* p, const float* sparse, cudaStream_t s, uint32_t* kernels, int slot = 0)
 {
     s3r_ctx* ctx = p->ctx;
+    float2* so = slot ? p->scale_offset_1 : p->scale_offset_dev;
     if (p->fmt != S3R_BRICK_F32) {
-        S3R_CUDA(ctx, launch_block_ranges(p->blocks_dev, p->nblocks, sparse, p->node_off_dev, p->scale_offset_dev, s));
+        S3R_CUDA(ctx, launch_block_ranges(p->blocks_dev, p->nblocks, sparse, p->node_off_dev, so, s));
         ++*kernels;
     }
     TileArgs a{};
@@ -714,27 +722,27 @@ int plan_launch_interp(s3r_plan* p, const float* sparse, cudaStream_t s, uint32_
     a.flags = p->flags_dev;
     a.flag_words = p->flag_words;
     a.sparse = sparse;
-    a.queue = p->queue_dev;
-    a.scale_offset = p->fmt == S3R_BRICK_F32 ? nullptr : p->scale_offset_dev;
-    a.out = p->bricks;
-    S3R_CUDA(ctx, cudaMemsetAsync(p->queue_dev, 0, sizeof(uint32_t), s));
+    a.queue = p->queue_dev + slot;
+    a.scale_offset = p->fmt == S3R_BRICK_F32 ? nullptr : so;
+    a.out = slot ? p->bricks_1 : p->bricks;
+    S3R_CUDA(ctx, cudaMemsetAsync(a.queue, 0, sizeof(uint32_t), s));
     S3R_CUDA(ctx, launch_interp_plan(a, p->fmt, p->tile_log2, p->grid_ctas, s));
     ++*kernels;
     return S3R_OK;
 }
 
 int plan_launch_render(s3r_plan* p, const float* tf, float* rgba, uint32_t* argb, unsigned long long* samples,
-                       cudaStream_t s, uint32_t* kernels)
+                       cudaStream_t s, uint32_t* kernels, int slot = 0)
 {
     FrameArgs fa{};
     fa.view = p->view_dev;
     fa.table = p->table_dev;
-    fa.bricks = p->bricks;
+    fa.bricks = slot ? p->bricks_1 : p->bricks;
     fa.tf = tf;
     fa.rgba = rgba;
     fa.argb = argb;
     fa.samples = samples;
-    fa.scale_offset = p->fmt == S3R_BRICK_F32 ? nullptr : p->scale_offset_dev;
+    fa.scale_offset = p->fmt == S3R_BRICK_F32 ? nullptr : (slot ? p->scale_offset_1 : p->scale_offset_dev);
     fa.cover = p->cover_dev;
     S3R_CUDA(p->ctx, launch_frame_render(fa, p->last_view.W, p->last_view.H, p->last_view.tf_n, p->fmt,
                                          p->render_tile, p->last_view.filter, s));
@@ -1287,7 +1295,7 @@ int s3r_frame_plan(s3r_ctx* ctx, const s3r_frame_desc* desc, s3r_plan** out)
     if ((e = cudaMalloc(&p->bricks, std::max<uint64_t>(p->brick_elems, 1) * esz)) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "cudaMalloc(bricks)"));
     if ((rc = upload(ctx, &p->node_off_dev, p->node_off))) return bail(rc);
-    if ((e = cudaMalloc(&p->queue_dev, sizeof(uint32_t))) != cudaSuccess)
+    if ((e = cudaMalloc(&p->queue_dev, 2 * sizeof(uint32_t))) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "cudaMalloc(queue)"));
     if ((e = cudaMalloc(&p->scale_offset_dev, sizeof(float2) * p->nblocks)) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "cudaMalloc(scales)"));
@@ -1467,8 +1475,9 @@ static int plan_launch_frame(s3r_plan* plan, int slot, const s3r_view* view, con
         cudaStream_t cs = ctx->capture;
         S3R_CUDA(ctx, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
         uint32_t k = 0;
-        int r1 = plan_launch_interp(plan, sparse, cs, &k);
-        int r3 = r1 ? r1 : plan_launch_render(plan, tf, rgba, argb, samples, cs, &k);
+        const int data = slot == 2 ? 1 : 0; // the host pipeline's second slot has its own bricks
+        int r1 = plan_launch_interp(plan, sparse, cs, &k, data);
+        int r3 = r1 ? r1 : plan_launch_render(plan, tf, rgba, argb, samples, cs, &k, data);
         cudaGraph_t graph = nullptr;
         cudaError_t e = cudaStreamEndCapture(cs, &graph);
         if (r3) {
@@ -1496,6 +1505,8 @@ static void plan_free_host_slots(s3r_plan* p)
 {
     if (p->hs_h2d) cudaStreamSynchronize(p->hs_h2d);
     if (p->hs_d2h) cudaStreamSynchronize(p->hs_d2h);
+    for (int b = 0; b < 2; ++b)
+        if (p->hs_comp[b]) cudaStreamSynchronize(p->hs_comp[b]);
     for (int b = 0; b < 2; ++b) {
         if (p->hs_sparse[b]) cudaFree(p->hs_sparse[b]);
         if (p->hs_argb[b]) cudaFree(p->hs_argb[b]);
@@ -1514,9 +1525,19 @@ static void plan_destroy_host_pipeline(s3r_plan* p)
             *ev = nullptr;
         }
     }
+    if (p->hs_entry) cudaEventDestroy(p->hs_entry);
+    p->hs_entry = nullptr;
+    for (int b = 0; b < 2; ++b) {
+        if (p->hs_comp[b]) cudaStreamDestroy(p->hs_comp[b]);
+        p->hs_comp[b] = nullptr;
+    }
     if (p->hs_h2d) cudaStreamDestroy(p->hs_h2d);
     if (p->hs_d2h) cudaStreamDestroy(p->hs_d2h);
     p->hs_h2d = p->hs_d2h = nullptr;
+    if (p->bricks_1) cudaFree(p->bricks_1);
+    if (p->scale_offset_1) cudaFree(p->scale_offset_1);
+    p->bricks_1 = nullptr;
+    p->scale_offset_1 = nullptr;
 }
 
 int s3r_frame_run_host(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* sparse_host, const float* tf,
@@ -1534,10 +1555,21 @@ int s3r_frame_run_host(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const
         if ((e = cudaStreamCreateWithFlags(&plan->hs_h2d, cudaStreamNonBlocking)) != cudaSuccess ||
             (e = cudaStreamCreateWithFlags(&plan->hs_d2h, cudaStreamNonBlocking)) != cudaSuccess)
             return cuda_fail(ctx, e, "cudaStreamCreate(host frames)");
-        for (int b = 0; b < 2; ++b)
+        for (int b = 0; b < 2; ++b) {
+            if ((e = cudaStreamCreateWithFlags(&plan->hs_comp[b], cudaStreamNonBlocking)) != cudaSuccess)
+                return cuda_fail(ctx, e, "cudaStreamCreate(host frames)");
             for (cudaEvent_t* ev : {&plan->hs_copied[b], &plan->hs_rendered[b], &plan->hs_read[b]})
                 if ((e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming)) != cudaSuccess)
                     return cuda_fail(ctx, e, "cudaEventCreate(host frames)");
+        }
+        if ((e = cudaEventCreateWithFlags(&plan->hs_entry, cudaEventDisableTiming)) != cudaSuccess)
+            return cuda_fail(ctx, e, "cudaEventCreate(host frames)");
+    }
+    if (!plan->bricks_1) {
+        const size_t esz = plan->fmt == S3R_BRICK_F32 ? 4 : 2;
+        if ((e = cudaMalloc(&plan->bricks_1, std::max<uint64_t>(plan->brick_elems, 1) * esz)) != cudaSuccess ||
+            (e = cudaMalloc(&plan->scale_offset_1, sizeof(float2) * std::max<uint32_t>(plan->nblocks, 1))) != cudaSuccess)
+            return cuda_fail(ctx, e, "cudaMalloc(second frame slot)");
     }
     const uint64_t pixels = (uint64_t)view->W * view->H;
     if (pixels != plan->hs_pixels || !plan->hs_sparse[0]) {
@@ -1553,19 +1585,29 @@ int s3r_frame_run_host(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const
     }
     cudaStream_t s = as_stream(stream);
     const int b = (int)(plan->hs_frames & 1);
+    cudaStream_t cb = plan->hs_comp[b];
+    S3R_CUDA(ctx, cudaEventRecord(plan->hs_entry, s)); // what the caller queued before comes first
     // H2D into slot b once the frame two back no longer reads it
     S3R_CUDA(ctx, cudaStreamWaitEvent(plan->hs_h2d, plan->hs_rendered[b], 0));
     if (plan->nodes)
         S3R_CUDA(ctx, cudaMemcpyAsync(plan->hs_sparse[b], sparse_host, plan->nodes * sizeof(float),
                                       cudaMemcpyHostToDevice, plan->hs_h2d));
     S3R_CUDA(ctx, cudaEventRecord(plan->hs_copied[b], plan->hs_h2d));
-    // the frame, once its input has landed and the image two frames back has been read out
-    S3R_CUDA(ctx, cudaStreamWaitEvent(s, plan->hs_copied[b], 0));
-    S3R_CUDA(ctx, cudaStreamWaitEvent(s, plan->hs_read[b], 0));
-    if ((rc = plan_stage_view(plan, view, s))) return rc;
-    if ((rc = plan_launch_frame(plan, 1 + b, view, plan->hs_sparse[b], tf, nullptr, plan->hs_argb[b], nullptr, s)))
+    // the frame on slot b's stream -- so that it overlaps the other slot's frame on the GPU -- once its
+    // input has landed and the image two frames back has been read out
+    S3R_CUDA(ctx, cudaStreamWaitEvent(cb, plan->hs_entry, 0));
+    S3R_CUDA(ctx, cudaStreamWaitEvent(cb, plan->hs_copied[b], 0));
+    S3R_CUDA(ctx, cudaStreamWaitEvent(cb, plan->hs_read[b], 0));
+    if (!plan->have_view || std::memcmp(&plan->last_view, view, sizeof(s3r_view)) != 0) {
+        // the render table both slots read changes: let the frames in flight finish first
+        for (int q = 0; q < 2; ++q) S3R_CUDA(ctx, cudaStreamSynchronize(plan->hs_comp[q]));
+    }
+    if ((rc = plan_stage_view(plan, view, cb))) return rc;
+    // the table upload may have been queued on the other slot's stream
+    S3R_CUDA(ctx, cudaStreamWaitEvent(cb, plan->staged, 0));
+    if ((rc = plan_launch_frame(plan, 1 + b, view, plan->hs_sparse[b], tf, nullptr, plan->hs_argb[b], nullptr, cb)))
         return rc;
-    S3R_CUDA(ctx, cudaEventRecord(plan->hs_rendered[b], s));
+    S3R_CUDA(ctx, cudaEventRecord(plan->hs_rendered[b], cb));
     // D2H of the image while the next frame runs
     S3R_CUDA(ctx, cudaStreamWaitEvent(plan->hs_d2h, plan->hs_rendered[b], 0));
     S3R_CUDA(ctx, cudaMemcpyAsync(argb_host, plan->hs_argb[b], pixels * sizeof(uint32_t), cudaMemcpyDeviceToHost,
@@ -1586,6 +1628,7 @@ int s3r_frame_host_sync(s3r_ctx* ctx, s3r_plan* plan)
     int rc = set_device(ctx);
     if (rc) return rc;
     S3R_CUDA(ctx, cudaStreamSynchronize(plan->hs_h2d));
+    for (int b = 0; b < 2; ++b) S3R_CUDA(ctx, cudaStreamSynchronize(plan->hs_comp[b]));
     S3R_CUDA(ctx, cudaStreamSynchronize(plan->hs_d2h));
     return S3R_OK;
 }
