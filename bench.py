@@ -425,7 +425,8 @@ def run_gb300(a):
             "e2e": {"value": V / (t_e2e * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": t_e2e,
                     "h2d_bytes_per_step": int(sparse.numel() * 4), "d2h_bytes_per_step": int(W * H * 4),
                     "how": f"s3r_frame_run_host, {K} frames back to back from pinned host buffers, copies "
-                           "overlapped with the neighbouring frames, first submit to last image in host memory; "
+                           "overlapped with the neighbouring frames and consecutive frames overlapped on the GPU "
+                           "(two slots, two brick stores, two streams), first submit to last image in host memory; "
                            f"no L2 flush between frames: every frame writes the {info.brick_bytes / 1e9:.2f} GB "
                            "brick store (the L2 holds 129 MB)"},
             "e2e_serial": {"value": V / (t_e2e_serial * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": t_e2e_serial,
