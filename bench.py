@@ -143,7 +143,8 @@ def run_reference(a):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": w.vertices / (value * 1e9) * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-        "config": {"workload": f"{a.config}: {w.nblocks} blocks, depths 3-7, {w.vertices} dense vertices",
+        "config": {"workload": f"{a.config}: {w.nblocks} blocks, depths {int(w.blocks[:, 3].min())}-"
+                               f"{int(w.blocks[:, 3].max())}, {w.vertices} dense vertices",
                    "what": "dense-field generation only (the reference has no CPU ray caster)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{len(blocks)} blocks ({sample_v} vertices) per step, all cores, "
@@ -409,7 +410,8 @@ def run_gb300(a):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generator, revise_gb300/workloads.py)",
-            "config": {"workload": f"{a.config}: {w.nblocks} blocks (16^3 at level {w.level}), octree depths 3-7, "
+            "config": {"workload": f"{a.config}: {w.nblocks} blocks ({1 << w.level}^3 at level {w.level}), octree depths "
+                                   f"{int(w.blocks[:, 3].min())}-{int(w.blocks[:, 3].max())}, "
                                    f"{V} dense vertices, {int(info.nodes)} sparse nodes, {W}x{H}, "
                                    "interpolate + ray-cast per frame, CUDA graph",
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
