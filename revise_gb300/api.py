@@ -264,9 +264,15 @@ class FramePlan:
         """One frame from host buffers (pinned torch tensors: the sparse values, the W*H int32 ARGB image),
         pipelined with the frames before and after it (s3r_frame_run_host).  On return sparse_host may be
         refilled and the previous call's image is complete; this call's after the next call or host_sync()."""
+        torch = _torch()
         for t in (sparse_host, argb_host):
-            if t.is_cuda or not t.is_pinned():
-                raise ValueError("run_host takes pinned host tensors")
+            if t.is_cuda or not t.is_pinned() or not t.is_contiguous():
+                raise ValueError("run_host takes contiguous pinned host tensors")
+        # the library copies one float per node in and W*H pixels out through plain pointers
+        if sparse_host.dtype != torch.float32 or sparse_host.numel() != int(self.info.nodes):
+            raise ValueError(f"sparse_host must hold {int(self.info.nodes)} float32 values")
+        if argb_host.dtype not in (torch.int32, torch.uint32) or argb_host.numel() != int(view.W) * int(view.H):
+            raise ValueError(f"argb_host must hold {int(view.W) * int(view.H)} 32-bit pixels")
         self.ctx._check(self.lib.s3r_frame_run_host(self.ctx.h, self.h, C.byref(view), ptr(sparse_host), ptr(tf_dev),
                                                     ptr(argb_host), _stream(stream)))
 
