@@ -425,15 +425,19 @@ int s3r_frame_run(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const floa
                   float* rgba, uint32_t* argb, unsigned long long* samples, void* stream);
 
 /* s3r_frame_run from host buffers, pipelined across frames: sparse_host (pinned, one float per node) is
- * copied to the device on a copy stream while the previous frame renders, the frame runs on `stream`,
- * and its ARGB8 image goes to argb_host (pinned, W*H) on a second copy stream while the next frame
- * renders.  Two device slots alternate (each with its own captured graph).  On return sparse_host may be
- * refilled, and the image of the previous call is complete in its argb_host; this call's image is
- * complete after the next call or s3r_frame_host_sync.  Two host image buffers used alternately let
- * the caller read each frame while the next one renders.  The two slots also hold their own brick
- * stores and run on their own streams (after the work already queued on `stream`), so that frame k
- * and frame k+1 overlap on the GPU; slot 0 is the plan's brick store, so s3r_frame_run and friends
- * on the same plan wait for s3r_frame_host_sync. */
+ * copied to the device on a copy stream while the previous frame renders, and the frame's ARGB8 image goes
+ * to argb_host (pinned, W*H) on a second copy stream while the next frame renders.  Two device slots
+ * alternate, each with its own captured graph, brick store and compute stream, so that frame k and frame
+ * k+1 overlap on the GPU; slot 0 is the plan's brick store, so s3r_frame_run and friends on the same plan
+ * wait for s3r_frame_host_sync.
+ * Ordering against `stream`: the frame starts after the work queued on `stream` before the call.  tf
+ * (device) is copied into the slot's own table by a copy queued on `stream` during the call, so work the
+ * caller queues on `stream` afterwards may change or free tf; the frame itself runs on the slot's
+ * stream, which `stream` does not wait for.
+ * On return sparse_host may be refilled, and the image of the previous call is complete in its
+ * argb_host; this call's image is complete after the next call or s3r_frame_host_sync, so argb_host must
+ * stay allocated until then (two host image buffers used alternately let the caller read each frame
+ * while the next one renders).  A failing call first waits for the work already queued by earlier calls. */
 int s3r_frame_run_host(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* sparse_host,
                        const float* tf, uint32_t* argb_host, void* stream);
 /* Waits until every frame submitted with s3r_frame_run_host has been copied back. */

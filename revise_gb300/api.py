@@ -174,6 +174,7 @@ class FramePlan:
         self.h = h
         self.fmt = brick_format
         self.level = w.level
+        self._host_inflight = []
 
     def close(self):
         if getattr(self, "h", None):
@@ -275,9 +276,14 @@ class FramePlan:
             raise ValueError(f"argb_host must hold {int(view.W) * int(view.H)} 32-bit pixels")
         self.ctx._check(self.lib.s3r_frame_run_host(self.ctx.h, self.h, C.byref(view), ptr(sparse_host), ptr(tf_dev),
                                                     ptr(argb_host), _stream(stream)))
+        # the image copy into argb_host completes after the next call, and tf_dev is read by a copy queued on
+        # the stream: keep both (and the call before's) alive until they are no longer used, so that neither
+        # allocator hands their memory out in between
+        self._host_inflight = (self._host_inflight + [(argb_host, tf_dev)])[-2:]
 
     def host_sync(self):
         self.ctx._check(self.lib.s3r_frame_host_sync(self.ctx.h, self.h))
+        self._host_inflight = []
 
     def autotune(self, view: View, sparse_dev, tf_dev, reps: int = 3, stream=None):
         self.ctx._check(self.lib.s3r_plan_autotune(self.ctx.h, self.h, C.byref(view), ptr(sparse_dev), ptr(tf_dev),

@@ -90,11 +90,16 @@ def build_library(force: bool = False, ptxas_verbose: bool = False) -> Path:
 
 
 def build_oracle(reference: str | None = None) -> None:
+    """The checkers under oracle/: the C restatement always; the reference's own code from the staged
+    tree oracle/_ref/tree (staged first when the reference project root is given, as `reference` or in the
+    REFERENCE environment variable)."""
     oracle = ROOT / "oracle"
     _run(["make", "-s", "-C", str(oracle), "port"])
-    ref = Path(reference or os.environ.get("S3R_REFERENCE", "/root/reference"))
-    if (ref / "include" / "s3dmm" / "DenseFieldInterpolator.hpp").exists():
-        _run(["make", "-s", "-C", str(oracle), "ref", "refcu", f"REFERENCE={ref}"])
+    ref = reference or os.environ.get("REFERENCE")
+    if ref:
+        _run(["make", "-s", "-C", str(oracle), "stage", f"REFERENCE={ref}"])
+    if (oracle / "_ref" / "tree" / "include" / "s3dmm" / "DenseFieldInterpolator.hpp").exists():
+        _run(["make", "-s", "-C", str(oracle), "ref", "refcu", f"NVCC={cuda_home() / 'bin' / 'nvcc'}"])
     # the harness around the reference's CUDA kernels builds anywhere the cubins exist
     if (oracle / "_ref" / "ref_render.cubin").exists() and (oracle / "_ref" / "ref_interp.cubin").exists():
         _run(["make", "-s", "-C", str(oracle), "refcu-harness", f"NVCC={cuda_home() / 'bin' / 'nvcc'}"])

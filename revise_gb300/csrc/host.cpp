@@ -98,6 +98,8 @@ struct s3r_plan {
     // streams and events that overlap frame k's copies with frames k-1 and k+1
     float* hs_sparse[2] = {nullptr, nullptr};
     uint32_t* hs_argb[2] = {nullptr, nullptr};
+    float* hs_tf[2] = {nullptr, nullptr}; // per slot: the frame's transfer function, copied on the caller's stream
+    uint32_t hs_tf_n = 0;
     uint64_t hs_pixels = 0;
     uint64_t hs_frames = 0;
     cudaStream_t hs_h2d = nullptr, hs_d2h = nullptr;
@@ -1510,10 +1512,13 @@ static void plan_free_host_slots(s3r_plan* p)
     for (int b = 0; b < 2; ++b) {
         if (p->hs_sparse[b]) cudaFree(p->hs_sparse[b]);
         if (p->hs_argb[b]) cudaFree(p->hs_argb[b]);
+        if (p->hs_tf[b]) cudaFree(p->hs_tf[b]);
         p->hs_sparse[b] = nullptr;
         p->hs_argb[b] = nullptr;
+        p->hs_tf[b] = nullptr;
     }
     p->hs_pixels = 0;
+    p->hs_tf_n = 0;
 }
 
 static void plan_destroy_host_pipeline(s3r_plan* p)
@@ -1538,6 +1543,51 @@ static void plan_destroy_host_pipeline(s3r_plan* p)
     if (p->scale_offset_1) cudaFree(p->scale_offset_1);
     p->bricks_1 = nullptr;
     p->scale_offset_1 = nullptr;
+}
+
+// The GPU work of one s3r_frame_run_host call on slot b: the copies and the frame, with the events that
+// order them against the neighbouring frames.
+static int frame_host_submit(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* sparse_host,
+                             const float* tf, uint32_t* argb_host, cudaStream_t s, int b)
+{
+    int rc;
+    cudaStream_t cb = plan->hs_comp[b];
+    const uint64_t pixels = (uint64_t)view->W * view->H;
+    // the caller's transfer function is copied on the caller's own stream into slot b's table, once the frame
+    // two back (the table's last reader) has finished: work the caller queues on `stream` after this call may
+    // then change or free tf
+    S3R_CUDA(ctx, cudaStreamWaitEvent(s, plan->hs_rendered[b], 0));
+    S3R_CUDA(ctx, cudaMemcpyAsync(plan->hs_tf[b], tf, (size_t)view->tf_n * 4 * sizeof(float), cudaMemcpyDeviceToDevice,
+                                  s));
+    S3R_CUDA(ctx, cudaEventRecord(plan->hs_entry, s)); // what the caller queued before comes first
+    // H2D into slot b once the frame two back no longer reads it
+    S3R_CUDA(ctx, cudaStreamWaitEvent(plan->hs_h2d, plan->hs_rendered[b], 0));
+    if (plan->nodes)
+        S3R_CUDA(ctx, cudaMemcpyAsync(plan->hs_sparse[b], sparse_host, plan->nodes * sizeof(float),
+                                      cudaMemcpyHostToDevice, plan->hs_h2d));
+    S3R_CUDA(ctx, cudaEventRecord(plan->hs_copied[b], plan->hs_h2d));
+    // the frame on slot b's stream -- so that it overlaps the other slot's frame on the GPU -- once its
+    // input has landed and the image two frames back has been read out
+    S3R_CUDA(ctx, cudaStreamWaitEvent(cb, plan->hs_entry, 0));
+    S3R_CUDA(ctx, cudaStreamWaitEvent(cb, plan->hs_copied[b], 0));
+    S3R_CUDA(ctx, cudaStreamWaitEvent(cb, plan->hs_read[b], 0));
+    if (!plan->have_view || std::memcmp(&plan->last_view, view, sizeof(s3r_view)) != 0) {
+        // the render table both slots read changes: let the frames in flight finish first
+        for (int q = 0; q < 2; ++q) S3R_CUDA(ctx, cudaStreamSynchronize(plan->hs_comp[q]));
+    }
+    if ((rc = plan_stage_view(plan, view, cb))) return rc;
+    // the table upload may have been queued on the other slot's stream
+    S3R_CUDA(ctx, cudaStreamWaitEvent(cb, plan->staged, 0));
+    if ((rc = plan_launch_frame(plan, 1 + b, view, plan->hs_sparse[b], plan->hs_tf[b], nullptr, plan->hs_argb[b],
+                                nullptr, cb)))
+        return rc;
+    S3R_CUDA(ctx, cudaEventRecord(plan->hs_rendered[b], cb));
+    // D2H of the image while the next frame runs
+    S3R_CUDA(ctx, cudaStreamWaitEvent(plan->hs_d2h, plan->hs_rendered[b], 0));
+    S3R_CUDA(ctx, cudaMemcpyAsync(argb_host, plan->hs_argb[b], pixels * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                  plan->hs_d2h));
+    S3R_CUDA(ctx, cudaEventRecord(plan->hs_read[b], plan->hs_d2h));
+    return S3R_OK;
 }
 
 int s3r_frame_run_host(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* sparse_host, const float* tf,
@@ -1572,47 +1622,28 @@ int s3r_frame_run_host(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const
             return cuda_fail(ctx, e, "cudaMalloc(second frame slot)");
     }
     const uint64_t pixels = (uint64_t)view->W * view->H;
-    if (pixels != plan->hs_pixels || !plan->hs_sparse[0]) {
+    if (pixels != plan->hs_pixels || view->tf_n != plan->hs_tf_n || !plan->hs_sparse[0]) {
         plan_free_host_slots(plan);
         for (int b = 0; b < 2; ++b) {
             if ((e = cudaMalloc(&plan->hs_sparse[b], std::max<uint64_t>(plan->nodes, 1) * sizeof(float))) != cudaSuccess ||
-                (e = cudaMalloc(&plan->hs_argb[b], pixels * sizeof(uint32_t))) != cudaSuccess) {
+                (e = cudaMalloc(&plan->hs_argb[b], pixels * sizeof(uint32_t))) != cudaSuccess ||
+                (e = cudaMalloc(&plan->hs_tf[b], (size_t)view->tf_n * 4 * sizeof(float))) != cudaSuccess) {
                 plan_free_host_slots(plan);
                 return cuda_fail(ctx, e, "cudaMalloc(host frames)");
             }
         }
         plan->hs_pixels = pixels;
+        plan->hs_tf_n = view->tf_n;
     }
-    cudaStream_t s = as_stream(stream);
     const int b = (int)(plan->hs_frames & 1);
-    cudaStream_t cb = plan->hs_comp[b];
-    S3R_CUDA(ctx, cudaEventRecord(plan->hs_entry, s)); // what the caller queued before comes first
-    // H2D into slot b once the frame two back no longer reads it
-    S3R_CUDA(ctx, cudaStreamWaitEvent(plan->hs_h2d, plan->hs_rendered[b], 0));
-    if (plan->nodes)
-        S3R_CUDA(ctx, cudaMemcpyAsync(plan->hs_sparse[b], sparse_host, plan->nodes * sizeof(float),
-                                      cudaMemcpyHostToDevice, plan->hs_h2d));
-    S3R_CUDA(ctx, cudaEventRecord(plan->hs_copied[b], plan->hs_h2d));
-    // the frame on slot b's stream -- so that it overlaps the other slot's frame on the GPU -- once its
-    // input has landed and the image two frames back has been read out
-    S3R_CUDA(ctx, cudaStreamWaitEvent(cb, plan->hs_entry, 0));
-    S3R_CUDA(ctx, cudaStreamWaitEvent(cb, plan->hs_copied[b], 0));
-    S3R_CUDA(ctx, cudaStreamWaitEvent(cb, plan->hs_read[b], 0));
-    if (!plan->have_view || std::memcmp(&plan->last_view, view, sizeof(s3r_view)) != 0) {
-        // the render table both slots read changes: let the frames in flight finish first
-        for (int q = 0; q < 2; ++q) S3R_CUDA(ctx, cudaStreamSynchronize(plan->hs_comp[q]));
-    }
-    if ((rc = plan_stage_view(plan, view, cb))) return rc;
-    // the table upload may have been queued on the other slot's stream
-    S3R_CUDA(ctx, cudaStreamWaitEvent(cb, plan->staged, 0));
-    if ((rc = plan_launch_frame(plan, 1 + b, view, plan->hs_sparse[b], tf, nullptr, plan->hs_argb[b], nullptr, cb)))
+    if ((rc = frame_host_submit(ctx, plan, view, sparse_host, tf, argb_host, as_stream(stream), b))) {
+        // a step failed part way: let everything already queued finish, so that the next call starts from
+        // a pipeline whose events all stand for completed work
+        cudaStreamSynchronize(plan->hs_h2d);
+        for (int q = 0; q < 2; ++q) cudaStreamSynchronize(plan->hs_comp[q]);
+        cudaStreamSynchronize(plan->hs_d2h);
         return rc;
-    S3R_CUDA(ctx, cudaEventRecord(plan->hs_rendered[b], cb));
-    // D2H of the image while the next frame runs
-    S3R_CUDA(ctx, cudaStreamWaitEvent(plan->hs_d2h, plan->hs_rendered[b], 0));
-    S3R_CUDA(ctx, cudaMemcpyAsync(argb_host, plan->hs_argb[b], pixels * sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                                  plan->hs_d2h));
-    S3R_CUDA(ctx, cudaEventRecord(plan->hs_read[b], plan->hs_d2h));
+    }
     ++plan->hs_frames;
     // on return this frame's input buffer is free and the previous frame's image is in host memory; the GPU
     // meanwhile renders the previous frame and then this one

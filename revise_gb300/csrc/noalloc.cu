@@ -20,7 +20,10 @@
 //     produce wrong grids: order them on one stream or serialize them.
 //   * The first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress) with that device current and caches it; make that
-//     first call before any stream capture.
+//     first call before any stream capture.  The cache is keyed on the unique id
+//     of the CUDA context current at the call (cuCtxGetId), so that a context
+//     made after cudaDeviceReset, or a caller's own driver-API context on the
+//     same device, gets its own lookup instead of a stale address.
 #include "s3r_internal.h"
 
 #include <mutex>
@@ -37,7 +40,41 @@ static __device__ __align__(256) float g_noalloc_grid[kNoAllocFloats];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
-float* g_grid_on_device[kMaxDevices] = {};
+struct GridAddress {
+    unsigned long long context_id = 0; // 0: none looked up yet
+    float* grid = nullptr;
+};
+GridAddress g_grid_on_device[kMaxDevices];
+
+// cuCtxGetCurrent / cuCtxGetId through the runtime's driver entry points (no link against the driver
+// library).  CUresult is an int-sized enum; 0 is success.
+using CtxGetCurrentFn = int (*)(void**);
+using CtxGetIdFn = int (*)(void*, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+bool g_entry_points_looked_up = false;
+
+// The unique id of the context current on this thread, 0 when there is none or it cannot be told.
+unsigned long long current_context_id()
+{
+    if (!g_entry_points_looked_up) {
+        g_entry_points_looked_up = true;
+        cudaDriverEntryPointQueryResult q1, q2;
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess && q2 == cudaDriverEntryPointSuccess) {
+            g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+            g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f2);
+        }
+    }
+    if (!g_ctx_get_current || !g_ctx_get_id) return 0;
+    void* c = nullptr;
+    unsigned long long id = 0;
+    if (g_ctx_get_current(&c) != 0 || !c || g_ctx_get_id(c, &id) != 0) return 0;
+    return id;
+}
 
 } // namespace
 } // namespace s3r
@@ -59,13 +96,19 @@ extern "C" int s3r_interp_dense_noalloc(const uint16_t* n2i_xyz, const float* sp
     float* grid = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_setup_mutex);
-        if (!g_grid_on_device[dev]) {
+        GridAddress& ga = g_grid_on_device[dev];
+        // the context the call runs in; before the runtime's first use of the device there is none yet,
+        // and the lookup below makes the device's primary context
+        unsigned long long id = current_context_id();
+        if (!ga.grid || id == 0 || id != ga.context_id) {
             void* p = nullptr;
             e = cudaGetSymbolAddress(&p, g_noalloc_grid);
             if (e != cudaSuccess) return record_cuda_error(e, "cudaGetSymbolAddress(g_noalloc_grid)");
-            g_grid_on_device[dev] = static_cast<float*>(p);
+            if (id == 0) id = current_context_id();
+            ga.grid = static_cast<float*>(p);
+            ga.context_id = id; // 0 (ids unavailable): looked up again on every call
         }
-        grid = g_grid_on_device[dev];
+        grid = ga.grid;
     }
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const uint64_t edge = (1ull << depth) + 1ull;

@@ -38,9 +38,9 @@ def make_view(cam: Camera, W: int, H: int, level: int, field_min: float, field_m
     return v
 
 
-def view_for(w, alpha_stop: float = 2.0, filter: int = _lib.FILTER_EXACT) -> View:
-    """The view of a revise_gb300.workloads.Workload."""
-    cam = camera_look_at(w.eye, w.center, w.up, w.fovy, w.W, w.H, w.ortho, w.ortho_height)
+def view_for(w, alpha_stop: float = 2.0, filter: int = _lib.FILTER_EXACT, eye=None) -> View:
+    """The view of a revise_gb300.workloads.Workload (eye: another camera position, same target)."""
+    cam = camera_look_at(w.eye if eye is None else eye, w.center, w.up, w.fovy, w.W, w.H, w.ortho, w.ortho_height)
     return make_view(cam, w.W, w.H, w.level, w.field_min, w.field_max, w.threshold, w.quality, w.tf.shape[0],
                      alpha_stop, filter)
 

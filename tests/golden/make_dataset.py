@@ -24,7 +24,6 @@ from __future__ import annotations
 
 import hashlib
 import json
-import os
 import shutil
 import subprocess
 import sys
@@ -66,8 +65,8 @@ def dump(meta: Path, field_files: list[Path], tmp: Path) -> list[dict]:
 
 
 def main() -> int:
-    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "_ref/ref_dataset_gen",
-                    f"REFERENCE={os.environ.get('S3R_REFERENCE', '/root/reference')}"], check=True)
+    # the reference's writer, compiled from the staged reference files (make -C oracle stage REFERENCE=<root>)
+    subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "_ref/ref_dataset_gen"], check=True)
     with tempfile.TemporaryDirectory() as t:
         tmp = Path(t)
         data = tmp / "data"

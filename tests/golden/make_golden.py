@@ -1,7 +1,7 @@
 """Generates tests/golden/golden.npz from the reference's own code.
 
-Run in a tree where the reference is available (it is compiled in place into
-oracle/_ref by `make -C oracle ref REFERENCE=<reference root>`):
+Run where the reference's code has been staged and compiled into oracle/_ref
+(`make -C oracle stage ref REFERENCE=<reference root>`):
 
     python tests/golden/make_golden.py
 
@@ -29,7 +29,7 @@ sys.path.insert(0, str(ROOT))
 import oracle  # noqa: E402
 from revise_gb300 import workloads as wl  # noqa: E402
 
-REFERENCE = Path("/root/reference")
+TREE = ROOT / "oracle" / "_ref" / "tree"  # the staged reference files
 
 
 def interp_cases(rng):
@@ -71,7 +71,7 @@ def interp_cases(rng):
 
 
 def b2f_cases(rng):
-    src = (REFERENCE / "tests" / "test_BackToFrontOrder.cpp").read_text()
+    src = (TREE / "tests" / "test_BackToFrontOrder.cpp").read_text()
     cases = []
     for m in re.finditer(r"format_b2fo_result<(\d)>\((\d+),\s*([^)]*?)\)\s*,", src):
         dim, size, eye = int(m.group(1)), int(m.group(2)), m.group(3)

@@ -8,7 +8,8 @@ from pathlib import Path
 import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
-REFERENCE = Path("/root/reference")
+# the reference headers as staged by `make -C oracle stage REFERENCE=<root>`
+TREE = ROOT / "oracle" / "_ref" / "tree"
 
 SRC = r'''
 #include "s3dmm/BlockTreeFieldService.hpp"
@@ -24,15 +25,16 @@ template void S::interpolateWith<s3dmm::DenseFieldInterpolatorGb300<s3dmm::Gb300
 
 
 def test_dense_field_interpolator_adapter_compiles(tmp_path):
-    if not (REFERENCE / "include" / "s3dmm" / "BlockTreeFieldService.hpp").exists():
-        pytest.skip("reference headers not present")
-    cuda_inc = Path("/usr/local/cuda/include")
+    if not (TREE / "include" / "s3dmm" / "BlockTreeFieldService.hpp").exists():
+        pytest.skip("reference headers not staged")
+    from revise_gb300.build import cuda_home
+    cuda_inc = cuda_home() / "include"
     if not cuda_inc.exists() or not shutil.which("g++"):
         pytest.skip("no toolchain")
     src = tmp_path / "adapter_check.cpp"
     src.write_text(SRC)
     cmd = ["g++", "-std=c++20", "-fsyntax-only", "-DS3DMM_REAL_TYPE=float", "-DS3DMM_ENABLE_CUDA",
-           "-DS3DMM_PROGRESS_REPORT", f"-I{ROOT / 'oracle' / 'shims_cpu'}", f"-I{ROOT / 'oracle' / 'shims'}", f"-I{REFERENCE / 'include'}",
+           "-DS3DMM_PROGRESS_REPORT", f"-I{ROOT / 'oracle' / 'shims_cpu'}", f"-I{ROOT / 'oracle' / 'shims'}", f"-I{TREE / 'include'}",
            f"-I{ROOT / 'include'}", f"-I{ROOT / 'revise_gb300' / 'adapters'}", f"-I{cuda_inc}", str(src)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]

@@ -128,3 +128,41 @@ def test_frame_run_host_pipeline_matches_device_frames(ctx):
         assert np.array_equal(imgs[k].numpy(), want[k]), k
     assert len({x.tobytes() for x in want}) == len(want)  # the frames differ
     plan.close()
+
+
+@pytest.mark.parametrize("fmt", [_lib.BRICK_F32, _lib.BRICK_F16, _lib.BRICK_BF16])
+def test_frame_run_host_view_change_and_tf_reuse(ctx, fmt):
+    """s3r_frame_run_host with 16-bit bricks in both slots (the second slot's per-brick scales) and a view
+    that changes mid-sequence (frames 0-2 one camera, 3-5 another, while the other slot is in flight);
+    after every call the caller overwrites its transfer function on the same stream, which the frame
+    must not see.  Every image equals s3r_frame_run's from device buffers, bit for bit."""
+    import torch
+    from revise_gb300 import host
+    from revise_gb300.api import FramePlan
+    w = workloads.small(seed=23, level=1, depths=(2, 3, 4), W=80, H=64)
+    views = [host.view_for(w), host.view_for(w, eye=(3.0, 12.0, 30.0))]
+    plan = FramePlan(ctx, w, fmt, tile_cells=8)
+    tf0 = np.ascontiguousarray(w.tf)
+    rng = np.random.default_rng(5)
+    frames = [(w.sparse * np.float32(1 + 0.1 * k) + np.float32(rng.normal())).astype(np.float32) for k in range(6)]
+    frames = [np.where(w.sparse == np.float32(1e30), np.float32(1e30), f).astype(np.float32) for f in frames]
+    vsel = [0, 0, 0, 1, 1, 1]
+    want = []
+    tf_dev = torch.from_numpy(tf0).cuda()
+    for f, vi in zip(frames, vsel):
+        argb = torch.zeros(w.W * w.H, dtype=torch.int32, device="cuda")
+        plan.run(views[vi], torch.from_numpy(f).cuda(), tf_dev, None, argb)
+        want.append(argb.cpu().numpy())
+    hosts = [torch.from_numpy(f).pin_memory() for f in frames]
+    imgs = [torch.zeros(w.W * w.H, dtype=torch.int32).pin_memory() for _ in frames]
+    tf_work = torch.from_numpy(tf0).cuda()
+    garbage = torch.from_numpy(np.full_like(tf0, 0.5)).cuda()
+    for f, im, vi in zip(hosts, imgs, vsel):
+        tf_work.copy_(torch.from_numpy(tf0).cuda())
+        plan.run_host(views[vi], f, tf_work, im)
+        tf_work.copy_(garbage)  # queued on the same stream after the call: the frame keeps the old table
+    plan.host_sync()
+    for k in range(len(frames)):
+        assert np.array_equal(imgs[k].numpy(), want[k]), k
+    assert len({x.tobytes() for x in want}) == len(want)
+    plan.close()
