@@ -194,8 +194,8 @@ def _frame_args(w, dense, rects):
     return blocks, off, dense, rects, rp
 
 
-def render_frame_f64(view: OrcView, w, dense: np.ndarray, rects, tf: np.ndarray, pixels=None):
-    """FP64 frame render: (np, 4) float32 RGBA and (np,) near-threshold flags."""
+def render_frame_f64(view: OrcView, w, dense: np.ndarray, rects, tf: np.ndarray, pixels=None, f64: bool = False):
+    """FP64 frame render: (np, 4) RGBA (float32, or float64 with f64) and (np,) near-threshold flags."""
     blocks, off, dense, rects, rp = _frame_args(w, dense, rects)
     tf = np.ascontiguousarray(tf, dtype=np.float32)
     if pixels is None:
@@ -205,11 +205,11 @@ def render_frame_f64(view: OrcView, w, dense: np.ndarray, rects, tf: np.ndarray,
         pixels = np.ascontiguousarray(pixels, dtype=np.uint32)
         npx = pixels.shape[0]
         pp = _p(pixels, C.c_uint32)
-    out = np.zeros((npx, 4), dtype=np.float32)
+    out = np.zeros((npx, 4), dtype=np.float64 if f64 else np.float32)
     flags = np.zeros(npx, dtype=np.uint8)
-    port().orc_render_frame_f64(C.byref(view), C.c_uint32(blocks.shape[0]), _p(blocks, C.c_uint32),
-                                _p(off, C.c_uint64), _p(dense, C.c_float), rp, _p(tf, C.c_float), C.c_uint32(npx),
-                                pp, _p(out, C.c_float), _p(flags, C.c_uint8))
+    fn = port().orc_render_frame_f64d if f64 else port().orc_render_frame_f64
+    fn(C.byref(view), C.c_uint32(blocks.shape[0]), _p(blocks, C.c_uint32), _p(off, C.c_uint64), _p(dense, C.c_float),
+       rp, _p(tf, C.c_float), C.c_uint32(npx), pp, _p(out, C.c_double if f64 else C.c_float), _p(flags, C.c_uint8))
     return out, flags
 
 

@@ -991,9 +991,10 @@ static void march_block_f64(const orc_view* v, const orc_ray* r, const float* br
     }
 }
 
-void orc_render_frame_f64(const orc_view* v, uint32_t nb, const uint32_t* blocks, const uint64_t* dense_off,
-                          const float* dense, const int32_t* rects, const float* tf, uint32_t np,
-                          const uint32_t* pixels, float* rgba_out, uint8_t* flags_out)
+/* The FP64 frame, per pixel non-premultiplied RGBA; rgba_out (float) and/or rgba64_out (double) receive it. */
+static void render_frame_f64_any(const orc_view* v, uint32_t nb, const uint32_t* blocks, const uint64_t* dense_off,
+                                 const float* dense, const int32_t* rects, const float* tf, uint32_t np,
+                                 const uint32_t* pixels, float* rgba_out, double* rgba64_out, uint8_t* flags_out)
 {
     hit* hits = (hit*)malloc(sizeof(hit) * (nb ? nb : 1));
     uint64_t total = pixels ? np : (uint64_t)v->W * v->H;
@@ -1012,12 +1013,30 @@ void orc_render_frame_f64(const orc_view* v, uint32_t nb, const uint32_t* blocks
             for (int ch = 0; ch < 3; ++ch) acc.C[ch] += T * blk.C[ch];
             acc.A += T * blk.A;
         }
-        float* o = rgba_out + 4 * p;
-        for (int ch = 0; ch < 3; ++ch) o[ch] = acc.A > 0 ? (float)(acc.C[ch] / acc.A) : 0.f;
-        o[3] = (float)acc.A;
+        double o[4];
+        for (int ch = 0; ch < 3; ++ch) o[ch] = acc.A > 0 ? acc.C[ch] / acc.A : 0.0;
+        o[3] = acc.A;
+        for (int ch = 0; ch < 4; ++ch) {
+            if (rgba_out) rgba_out[4 * p + ch] = (float)o[ch];
+            if (rgba64_out) rgba64_out[4 * p + ch] = o[ch];
+        }
         if (flags_out) flags_out[p] = (uint8_t)near;
     }
     free(hits);
+}
+
+void orc_render_frame_f64(const orc_view* v, uint32_t nb, const uint32_t* blocks, const uint64_t* dense_off,
+                          const float* dense, const int32_t* rects, const float* tf, uint32_t np,
+                          const uint32_t* pixels, float* rgba_out, uint8_t* flags_out)
+{
+    render_frame_f64_any(v, nb, blocks, dense_off, dense, rects, tf, np, pixels, rgba_out, NULL, flags_out);
+}
+
+void orc_render_frame_f64d(const orc_view* v, uint32_t nb, const uint32_t* blocks, const uint64_t* dense_off,
+                           const float* dense, const int32_t* rects, const float* tf, uint32_t np,
+                           const uint32_t* pixels, double* rgba_out, uint8_t* flags_out)
+{
+    render_frame_f64_any(v, nb, blocks, dense_off, dense, rects, tf, np, pixels, NULL, rgba_out, flags_out);
 }
 
 void orc_render_frame_argb8(const orc_view* v, uint32_t nb, const uint32_t* blocks, const uint64_t* dense_off,

@@ -112,6 +112,10 @@ void orc_render_block_mode(const orc_view* v, const orc_presentation* pr, const 
 void orc_render_frame_f64(const orc_view* v, uint32_t nb, const uint32_t* blocks, const uint64_t* dense_off,
                           const float* dense, const int32_t* rects, const float* tf, uint32_t np,
                           const uint32_t* pixels, float* rgba_out, uint8_t* flags_out);
+/* orc_render_frame_f64 with the colours kept in double (for finite differences of image losses). */
+void orc_render_frame_f64d(const orc_view* v, uint32_t nb, const uint32_t* blocks, const uint64_t* dense_off,
+                           const float* dense, const int32_t* rects, const float* tf, uint32_t np,
+                           const uint32_t* pixels, double* rgba_out, uint8_t* flags_out);
 
 /* Same march in FP32 with the reference's non-premultiplied per-block compositing followed by
  * ARGB8 read-modify-write per block in back-to-front order: the plain worker path for a whole

@@ -1,6 +1,6 @@
-"""Hand-written adjoint of the batched ray caster: GPU gradient vs the FP64
-oracle gradient (relative error < 1e-3) and central finite differences
-(eps = 1e-3) of the FP64 oracle forward at 64 random coordinates."""
+"""Hand-written adjoint of the batched ray caster on the differentiation configuration (2x2x2 blocks of
+depth 6, 512x512): GPU gradient vs the FP64 oracle gradient (relative error < 1e-3) and vs central finite
+differences (eps = 1e-3) of the FP64 oracle forward at 64 coordinates, each below 1e-3."""
 import numpy as np
 import pytest
 
@@ -47,18 +47,23 @@ def _rects(w, view):
     return np.array([host.block_view_rect(view, w.blocks[b, :3]) for b in range(w.nblocks)], np.int32)
 
 
+def _keep(ov, w, dense, rects):
+    """Pixels where no block-local early-termination test lands within 1e-5 of its threshold (the FP64
+    oracle flags the others): there float and FP64 arithmetic keep the same sample sets."""
+    _, flags = oracle.render_frame_f64(ov, w, dense, rects, w.tf)
+    return flags == 0
+
+
 def test_adjoint_matches_fp64_gradient(ctx):
-    """Pixels where a block-local early-termination test lands within 1e-5 of its
-    threshold (the FP64 oracle flags them) are left out of both gradients: there
-    float and FP64 arithmetic may keep different sample sets."""
-    w = _setup(160, 160)
+    """cfg5 at its full 512x512: the GPU gradients of the loss over the kept pixels against the FP64
+    oracle's gradients of the same loss, relative error (2-norm over all coordinates) below 1e-3."""
+    w = _setup(512, 512)
     view = host.view_for(w)
     ov = oracle.view_from(view)
     dense = oracle.interp_workload(w)
     rects = _rects(w, view)
     target, _ = oracle.render_frame_f64(ov, w, dense, rects, w.meta["target_tf"])
-    _, flags = oracle.render_frame_f64(ov, w, dense, rects, w.tf)
-    keep = flags == 0
+    keep = _keep(ov, w, dense, rects)
     assert keep.mean() > 0.97
     p = np.arange(w.W * w.H)[keep]
     pixels = np.stack([p % w.W, w.H - 1 - p // w.W], 1)
@@ -68,48 +73,90 @@ def test_adjoint_matches_fp64_gradient(ctx):
     e_tf = np.linalg.norm(dtf - dtf64) / np.linalg.norm(dtf64)
     m = ~np.isnan(dense)
     e_dd = np.linalg.norm(dd[m] - dd64[m]) / np.linalg.norm(dd64[m])
+    print(f"adjoint vs FP64 gradient (512x512): transfer function {e_tf:.2e}, dense values {e_dd:.2e}")
     assert e_tf < REL_TOL, e_tf
     assert e_dd < REL_TOL, e_dd
 
 
 def test_adjoint_vs_central_differences(ctx):
-    w = _setup(48, 48)
+    """cfg5 at its full 512x512, loss over the kept pixels: 32 transfer-function entries and 32 dense
+    values, each GPU gradient within 1e-3 relative of the central difference (eps 1e-3) of the FP64
+    oracle's loss -- every one of the 64, no median.  Coordinates are drawn at random among those with a
+    gradient above 1e-3 of the largest and kept only where the loss is smooth across +-eps: the central
+    differences at eps and eps/2 agree to 2e-4 (a kink of the piecewise-linear transfer function or an
+    early-termination switch inside the interval shows up as a disagreement).  The selection uses the
+    oracle alone."""
+    import os
+    from oracle import fd
+    w = _setup(512, 512)
     view = host.view_for(w)
     ov = oracle.view_from(view)
     dense = oracle.interp_workload(w)
     rects = _rects(w, view)
     target, _ = oracle.render_frame_f64(ov, w, dense, rects, w.meta["target_tf"])
-    _, _, dtf, dd = _gpu_grad(ctx, w, target)
-
-    def loss(tf, dn):
-        img, _ = oracle.render_frame_f64(ov, w, dn, rects, tf)
-        return 0.5 * float(((img.astype(np.float64) - target) ** 2).sum())
-
-    rng = np.random.default_rng(64)
+    keep = _keep(ov, w, dense, rects)
+    pool = fd.LossPool(ov, w, dense, rects, w.tf, target, keep, processes=min(16, os.cpu_count() or 1))
+    _, _, dtf, dd = _gpu_grad(ctx, w, target, keep)
+    cam = view.cam
     eps = 1e-3
-    # 32 transfer-function coordinates with nonzero gradient and 32 dense values
-    tf_cand = np.flatnonzero(np.abs(dtf.ravel()) > 1e-3 * np.abs(dtf).max())
-    dn_cand = np.flatnonzero(np.abs(dd) > 1e-3 * np.abs(dd).max())
-    tf_sel = rng.choice(tf_cand, min(32, tf_cand.size), replace=False)
-    dn_sel = rng.choice(dn_cand, 64 - tf_sel.size, replace=False)
-    errs = []
-    for i in tf_sel:
-        p, m = w.tf.copy().ravel(), w.tf.copy().ravel()
-        p[i] += eps
-        m[i] -= eps
-        fd = (loss(p.reshape(-1, 4), dense) - loss(m.reshape(-1, 4), dense)) / (2 * eps)
-        errs.append(abs(fd - dtf.ravel()[i]) / max(abs(fd), 1e-3 * np.abs(dtf).max()))
-    for i in dn_sel:
-        p, m = dense.copy(), dense.copy()
-        p[i] += eps
-        m[i] -= eps
-        fd = (loss(w.tf, p) - loss(w.tf, m)) / (2 * eps)
-        errs.append(abs(fd - dd[i]) / max(abs(fd), 1e-3 * np.abs(dd).max()))
-    errs = np.array(errs)
-    assert len(errs) == 64
-    # piecewise-linear transfer functions put kinks inside some +-eps intervals
-    assert np.median(errs) < REL_TOL, np.sort(errs)
-    assert np.mean(errs < 1e-2) >= 0.9, np.sort(errs)
+    rng = np.random.default_rng(64)
+
+    def fd_pairs(kind, base, idx, pix):
+        """FD at eps and eps/2 for each index (the actual float32 steps as denominators)."""
+        jobs, steps = [], []
+        for i, px in zip(idx, pix):
+            x = np.float32(base[i])
+            row = []
+            for e in (eps, eps / 2):
+                p, m = np.float32(x + np.float32(e)), np.float32(x - np.float32(e))
+                jobs += [(kind, int(i), float(p), px), (kind, int(i), float(m), px)]
+                row.append(float(p) - float(m))
+            steps.append(row)
+        L = pool.losses(jobs)
+        out = []
+        for k, (s1, s2) in enumerate(steps):
+            out.append(((L[4 * k] - L[4 * k + 1]) / s1, (L[4 * k + 2] - L[4 * k + 3]) / s2))
+        return out
+
+    def dense_pixels(i):
+        b = int(np.searchsorted(w.vertex_off, i, side="right") - 1)
+        d = int(w.blocks[b, 3])
+        e = (1 << d) + 1
+        o = i - int(w.vertex_off[b])
+        v = np.array([o % e, (o // e) % e, o // (e * e)], np.float64)
+        c, h = host.block_cube(w.level, w.blocks[b, :3])
+        texel = 2.0 * float(h) / e
+        hh = float(h) + 0.5 * texel
+        lo = np.asarray(c, np.float64) - hh + (v - 0.5) * (2 * hh / e)
+        hi = np.asarray(c, np.float64) - hh + (v + 1.5) * (2 * hh / e)
+        return fd.influence_pixels(cam, w.W, w.H, lo, hi)
+
+    checked = []
+    try:
+        for kind, grad, base, want in (("tf", dtf.ravel(), w.tf.ravel(), 32), ("dense", dd, dense, 32)):
+            cand = np.flatnonzero(np.abs(grad) > 1e-3 * np.abs(grad).max())
+            cand = rng.permutation(cand)
+            got = 0
+            for start in range(0, cand.size, 16):
+                idx = cand[start:start + 16]
+                pix = [None] * idx.size if kind == "tf" else [dense_pixels(int(i)) for i in idx]
+                for i, (f1, f2) in zip(idx, fd_pairs(kind, base, idx, pix)):
+                    if abs(f1) <= 1e-3 * np.abs(grad).max() or abs(f1 - f2) > 2e-4 * abs(f1):
+                        continue  # negligible, or not smooth across the interval
+                    checked.append((kind, int(i), float(grad[i]), f1, abs(grad[i] - f1) / abs(f1)))
+                    got += 1
+                    if got == want:
+                        break
+                if got == want:
+                    break
+            assert got == want, (kind, got)
+    finally:
+        pool.close()
+    errs = np.array([c[4] for c in checked])
+    print(f"adjoint vs central differences (512x512, 64 coordinates): max {errs.max():.2e}, "
+          f"median {np.median(errs):.2e}")
+    assert len(checked) == 64
+    assert errs.max() < REL_TOL, sorted(checked, key=lambda c: -c[4])[:5]
 
 
 def test_autograd_binding_matches_the_adjoint(ctx):

@@ -1,0 +1,125 @@
+"""Parity on the headline configuration: the 4096-block workload (16^3 blocks of octree depth 3-7, 1920x1080)
+that the benchmark times.
+
+* The batched frame as the benchmark runs it (interpolation + ray cast replayed from one CUDA graph, exact
+  filter) against the FP64 oracle on a seeded sample of 2,000 covered pixels and 500 random pixels:
+  2e-3 max absolute per RGBA channel.
+* The per-block drop-in path as the reference's worker runs it (s3r_render_scene_part: per block, back to
+  front, interpolation then the texture-filter ray cast into one ARGB8 viewport) against the image of the
+  reference's own CUDA worker loop (its kernels compiled from its sources, oracle/refcu_harness.cpp) on
+  the same frame: at most 1 LSB per channel, with the share of differing pixels reported.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from oracle import refcu
+from revise_gb300 import _lib, host, workloads
+
+pytestmark = pytest.mark.gpu
+
+TOL_IMAGE = 2e-3
+
+
+@pytest.fixture(scope="module")
+def cfg3():
+    return workloads.cfg3()
+
+
+def _rects(w, view):
+    return np.array([host.block_view_rect(view, w.blocks[b, :3]) for b in range(w.nblocks)], np.int32)
+
+
+def test_cfg3_graph_frame_vs_fp64_oracle(ctx, cfg3):
+    import torch
+    from revise_gb300.api import FramePlan
+    w = cfg3
+    view = host.view_for(w)
+    plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=16)
+    sparse = torch.from_numpy(w.sparse).cuda()
+    tf = torch.from_numpy(np.ascontiguousarray(w.tf)).cuda()
+    plan.autotune(view, sparse, tf, reps=1)
+    rgba = torch.zeros(w.W * w.H * 4, dtype=torch.float32, device="cuda")
+    plan.run(view, sparse, tf, rgba)   # captures the graph
+    rgba.zero_()
+    plan.run(view, sparse, tf, rgba)   # replays it
+    torch.cuda.synchronize()
+    img = rgba.cpu().numpy().reshape(-1, 4)
+    plan.close()
+    hit = np.flatnonzero(img[:, 3] > 0)
+    assert hit.size > 20000
+    rng = np.random.default_rng(7)
+    sel = np.concatenate([rng.choice(hit, 2000, replace=False), rng.choice(img.shape[0], 500, replace=False)])
+    vx = sel % w.W
+    vy = w.H - 1 - sel // w.W
+    ref, flags = oracle.render_frame_f64(oracle.view_from(view), w, oracle.interp_workload(w), _rects(w, view),
+                                         w.tf, np.stack([vx, vy], 1))
+    ok = flags == 0
+    err = np.abs(img[sel] - ref).max(axis=1)
+    print(f"cfg3 frame vs FP64: max {err[ok].max():.2e}, mean {err[ok].mean():.2e}, "
+          f"{(~ok).sum()} of {sel.size} pixels flagged (block termination within 1e-5 of the threshold)")
+    assert ref[:, 3].max() > 0.5
+    assert err[ok].max() <= TOL_IMAGE, err[ok].max()
+    assert ok.mean() > 0.99
+
+
+@pytest.mark.skipif(not refcu.available(), reason="reference CUDA cubins not built here")
+def test_cfg3_worker_texture_path_vs_reference_cuda_worker(ctx, cfg3):
+    import torch
+    from revise_gb300.api import RenderSharedState, VsWorker
+    w = cfg3
+    st = RenderSharedState(w, filter=_lib.FILTER_TEXTURE)
+    wk = VsWorker(ctx)
+    wk.set_render_shared_state(st)
+    m = 1 << w.level
+    origin, size, pixels = wk.render_scene_part_native(w.level, (0, 0, 0), (m, m, m))
+    torch.cuda.synchronize()
+    got = np.zeros((w.H, w.W), np.uint32)
+    if size[0]:
+        got[origin[1]:origin[1] + size[1], origin[0]:origin[0] + size[0]] = \
+            pixels.cpu().numpy().view(np.uint32).reshape(size[1], size[0])
+    view = st.view
+    refcu.set_tf(np.ascontiguousarray(w.tf, np.float32))
+    order = host.b2f_order([0, 0, 0], [m, m, m], [-5.0] * 3, [5.0] * 3, w.eye)
+    where = {tuple(b[:3]): i for i, b in enumerate(w.blocks.tolist())}
+    oi = np.array([where[tuple(b)] for b in order.tolist()])
+    ref, _, _ = refcu.worker(view, w, oi, _rects(w, view))
+    ref = ref.reshape(w.H, w.W)
+    d = np.abs(got.view(np.uint8).reshape(-1, 4).astype(int) - ref.view(np.uint8).reshape(-1, 4).astype(int)).max(1)
+    covered = (ref.ravel() >> 24) > 0
+    print(f"cfg3 worker vs reference CUDA worker: {covered.sum()} covered pixels, max {d.max()} LSB, "
+          f"{(d > 0).sum()} pixels differ ({(d > 0).mean():.2e} of all, "
+          f"{(d[covered] > 0).mean():.2e} of covered); by LSB: {np.bincount(d)[:8].tolist()}")
+    assert covered.mean() > 0.005
+    assert d.max() <= 1, d.max()
+
+
+@pytest.mark.parametrize("fmt", [_lib.BRICK_F32, _lib.BRICK_F16, _lib.BRICK_BF16])
+def test_cfg4_brick_precision_vs_fp64(ctx, fmt):
+    """The precision configuration: the cfg2 workload (64 blocks of depth 6, 1920x1080) with bricks stored
+    as FP32, FP16 or BF16 (per-brick FP32 scale and offset), sampled and composited in FP32, against the
+    FP64 oracle on 2,000 covered and 500 random pixels: max and mean absolute RGBA error.  FP32 bricks meet
+    the 2e-3 image tolerance; the 16-bit bounds are the measured errors with a margin (their quantization
+    step is 2^-11 (FP16) and 2^-8 (BF16) of each brick's value range)."""
+    import torch
+    from revise_gb300.api import FramePlan
+    w = workloads.cfg2()
+    view = host.view_for(w)
+    plan = FramePlan(ctx, w, fmt, tile_cells=16)
+    rgba = torch.zeros(w.W * w.H * 4, dtype=torch.float32, device="cuda")
+    plan.run(view, torch.from_numpy(w.sparse).cuda(), torch.from_numpy(np.ascontiguousarray(w.tf)).cuda(), rgba)
+    torch.cuda.synchronize()
+    img = rgba.cpu().numpy().reshape(-1, 4)
+    plan.close()
+    hit = np.flatnonzero(img[:, 3] > 0)
+    rng = np.random.default_rng(11)
+    sel = np.concatenate([rng.choice(hit, 2000, replace=False), rng.choice(img.shape[0], 500, replace=False)])
+    ref, flags = oracle.render_frame_f64(oracle.view_from(view), w, oracle.interp_workload(w), _rects(w, view),
+                                         w.tf, np.stack([sel % w.W, w.H - 1 - sel // w.W], 1))
+    ok = flags == 0
+    err = np.abs(img[sel] - ref)[ok]
+    name = {_lib.BRICK_F32: "FP32", _lib.BRICK_F16: "FP16", _lib.BRICK_BF16: "BF16"}[fmt]
+    print(f"cfg4 {name} bricks vs FP64: max {err.max():.3e}, mean {err.mean():.3e} (RGBA, {ok.sum()} pixels)")
+    bound = {_lib.BRICK_F32: TOL_IMAGE, _lib.BRICK_F16: 1e-2, _lib.BRICK_BF16: 5e-2}[fmt]
+    assert err.max() <= bound, err.max()
+    assert ok.mean() > 0.99
