@@ -599,6 +599,7 @@ def measure_modes(ctx, torch, np, with_reference: bool):
         a, c = int(w.node_off[b]), int(w.node_off[b + 1])
         x = w.n2i[a:c].astype(np.float64) / (1 << int(w.blocks[b, 3])) + w.blocks[b, :3]
         u[a:c] = (0.25 * x[:, 0] + 0.2 * x[:, 1] + 0.1 * x[:, 2]).astype(np.float32)
+    texs, texs2 = {}, {}
     for b in range(w.nblocks):
         n2i, sp = w.block_nodes(b)
         d = int(w.blocks[b, 3])
@@ -606,6 +607,11 @@ def measure_modes(ctx, torch, np, with_reference: bool):
         dense[b] = ctx.interp_dense(dn, torch.from_numpy(np.ascontiguousarray(sp)).cuda(), d)
         a, c = int(w.node_off[b]), int(w.node_off[b + 1])
         dense2[b] = ctx.interp_dense(dn, torch.from_numpy(np.ascontiguousarray(u[a:c])).cuda(), d)
+        # the same fields as textures (the reference keeps a block's field in a texture)
+        texs[b], texs2[b] = ctx.texture(d), ctx.texture(d)
+        texs[b].fill(dense[b])
+        texs2[b].fill(dense2[b])
+    tf_tex = ctx.tf_texture(tf)
     refcu = None
     if with_reference:
         try:
@@ -615,9 +621,12 @@ def measure_modes(ctx, torch, np, with_reference: bool):
                 refcu.set_tf(np.ascontiguousarray(w.tf, np.float32))
         except Exception:
             refcu = None
-    out = {"workload": "cfg2: 4x4x4 blocks of depth 6 (17.6 M dense vertices), 1920x1080, texture filter, "
-                       "64 render launches back to front, interpolation excluded; batched_ms: the whole frame "
-                       "in one s3r_frame_render_mode launch (exact filter, FP32 compositing) on resident bricks"}
+    out = {"workload": "cfg2: 4x4x4 blocks of depth 6 (17.6 M dense vertices), 1920x1080, 64 render launches "
+                       "back to front, interpolation excluded; ms: s3r_render_block_texture (fields and transfer "
+                       "function in textures, sampled by the texture unit as the reference samples); "
+                       "ms_software_texture_filter / ms_exact_filter: s3r_render_block on linear bricks; batched_ms: "
+                       "the whole frame in one s3r_frame_render_mode launch (exact filter, FP32 compositing) on "
+                       "resident bricks"}
     from revise_gb300.api import FramePlan
     plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=16)
     plan.interp(torch.from_numpy(w.sparse).cuda())
@@ -655,7 +664,22 @@ def measure_modes(ctx, torch, np, with_reference: bool):
             return sum(x.elapsed_time(y) for x, y in evs)
 
         frame()
-        ours = statistics.median([frame() for _ in range(3)])
+        ours_sw = statistics.median([frame() for _ in range(3)])
+
+        def frame_tex():
+            evs = []
+            for b in oi:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                ctx.render_block_texture(view, pres, texs[b], [int(x) for x in w.blocks[b, :3]], rects[b], tf_tex, vp,
+                                         tex2=texs2[b] if two else None)
+                e1.record()
+                evs.append((e0, e1))
+            torch.cuda.synchronize()
+            return sum(x.elapsed_time(y) for x, y in evs)
+
+        frame_tex()
+        ours = statistics.median([frame_tex() for _ in range(3)])
         view.filter = _lib.FILTER_EXACT
         frame()
         ours_exact = statistics.median([frame() for _ in range(3)])
@@ -673,7 +697,7 @@ def measure_modes(ctx, torch, np, with_reference: bool):
         batched()
         bms = statistics.median([batched() for _ in range(5)])
         view.filter = _lib.FILTER_TEXTURE
-        rec = {"ms": ours, "ms_exact_filter": ours_exact, "batched_ms": bms}
+        rec = {"ms": ours, "ms_software_texture_filter": ours_sw, "ms_exact_filter": ours_exact, "batched_ms": bms}
         if refcu is not None:
             try:
                 rms = statistics.median([refcu.time_render(view, pres, w, oi, rects, u if two else None, clear)[0]

@@ -58,7 +58,7 @@
 extern "C" {
 #endif
 
-#define S3R_ABI_VERSION 5
+#define S3R_ABI_VERSION 6
 
 /* status codes */
 #define S3R_OK 0
@@ -245,6 +245,40 @@ int s3r_render_block(s3r_ctx* ctx, const s3r_view* view, const s3r_presentation*
                      const float* brick2, uint32_t depth, const uint32_t idx[3], const int32_t rect[4],
                      const float* tf, uint32_t* viewport, void* stream);
 
+/* ------------------------------------------------- texture-unit block render
+ *
+ * The reference samples a block's dense field and the transfer function through the GPU's texture unit
+ * (tex3D on a 3-D float array with linear filtering and clamp addressing, tex1D on a one-row RGBA array;
+ * DenseFieldRenderer_cu.cu:503-586, RenderFuncInput.hpp:42-50, renderArgb.hpp:44).  These calls do the
+ * same, so that their images are the reference's: the per-block drop-in for renderDenseField and the
+ * worker loop (s3r_render_scene_part with S3R_FILTER_TEXTURE). */
+
+typedef struct s3r_texture s3r_texture;       /* a block's dense field, (2^depth+1)^3 texels */
+typedef struct s3r_tf_texture s3r_tf_texture; /* a transfer function, tf_n RGBA texels */
+
+/* A field texture for blocks of this depth (Device3DArray + DeviceTextureObject; allocates). */
+int s3r_texture_create(s3r_ctx* ctx, uint32_t depth, s3r_texture** out);
+int s3r_texture_destroy(s3r_texture* tex);
+/* Copies a dense grid (device, (2^depth+1)^3 floats in the s3r_interp_dense layout) into the texture. */
+int s3r_texture_fill(s3r_ctx* ctx, s3r_texture* tex, const float* dense, void* stream);
+/* s3r_interp_dense into the texture (DeviceField::makeField, DenseFieldRenderer_cu.cu:505-546): the grid
+ * is interpolated into a context-owned linear grid (grown on demand) and copied into the array. */
+int s3r_interp_dense_texture(s3r_ctx* ctx, const uint16_t* n2i_xyz, const float* sparse, uint32_t n,
+                             s3r_texture* tex, void* stream);
+/* A transfer-function texture of tf_n entries (makeColorTransferTexture, DenseFieldRenderer_cu.cu:566-586:
+ * one row of RGBA floats, normalized coordinates, linear filtering, clamp; allocates). */
+int s3r_tf_texture_create(s3r_ctx* ctx, uint32_t tf_n, s3r_tf_texture** out);
+/* Copies tf (device, tf_n RGBA floats) into the texture. */
+int s3r_tf_texture_set(s3r_ctx* ctx, s3r_tf_texture* tex, const float* tf, void* stream);
+int s3r_tf_texture_destroy(s3r_tf_texture* tex);
+/* renderDenseField's kernel launch (renderKernel<mode>, DenseFieldRenderer_cu.cu:62-215, 447-483) for one
+ * block sampled through the texture unit: s3r_render_block's arithmetic with tex3D / tex1D fetches and the
+ * reference's ray set-up.  pres NULL: Argb.  field2: the secondary field (value-on-isosurface modes), same
+ * depth.  tf->tf_n must equal view->tf_n; view->filter is not consulted. */
+int s3r_render_block_texture(s3r_ctx* ctx, const s3r_view* view, const s3r_presentation* pres,
+                             const s3r_texture* field, const s3r_texture* field2, const uint32_t idx[3],
+                             const int32_t rect[4], const s3r_tf_texture* tf, uint32_t* viewport, void* stream);
+
 /* ----------------------------------------------------------- ordering */
 
 /* Back-to-front order of the blocks of index box [bmin, bmax) whose world box
@@ -317,7 +351,9 @@ typedef struct s3r_worker_blocks {
  * the box's blocks visited back to front for the view's eye (BackToFrontOrder over the box, blocks missing
  * from wb skipped), each block's dense field interpolated from its nodes into the context's scratch
  * (s3r_interp_dense; the secondary field too for the value-on-isosurface modes) and ray-cast into the
- * viewport (s3r_render_block, or s3r_render_block_argb when pres is NULL); then rect = the bounding
+ * viewport (s3r_render_block, or s3r_render_block_argb when pres is NULL) -- with S3R_FILTER_TEXTURE into
+ * context-owned field textures per depth and a transfer-function texture filled from tf at the start of the
+ * call (s3r_interp_dense_texture, s3r_render_block_texture), as the reference samples; then rect = the bounding
  * rectangle of the non-transparent pixels (s3r_bound_rect; {0,0,0,0} when empty) -- the part s3r_crop
  * cuts out.  Allocates the scratch on the first call for a depth; synchronizes the stream at the end. */
 int s3r_render_scene_part(s3r_ctx* ctx, const s3r_view* view, const s3r_presentation* pres,

@@ -22,7 +22,7 @@ MAX_DEPTH = 9
 
 BRICK_F32, BRICK_F16, BRICK_BF16 = 0, 1, 2
 FILTER_EXACT, FILTER_TEXTURE = 0, 1
-ABI_VERSION = 5
+ABI_VERSION = 6
 
 u8p = C.POINTER(C.c_uint8)
 u16p = C.POINTER(C.c_uint16)
@@ -112,6 +112,15 @@ _SIGS = {
     "s3r_block_view_rect": (C.c_int, [C.POINTER(View), u32p, i32p]),
     "s3r_clear_viewport": (C.c_int, [vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, vp]),
     "s3r_render_block_argb": (C.c_int, [vp, C.POINTER(View), vp, C.c_uint32, u32p, i32p, vp, vp, vp]),
+    "s3r_texture_create": (C.c_int, [vp, C.c_uint32, C.POINTER(vp)]),
+    "s3r_texture_destroy": (C.c_int, [vp]),
+    "s3r_texture_fill": (C.c_int, [vp, vp, vp, vp]),
+    "s3r_interp_dense_texture": (C.c_int, [vp, vp, vp, C.c_uint32, vp, vp]),
+    "s3r_tf_texture_create": (C.c_int, [vp, C.c_uint32, C.POINTER(vp)]),
+    "s3r_tf_texture_set": (C.c_int, [vp, vp, vp, vp]),
+    "s3r_tf_texture_destroy": (C.c_int, [vp]),
+    "s3r_render_block_texture": (C.c_int, [vp, C.POINTER(View), C.POINTER(Presentation), vp, vp, u32p, i32p, vp, vp,
+                                           vp]),
     "s3r_render_block": (C.c_int, [vp, C.POINTER(View), C.POINTER(Presentation), vp, vp, C.c_uint32, u32p, i32p, vp,
                                    vp, vp]),
     "s3r_default_light": (C.c_int, [C.POINTER(View), C.POINTER(Light)]),

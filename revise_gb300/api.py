@@ -121,6 +121,28 @@ class Context:
         self._check(self.lib.s3r_render_block(self.h, C.byref(view), C.byref(pres), ptr(brick), ptr(brick2), depth,
                                               i, r, ptr(tf_dev), ptr(viewport), _stream(stream)))
 
+    # -- texture-unit render ----------------------------------------------
+    def texture(self, depth: int) -> "FieldTexture":
+        return FieldTexture(self, depth)
+
+    def tf_texture(self, tf_dev, stream=None) -> "TfTexture":
+        t = TfTexture(self, int(tf_dev.numel()) // 4)
+        t.set(tf_dev, stream)
+        return t
+
+    def interp_dense_texture(self, n2i_dev, sparse_dev, tex: "FieldTexture", stream=None):
+        self._check(self.lib.s3r_interp_dense_texture(self.h, ptr(n2i_dev), ptr(sparse_dev), int(sparse_dev.numel()),
+                                                      tex.h, _stream(stream)))
+
+    def render_block_texture(self, view: View, pres, tex: "FieldTexture", idx, rect, tf: "TfTexture", viewport,
+                             tex2: "FieldTexture" = None, stream=None):
+        """One block in any field mode (pres None: Argb) sampled through the texture unit."""
+        i = (C.c_uint32 * 3)(*[int(x) for x in idx])
+        r = (C.c_int32 * 4)(*[int(x) for x in rect])
+        self._check(self.lib.s3r_render_block_texture(self.h, C.byref(view), C.byref(pres) if pres is not None else None,
+                                                      tex.h, tex2.h if tex2 is not None else None, i, r, tf.h,
+                                                      ptr(viewport), _stream(stream)))
+
     def bound_rect(self, viewport, W: int, H: int, stream=None):
         r = (C.c_int32 * 4)()
         self._check(self.lib.s3r_bound_rect(self.h, ptr(viewport), W, H, r, _stream(stream)))
@@ -295,20 +317,75 @@ class FramePlan:
                                                           _stream(stream)))
 
 
+class FieldTexture:
+    """A block's dense field as a 3-D texture (s3r_texture): fill it from a dense grid or interpolate into it."""
+
+    def __init__(self, ctx: Context, depth: int):
+        self.ctx = ctx
+        self.depth = depth
+        h = C.c_void_p()
+        ctx._check(ctx.lib.s3r_texture_create(ctx.h, depth, C.byref(h)))
+        self.h = h
+
+    def fill(self, dense_dev, stream=None):
+        self.ctx._check(self.ctx.lib.s3r_texture_fill(self.ctx.h, self.h, ptr(dense_dev), _stream(stream)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.s3r_texture_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class TfTexture:
+    """A transfer function as a one-row RGBA texture (s3r_tf_texture)."""
+
+    def __init__(self, ctx: Context, tf_n: int):
+        self.ctx = ctx
+        self.n = tf_n
+        h = C.c_void_p()
+        ctx._check(ctx.lib.s3r_tf_texture_create(ctx.h, tf_n, C.byref(h)))
+        self.h = h
+
+    def set(self, tf_dev, stream=None):
+        self.ctx._check(self.ctx.lib.s3r_tf_texture_set(self.ctx.h, self.h, ptr(tf_dev), _stream(stream)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.s3r_tf_texture_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class DenseFieldRenderer:
     """DenseFieldRenderer_cu for the Argb mode: interpolates one block's dense
     field (DeviceField::makeField, DenseFieldRenderer_cu.cu:504-545) and ray-casts
-    it into a device ARGB32 viewport (renderDenseField, :279-486)."""
+    it into a device ARGB32 viewport (renderDenseField, :279-486).  With the texture
+    filter (the reference's sampling) the field goes into a texture per depth and the
+    transfer function into a colour texture, as the reference keeps them."""
 
     def __init__(self, ctx: Context):
         self.ctx = ctx
         self.state = None
         self._dense = None
         self._tf = None
+        self._tex = {}
+        self._tf_tex = None
 
     def set_render_shared_state(self, state: "RenderSharedState"):
         self.state = state
         self._tf = None
+        self._tf_tex = None
 
     def clear_viewport(self, viewport):
         s = self.state
@@ -320,15 +397,26 @@ class DenseFieldRenderer:
         b = s.block_index[(int(index[0]), int(index[1]), int(index[2]))]
         depth = int(s.blocks[b, 3])
         n2i_dev, sparse_dev = s.device_nodes(b)
-        self._dense = self.ctx.interp_dense(n2i_dev, sparse_dev, depth, out=None)
         if self._tf is None:
             self._tf = torch.from_numpy(np.ascontiguousarray(s.tf, dtype=np.float32)).cuda()
+        tex = s.view.filter == _lib.FILTER_TEXTURE
+        if tex:
+            if depth not in self._tex:
+                self._tex[depth] = self.ctx.texture(depth)
+            self.ctx.interp_dense_texture(n2i_dev, sparse_dev, self._tex[depth])
+            if self._tf_tex is None:
+                self._tf_tex = self.ctx.tf_texture(self._tf)
+        else:
+            self._dense = self.ctx.interp_dense(n2i_dev, sparse_dev, depth, out=None)
         if cancelled():
             return
         rect = host.block_view_rect(s.view, index)
         if rect[2] == 0 or rect[3] == 0:
             return
-        self.ctx.render_block_argb(s.view, self._dense, depth, index, rect, self._tf, viewport)
+        if tex:
+            self.ctx.render_block_texture(s.view, None, self._tex[depth], index, rect, self._tf_tex, viewport)
+        else:
+            self.ctx.render_block_argb(s.view, self._dense, depth, index, rect, self._tf, viewport)
 
 
 class RenderSharedState:

@@ -37,6 +37,12 @@ struct s3r_ctx {
     cudaStream_t capture = nullptr;
     float* worker_dense[2] = {nullptr, nullptr}; // s3r_render_scene_part: primary / secondary dense field
     size_t worker_cap[2] = {0, 0};
+    // s3r_render_scene_part with the texture filter: per depth a primary / secondary field texture, the
+    // transfer-function texture, and the linear grid s3r_interp_dense_texture interpolates into
+    s3r_texture* worker_tex[2][S3R_MAX_DEPTH + 1] = {};
+    s3r_tf_texture* worker_tf = nullptr;
+    float* tex_stage = nullptr;
+    size_t tex_stage_cap = 0;
     uint64_t launches = 0;
     int sms = 152;
 };
@@ -106,6 +112,25 @@ struct s3r_plan {
     cudaStream_t hs_comp[2] = {nullptr, nullptr}; // one compute stream per slot: frames k and k+1 overlap
     cudaEvent_t hs_copied[2] = {nullptr, nullptr}, hs_rendered[2] = {nullptr, nullptr}, hs_read[2] = {nullptr, nullptr};
     cudaEvent_t hs_entry = nullptr; // work queued on the caller's stream before a frame
+};
+
+// A block's dense field as the reference holds it for rendering (DeviceField, DenseFieldRenderer_cu.cu:503-560):
+// a 3-D float array with a texture object over it (unnormalized coordinates, linear filtering, clamp).
+struct s3r_texture {
+    s3r_ctx* ctx = nullptr;
+    uint32_t depth = 0, n = 0;
+    cudaArray_t array = nullptr;
+    cudaTextureObject_t tex = 0;
+};
+
+// The transfer function as the reference's colour texture (makeColorTransferTexture,
+// DenseFieldRenderer_cu.cu:566-586): one row of RGBA floats, normalized coordinates, linear filtering,
+// clamp along x.
+struct s3r_tf_texture {
+    s3r_ctx* ctx = nullptr;
+    uint32_t n = 0;
+    cudaArray_t array = nullptr;
+    cudaTextureObject_t tex = 0;
 };
 
 void s3r::set_thread_error(const char* msg) { g_last_error = msg; }
@@ -814,6 +839,10 @@ int s3r_ctx_destroy(s3r_ctx* ctx)
     if (ctx->capture) cudaStreamDestroy(ctx->capture);
     for (float* d : ctx->worker_dense)
         if (d) cudaFree(d);
+    for (auto& per_field : ctx->worker_tex)
+        for (s3r_texture* t : per_field) s3r_texture_destroy(t);
+    s3r_tf_texture_destroy(ctx->worker_tf);
+    if (ctx->tex_stage) cudaFree(ctx->tex_stage);
     delete ctx;
     return S3R_OK;
 }
@@ -1101,6 +1130,179 @@ int s3r_render_block(s3r_ctx* ctx, const s3r_view* view, const s3r_presentation*
                      const float* tf, uint32_t* viewport, void* stream)
 {
     return render_block_pitched(ctx, view, pres, brick, brick2, depth, 0, idx, rect, tf, viewport, stream);
+}
+
+// ------------------------------------------------------------------ texture-unit path
+
+int s3r_texture_create(s3r_ctx* ctx, uint32_t depth, s3r_texture** out)
+{
+    if (!ctx || !out) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (depth > S3R_MAX_DEPTH) return fail(ctx, S3R_ERR_INVALID, "depth exceeds S3R_MAX_DEPTH");
+    int rc = set_device(ctx);
+    if (rc) return rc;
+    auto* t = new (std::nothrow) s3r_texture;
+    if (!t) return fail(ctx, S3R_ERR_NOMEM, "out of host memory");
+    t->ctx = ctx;
+    t->depth = depth;
+    t->n = (1u << depth) + 1u;
+    const cudaChannelFormatDesc desc = cudaCreateChannelDesc(32, 0, 0, 0, cudaChannelFormatKindFloat);
+    cudaError_t e = cudaMalloc3DArray(&t->array, &desc, make_cudaExtent(t->n, t->n, t->n), cudaArraySurfaceLoadStore);
+    if (e == cudaSuccess) {
+        cudaResourceDesc res;
+        std::memset(&res, 0, sizeof(res));
+        res.resType = cudaResourceTypeArray;
+        res.res.array.array = t->array;
+        cudaTextureDesc td;
+        std::memset(&td, 0, sizeof(td));
+        td.normalizedCoords = 0;
+        td.filterMode = cudaFilterModeLinear;
+        td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;
+        td.readMode = cudaReadModeElementType;
+        e = cudaCreateTextureObject(&t->tex, &res, &td, nullptr);
+    }
+    if (e != cudaSuccess) {
+        s3r_texture_destroy(t);
+        return cuda_fail(ctx, e, "field texture");
+    }
+    *out = t;
+    return S3R_OK;
+}
+
+int s3r_texture_destroy(s3r_texture* t)
+{
+    if (!t) return S3R_OK;
+    if (t->ctx) cudaSetDevice(t->ctx->device);
+    if (t->tex) cudaDestroyTextureObject(t->tex);
+    if (t->array) cudaFreeArray(t->array);
+    delete t;
+    return S3R_OK;
+}
+
+int s3r_texture_fill(s3r_ctx* ctx, s3r_texture* t, const float* dense, void* stream)
+{
+    if (!ctx || !t || !dense) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (t->ctx != ctx) return fail(ctx, S3R_ERR_INVALID, "texture belongs to another context");
+    int rc = set_device(ctx);
+    if (rc) return rc;
+    cudaMemcpy3DParms p;
+    std::memset(&p, 0, sizeof(p));
+    p.srcPtr = make_cudaPitchedPtr(const_cast<float*>(dense), t->n * sizeof(float), t->n, t->n);
+    p.dstArray = t->array;
+    p.extent = make_cudaExtent(t->n, t->n, t->n);
+    p.kind = cudaMemcpyDeviceToDevice;
+    S3R_CUDA(ctx, cudaMemcpy3DAsync(&p, as_stream(stream)));
+    return S3R_OK;
+}
+
+int s3r_interp_dense_texture(s3r_ctx* ctx, const uint16_t* n2i_xyz, const float* sparse, uint32_t n, s3r_texture* t,
+                             void* stream)
+{
+    if (!ctx || !t) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (t->ctx != ctx) return fail(ctx, S3R_ERR_INVALID, "texture belongs to another context");
+    int rc = set_device(ctx);
+    if (rc) return rc;
+    const uint64_t count = (uint64_t)t->n * t->n * t->n;
+    if (ctx->tex_stage_cap < count) {
+        if (ctx->tex_stage) cudaFree(ctx->tex_stage);
+        ctx->tex_stage = nullptr;
+        ctx->tex_stage_cap = 0;
+        S3R_CUDA(ctx, cudaMalloc(&ctx->tex_stage, count * sizeof(float)));
+        ctx->tex_stage_cap = count;
+    }
+    if ((rc = s3r_interp_dense(ctx, n2i_xyz, sparse, n, t->depth, ctx->tex_stage, stream))) return rc;
+    return s3r_texture_fill(ctx, t, ctx->tex_stage, stream);
+}
+
+int s3r_tf_texture_create(s3r_ctx* ctx, uint32_t tf_n, s3r_tf_texture** out)
+{
+    if (!ctx || !out) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (tf_n < 2 || tf_n > 4096) return fail(ctx, S3R_ERR_INVALID, "tf_n must be in [2, 4096]");
+    int rc = set_device(ctx);
+    if (rc) return rc;
+    auto* t = new (std::nothrow) s3r_tf_texture;
+    if (!t) return fail(ctx, S3R_ERR_NOMEM, "out of host memory");
+    t->ctx = ctx;
+    t->n = tf_n;
+    const cudaChannelFormatDesc desc = cudaCreateChannelDesc(32, 32, 32, 32, cudaChannelFormatKindFloat);
+    cudaError_t e = cudaMallocArray(&t->array, &desc, tf_n, 1, cudaArrayTextureGather);
+    if (e == cudaSuccess) {
+        cudaResourceDesc res;
+        std::memset(&res, 0, sizeof(res));
+        res.resType = cudaResourceTypeArray;
+        res.res.array.array = t->array;
+        cudaTextureDesc td;
+        std::memset(&td, 0, sizeof(td));
+        td.normalizedCoords = 1;
+        td.filterMode = cudaFilterModeLinear;
+        td.addressMode[0] = cudaAddressModeClamp;
+        td.readMode = cudaReadModeElementType;
+        e = cudaCreateTextureObject(&t->tex, &res, &td, nullptr);
+    }
+    if (e != cudaSuccess) {
+        s3r_tf_texture_destroy(t);
+        return cuda_fail(ctx, e, "transfer-function texture");
+    }
+    *out = t;
+    return S3R_OK;
+}
+
+int s3r_tf_texture_set(s3r_ctx* ctx, s3r_tf_texture* t, const float* tf, void* stream)
+{
+    if (!ctx || !t || !tf) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (t->ctx != ctx) return fail(ctx, S3R_ERR_INVALID, "texture belongs to another context");
+    int rc = set_device(ctx);
+    if (rc) return rc;
+    const size_t row = (size_t)t->n * 4 * sizeof(float);
+    S3R_CUDA(ctx, cudaMemcpy2DToArrayAsync(t->array, 0, 0, tf, row, row, 1, cudaMemcpyDeviceToDevice,
+                                           as_stream(stream)));
+    return S3R_OK;
+}
+
+int s3r_tf_texture_destroy(s3r_tf_texture* t)
+{
+    if (!t) return S3R_OK;
+    if (t->ctx) cudaSetDevice(t->ctx->device);
+    if (t->tex) cudaDestroyTextureObject(t->tex);
+    if (t->array) cudaFreeArray(t->array);
+    delete t;
+    return S3R_OK;
+}
+
+int s3r_render_block_texture(s3r_ctx* ctx, const s3r_view* view, const s3r_presentation* pres,
+                             const s3r_texture* field, const s3r_texture* field2, const uint32_t idx[3],
+                             const int32_t rect[4], const s3r_tf_texture* tf, uint32_t* viewport, void* stream)
+{
+    if (!ctx) return fail(nullptr, S3R_ERR_INVALID, "ctx is null");
+    int rc = check_view(ctx, view);
+    if (rc) return rc;
+    if (!field || !idx || !rect || !tf || !viewport) return fail(ctx, S3R_ERR_INVALID, "null pointer");
+    if (field->ctx != ctx || tf->ctx != ctx || (field2 && field2->ctx != ctx))
+        return fail(ctx, S3R_ERR_INVALID, "texture belongs to another context");
+    if (tf->n != view->tf_n) return fail(ctx, S3R_ERR_INVALID, "transfer-function texture size differs from tf_n");
+    s3r_presentation argb{};
+    argb.mode = S3R_MODE_ARGB;
+    const s3r_presentation* pr = pres ? pres : &argb;
+    if (pr->mode > S3R_MODE_VALUE_ON_ISOSURFACES) return fail(ctx, S3R_ERR_INVALID, "unknown field mode");
+    if (pr->level_count > S3R_MAX_LEVELS) return fail(ctx, S3R_ERR_INVALID, "more than S3R_MAX_LEVELS levels");
+    if (pr->light_count > S3R_MAX_LIGHTS) return fail(ctx, S3R_ERR_INVALID, "more than S3R_MAX_LIGHTS lights");
+    for (uint32_t i = 1; i < pr->level_count; ++i)
+        if (!(pr->levels[i] > pr->levels[i - 1])) return fail(ctx, S3R_ERR_INVALID, "levels must ascend strictly");
+    const bool secondary = pr->mode == S3R_MODE_VALUE_ON_ISOSURFACE || pr->mode == S3R_MODE_VALUE_ON_ISOSURFACES;
+    if (secondary && (!field2 || field2->depth != field->depth))
+        return fail(ctx, S3R_ERR_INVALID, "this mode needs the secondary field's texture, of the same depth");
+    if (secondary && !(pr->secondary_max > pr->secondary_min))
+        return fail(ctx, S3R_ERR_INVALID, "secondary field range is empty");
+    const uint32_t m = 1u << view->level;
+    if (idx[0] >= m || idx[1] >= m || idx[2] >= m) return fail(ctx, S3R_ERR_INVALID, "block index outside level");
+    if (rect[2] < 0 || rect[3] < 0) return fail(ctx, S3R_ERR_INVALID, "negative view rectangle");
+    if ((rc = set_device(ctx))) return rc;
+    RenderBlock rb{};
+    block_sampling(view->level, idx, field->depth, rb);
+    for (int i = 0; i < 4; ++i) rb.rect[i] = rect[i];
+    S3R_CUDA(ctx, launch_render_block_texture(view, pr, (uint64_t)field->tex, field2 ? (uint64_t)field2->tex : 0,
+                                              (uint64_t)tf->tex, rb, viewport, as_stream(stream)));
+    if (rect[2] > 0 && rect[3] > 0) ++ctx->launches;
+    return S3R_OK;
 }
 
 int s3r_blend_image_part_mip_host(float* dst, int32_t dw, int32_t dh, const float* src, int32_t sw, int32_t sh,
@@ -1804,6 +2006,17 @@ int s3r_render_scene_part(s3r_ctx* ctx, const s3r_view* view, const s3r_presenta
     Split sp[3];
     for (int a = 0; a < 3; ++a)
         sp[a] = split_range(box_min[a], box_max[a], (float)cmin[a], (float)cmax[a], view->cam.eye[a]);
+    // the texture filter samples through the texture unit, as the reference's renderer does: the transfer
+    // function goes into the context's colour texture first
+    const bool tex = view->filter == S3R_FILTER_TEXTURE;
+    if (tex) {
+        if (ctx->worker_tf && ctx->worker_tf->n != view->tf_n) {
+            s3r_tf_texture_destroy(ctx->worker_tf);
+            ctx->worker_tf = nullptr;
+        }
+        if (!ctx->worker_tf && (rc = s3r_tf_texture_create(ctx, view->tf_n, &ctx->worker_tf))) return rc;
+        if ((rc = s3r_tf_texture_set(ctx, ctx->worker_tf, tf, stream))) return rc;
+    }
     std::unordered_map<uint64_t, uint32_t> where;
     where.reserve(wb->nblocks * 2 + 1);
     for (uint32_t b = 0; b < wb->nblocks; ++b) {
@@ -1820,6 +2033,24 @@ int s3r_render_scene_part(s3r_ctx* ctx, const s3r_view* view, const s3r_presenta
             rc = fail(ctx, S3R_ERR_INVALID, "depth exceeds S3R_MAX_DEPTH");
             return;
         }
+        const uint64_t o = wb->node_off[b], n = wb->node_off[b + 1] - o;
+        if (tex) {
+            // DeviceField::makeField: the block's dense field interpolated into the depth's field texture
+            for (int f = 0; f < (secondary ? 2 : 1); ++f) {
+                if (!ctx->worker_tex[f][depth] && (rc = s3r_texture_create(ctx, depth, &ctx->worker_tex[f][depth])))
+                    return;
+                if ((rc = s3r_interp_dense_texture(ctx, wb->n2i + 3 * o, (f ? wb->sparse2 : wb->sparse) + o,
+                                                   (uint32_t)n, ctx->worker_tex[f][depth], stream)))
+                    return;
+            }
+            int32_t r[4];
+            view_rect(*view, wb->blocks + 4 * b, r);
+            if (r[2] <= 0 || r[3] <= 0) return;
+            rc = s3r_render_block_texture(ctx, view, pres, ctx->worker_tex[0][depth],
+                                          secondary ? ctx->worker_tex[1][depth] : nullptr, wb->blocks + 4 * b, r,
+                                          ctx->worker_tf, viewport, stream);
+            return;
+        }
         const uint64_t e = (1ull << depth) + 1, count = e * e * e;
         for (int f = 0; f < (secondary ? 2 : 1); ++f)
             if (ctx->worker_cap[f] < count) {
@@ -1833,7 +2064,6 @@ int s3r_render_scene_part(s3r_ctx* ctx, const s3r_view* view, const s3r_presenta
                 }
                 ctx->worker_cap[f] = count;
             }
-        const uint64_t o = wb->node_off[b], n = wb->node_off[b + 1] - o;
         // DeviceField::makeField: the block's dense field from its nodes
         if ((rc = s3r_interp_dense(ctx, wb->n2i + 3 * o, wb->sparse + o, (uint32_t)n, depth, ctx->worker_dense[0],
                                    stream)))

@@ -477,17 +477,55 @@ __device__ __forceinline__ F3 blinn(F3 N, F3 V, F3 L, const s3r_light& light, F3
     return f3(light.ambient) + kd * f3(light.diffuse) * diff + F3{0.5f, 0.5f, 0.5f} * f3(light.specular) * spec;
 }
 
+// Where a field-mode march takes its samples from.
+//   BrickSampler<kTex>: linear bricks in HBM, filtered in software (kTex: the
+//     texture unit's rule, else exact trilinear); the table in shared memory.
+//   TextureSampler: the GPU's texture unit itself, as the reference samples --
+//     tex3D on a 3-D float array (unnormalized coordinates, linear filtering,
+//     clamp) and tex1D on the transfer-function array (normalized, linear,
+//     clamp).
+// kStepwise: sample positions accumulated step by step from the entry point
+// (pos += step), as the reference forms them, because texture filtering's
+// 8-bit fractions are sensitive to the last ulp of a position; else entry +
+// k * step (one fma), as the oracle and the batched path form them.
+// kContracted: the crossing positions of the isosurface modes written as the
+// reference writes them (pos + step * t, which nvcc fuses into one fma), else
+// rounded twice as the oracle rounds them.
+template <bool kTex> struct BrickSampler {
+    const float* b1;
+    const float* b2;
+    Dim n;
+    const float4* tf;
+    uint32_t tfn;
+    static constexpr bool kStepwise = kTex, kContracted = false;
+    __device__ float field(int second, float x, float y, float z) const
+    {
+        return field_at<kTex>(second ? b2 : b1, n, x, y, z);
+    }
+    __device__ float4 colour(float v01) const { return tf_rgba<kTex>(tf, tfn, v01); }
+};
+
+struct TextureSampler {
+    cudaTextureObject_t t1, t2, tf;
+    static constexpr bool kStepwise = true, kContracted = true;
+    __device__ float field(int second, float x, float y, float z) const
+    {
+        return tex3D<float>(second ? t2 : t1, x, y, z);
+    }
+    __device__ float4 colour(float v01) const { return tex1D<float4>(tf, v01); }
+};
+
 // computeFragColor (cuda_lighting.hpp:52-95): normal from central differences
 // of the field at +-0.1 texel, double-sided lighting, colour clamped to [0, 1].
-template <bool kTex>
-__device__ __forceinline__ float4 frag_color(const float* brick, Dim n, float4 diffuse, F3 eye, F3 surf, F3 tc,
+template <class S>
+__device__ __forceinline__ float4 frag_color(const S& smp, float4 diffuse, F3 eye, F3 surf, F3 tc,
                                              const s3r_presentation& pr)
 {
     constexpr float d = 0.1f;
-    const F3 a{field_at<kTex>(brick, n, tc.x - d, tc.y, tc.z), field_at<kTex>(brick, n, tc.x, tc.y - d, tc.z),
-               field_at<kTex>(brick, n, tc.x, tc.y, tc.z - d)};
-    const F3 b{field_at<kTex>(brick, n, tc.x + d, tc.y, tc.z), field_at<kTex>(brick, n, tc.x, tc.y + d, tc.z),
-               field_at<kTex>(brick, n, tc.x, tc.y, tc.z + d)};
+    const F3 a{smp.field(0, tc.x - d, tc.y, tc.z), smp.field(0, tc.x, tc.y - d, tc.z),
+               smp.field(0, tc.x, tc.y, tc.z - d)};
+    const F3 b{smp.field(0, tc.x + d, tc.y, tc.z), smp.field(0, tc.x, tc.y + d, tc.z),
+               smp.field(0, tc.x, tc.y, tc.z + d)};
     F3 N = normalize3(a - b);
     const F3 V = normalize3(eye - surf);
     F3 c{0.f, 0.f, 0.f};
@@ -555,13 +593,11 @@ struct ModeOut {
 // block's maximum above the threshold; the colour modes (Argb, ArgbLight,
 // DomainVoxels) and the isosurface modes the colour gathered with blendBehind;
 // multi-level modes with no level clear the pixel.
-template <bool kTex>
-__device__ __forceinline__ ModeOut march_block_mode(const s3r_view& v, const s3r_presentation& pr,
-                                                    const float* __restrict__ brick, const float* __restrict__ brick2,
-                                                    const BlockRay& r, uint32_t depth, const float4* tf)
+template <class S>
+__device__ __forceinline__ ModeOut march_block_mode(const s3r_view& v, const s3r_presentation& pr, const S& smp,
+                                                    const BlockRay& r, uint32_t depth)
 {
     ModeOut out{ModeOut::kNone, make_float4(0.f, 0.f, 0.f, 0.f), 0.f};
-    const Dim n = dim_of(r);
     const float span = v.field_max - v.field_min;
     const F3 eye = f3(v.cam.eye);
     const F3 step{r.step[0], r.step[1], r.step[2]};
@@ -573,7 +609,7 @@ __device__ __forceinline__ ModeOut march_block_mode(const s3r_view& v, const s3r
     F3 seq{r.p0[0], r.p0[1], r.p0[2]};
     int seq_k = 0;
     auto pos_of = [&](int k) {
-        if constexpr (kTex) {
+        if constexpr (S::kStepwise) {
             for (; seq_k < k; ++seq_k)
                 seq = F3{__fadd_rn(seq.x, r.step[0]), __fadd_rn(seq.y, r.step[1]), __fadd_rn(seq.z, r.step[2])};
             return seq;
@@ -586,9 +622,9 @@ __device__ __forceinline__ ModeOut march_block_mode(const s3r_view& v, const s3r
         return F3{__fmul_rn(__fsub_rn(p.x, r.origin[0]), r.factor), __fmul_rn(__fsub_rn(p.y, r.origin[1]), r.factor),
                   __fmul_rn(__fsub_rn(p.z, r.origin[2]), r.factor)};
     };
-    auto value = [&](const float* b, F3 p) {
+    auto value = [&](int second, F3 p) {
         const F3 tc = tc_of(p);
-        return field_at<kTex>(b, n, tc.x, tc.y, tc.z);
+        return smp.field(second, tc.x, tc.y, tc.z);
     };
     constexpr float kMax = 0.996f; // AlphaThreshold / AlphaMaxThreshold
     const uint32_t mode = pr.mode;
@@ -596,7 +632,7 @@ __device__ __forceinline__ ModeOut march_block_mode(const s3r_view& v, const s3r
         // renderMaxIntensityProjection.hpp:30-50; the pixel holds float bits
         float maxv = v.field_min - span;
         for (int i = 1; i < r.samples; ++i) {
-            const float val = value(brick, pos_of(i - 1));
+            const float val = value(0, pos_of(i - 1));
             if (val >= v.threshold && maxv < val) maxv = val;
         }
         if (maxv < v.field_min) return out;
@@ -611,23 +647,23 @@ __device__ __forceinline__ ModeOut march_block_mode(const s3r_view& v, const s3r
         float4 dom = make_float4(0.f, 0.f, 0.f, 0.f);
         if (mode == S3R_MODE_DOMAIN_VOXELS) {
             // renderDomainVoxels.hpp:41-42: one colour, the table's middle
-            dom = tf_rgba<kTex>(tf, v.tf_n, 0.5f);
+            dom = smp.colour(0.5f);
             dom.w = 1.f - powf(1.f - dom.w * of, il);
         }
         for (int i = 1; i < r.samples; ++i) {
             const F3 p = pos_of(i - 1);
-            const float val = value(brick, p);
+            const float val = value(0, p);
             if (isnan(val)) continue;
             float4 col;
             if (mode == S3R_MODE_DOMAIN_VOXELS) {
                 col = dom;
             } else {
-                col = tf_rgba<kTex>(tf, v.tf_n, (val - v.field_min) / span);
+                col = smp.colour((val - v.field_min) / span);
                 col.w = 1.f - powf(1.f - col.w * of, il);
                 if (mode == S3R_MODE_ARGB_LIGHT) {
                     // renderArgbLight.hpp:44-56: only visible enough samples are lit
                     if (!(col.w >= 0.00001f)) continue;
-                    col = frag_color<kTex>(brick, n, col, eye, p, tc_of(p), pr);
+                    col = frag_color(smp, col, eye, p, tc_of(p), pr);
                 }
             }
             blend_behind(acc, col);
@@ -649,24 +685,26 @@ __device__ __forceinline__ ModeOut march_block_mode(const s3r_view& v, const s3r
     auto surface_colour = [&](float level, F3 xpos) {
         float4 dif;
         if (secondary) {
-            const float vs = value(brick2, xpos);
-            dif = tf_rgba<kTex>(tf, v.tf_n, (vs - pr.secondary_min) / (pr.secondary_max - pr.secondary_min));
+            const float vs = value(1, xpos);
+            dif = smp.colour((vs - pr.secondary_min) / (pr.secondary_max - pr.secondary_min));
         } else {
-            dif = tf_rgba<kTex>(tf, v.tf_n, (level - v.field_min) / span);
+            dif = smp.colour((level - v.field_min) / span);
         }
         dif.w *= pr.isosurface_opacity;
-        return frag_color<kTex>(brick, n, dif, eye, xpos, tc_of(xpos), pr);
+        return frag_color(smp, dif, eye, xpos, tc_of(xpos), pr);
     };
     auto xpos_of = [&](F3 p, float t) {
-        return F3{__fadd_rn(p.x, __fmul_rn(step.x, t)), __fadd_rn(p.y, __fmul_rn(step.y, t)),
-                  __fadd_rn(p.z, __fmul_rn(step.z, t))};
+        if constexpr (S::kContracted) return F3{p.x + step.x * t, p.y + step.y * t, p.z + step.z * t};
+        else
+            return F3{__fadd_rn(p.x, __fmul_rn(step.x, t)), __fadd_rn(p.y, __fmul_rn(step.y, t)),
+                      __fadd_rn(p.z, __fmul_rn(step.z, t))};
     };
-    float v1 = value(brick, pos_of(0));
+    float v1 = value(0, pos_of(0));
     if (!multi) {
         const float thr = v.threshold;
         for (int i = 1; i < r.samples; ++i) {
             const F3 p = pos_of(i);
-            const float v2 = value(brick, p);
+            const float v2 = value(0, p);
             if (!isnan(v1) && !isnan(v2) && (v1 - thr) * (v2 - thr) < 0.f) {
                 const float t = (thr - v1) / (v2 - v1);
                 blend_behind(acc, surface_colour(thr, xpos_of(p, t)));
@@ -679,7 +717,7 @@ __device__ __forceinline__ ModeOut march_block_mode(const s3r_view& v, const s3r
         int iint = isnan(v1) ? -1 : find_interval(v1, pr.levels, nl);
         for (int i = 1; i < r.samples; ++i) {
             const F3 p = pos_of(i);
-            const float v2 = value(brick, p);
+            const float v2 = value(0, p);
             if (isnan(v2)) {
                 iint = -1;
                 v1 = __int_as_float(0x7fc00000);
@@ -726,6 +764,21 @@ __device__ __forceinline__ ModeOut march_block_mode(const s3r_view& v, const s3r
     return out;
 }
 
+// A block's contribution to one pixel of the ARGB8 viewport, as renderKernel<mode> stores it.
+__device__ __forceinline__ void store_mode_pixel(uint32_t* px, const ModeOut& o)
+{
+    if (o.kind == ModeOut::kMax) {
+        // renderMaxIntensityProjection.hpp:30-50; the pixel holds float bits
+        const float prev = __uint_as_float(*px);
+        if (!isnan(prev) && prev > o.t) return;
+        *px = __float_as_uint(o.t);
+    } else if (o.kind == ModeOut::kBlend) {
+        *px = blend_above_argb(*px, o.acc);
+    } else if (o.kind == ModeOut::kClear) {
+        *px = 0u;
+    }
+}
+
 template <bool kTex>
 __global__ void render_block_mode_kernel(const s3r_view v, const s3r_presentation pr, const float* __restrict__ brick,
                                          const float* __restrict__ brick2, const RenderBlock rb,
@@ -744,18 +797,94 @@ __global__ void render_block_mode_kernel(const s3r_view v, const s3r_presentatio
     pixel_ray(v, vx, vy, org, dir);
     BlockRay r;
     if (!block_ray(v, org, dir, rb, r)) return;
-    uint32_t* px = &viewport[(size_t)(v.H - 1 - vy) * v.W + vx];
-    const ModeOut o = march_block_mode<kTex>(v, pr, brick, brick2, r, rb.depth, tf);
-    if (o.kind == ModeOut::kMax) {
-        // renderMaxIntensityProjection.hpp:30-50; the pixel holds float bits
-        const float prev = __uint_as_float(*px);
-        if (!isnan(prev) && prev > o.t) return;
-        *px = __float_as_uint(o.t);
-    } else if (o.kind == ModeOut::kBlend) {
-        *px = blend_above_argb(*px, o.acc);
-    } else if (o.kind == ModeOut::kClear) {
-        *px = 0u;
+    const BrickSampler<kTex> smp{brick, brick2, dim_of(r), tf, v.tf_n};
+    store_mode_pixel(&viewport[(size_t)(v.H - 1 - vy) * v.W + vx], march_block_mode(v, pr, smp, r, rb.depth));
+}
+
+// The per-pixel ray and the block's sampling set-up written with plain float
+// operators in the order of DenseFieldRenderer_cu.cu:72-181 (ray = n + e1 x +
+// e2 y, face points eye + ray tau, the dot product of the sample count), so
+// that nvcc fuses the same products into the same fmas as in the reference's
+// kernel and the samples land where the reference's land.  The texture-unit
+// path uses them; the other kernels round every step explicitly, as the
+// oracle does.
+__device__ __forceinline__ void pixel_ray_fused(const s3r_view& v, uint32_t vx, uint32_t vy, float org[3],
+                                                float dir[3])
+{
+    const float x = (-0.5f + ((float)vx + 0.5f) / (float)v.W) * v.cam.w;
+    const float y = (-0.5f + ((float)vy + 0.5f) / (float)v.H) * v.cam.h;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (v.cam.ortho) {
+            org[d] = v.cam.eye[d] + v.cam.e1[d] * x + v.cam.e2[d] * y;
+            dir[d] = v.cam.n[d];
+        } else {
+            org[d] = v.cam.eye[d];
+            dir[d] = v.cam.n[d] + v.cam.e1[d] * x + v.cam.e2[d] * y;
+        }
     }
+}
+
+__device__ __forceinline__ bool block_ray_fused(const s3r_view& v, const float org[3], const float dir[3],
+                                                const RenderBlock& rb, BlockRay& r)
+{
+    const float* c = rb.center;
+    const float h = rb.half;
+    float te = 1.f, tx = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (!(fabsf(dir[a]) > 1e-10f)) continue;
+        const int b1 = a == 0 ? 1 : 0;
+        const int b2 = a == 2 ? 1 : 2;
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+            const float face = side ? c[a] + h : c[a] - h;
+            const float tau = (face - org[a]) / dir[a];
+            const float p1 = org[b1] + dir[b1] * tau;
+            const float p2 = org[b2] + dir[b2] * tau;
+            if (fabsf(p1 - c[b1]) <= h && fabsf(p2 - c[b2]) <= h) {
+                const bool enter = (dir[a] > 0.f) == (side == 0);
+                if (enter) te = tau;
+                else tx = tau;
+            }
+        }
+    }
+    if (te < 1.f) te = 1.f;
+    r.tau_enter = te;
+    r.tau_exit = tx;
+    if (!(tx > te)) return false;
+    const uint32_t n = (1u << rb.depth) + 1u;
+    const float dotr = dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2];
+    const int s = (int)(v.quality * (tx - te) * dotr / (rb.texel * (fabsf(dir[0]) + fabsf(dir[1]) + fabsf(dir[2]))));
+    const float dtau = (tx - te) / (float)s;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        r.step[d] = dir[d] * dtau;
+        r.p0[d] = org[d] + dir[d] * te;
+        r.origin[d] = rb.origin[d];
+    }
+    r.factor = rb.factor;
+    r.n = n;
+    r.pitch = n;
+    r.samples = s;
+    return true;
+}
+
+// One block in any field mode sampled through the texture unit (the field and
+// the transfer function as texture objects), on the fused ray set-up above.
+__global__ void render_block_texture_kernel(const s3r_view v, const s3r_presentation pr, const TextureSampler smp,
+                                            const RenderBlock rb, uint32_t* __restrict__ viewport)
+{
+    const int32_t xx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int32_t yy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (xx >= rb.rect[2] || yy >= rb.rect[3]) return;
+    const uint32_t vx = (uint32_t)(rb.rect[0] + xx), vy = (uint32_t)(rb.rect[1] + yy);
+    if (vx >= v.W || vy >= v.H) return;
+    float org[3], dir[3];
+    pixel_ray_fused(v, vx, vy, org, dir);
+    BlockRay r;
+    if (!block_ray_fused(v, org, dir, rb, r)) return;
+    store_mode_pixel(&viewport[(size_t)(v.H - 1 - vy) * v.W + vx], march_block_mode(v, pr, smp, r, rb.depth));
 }
 
 // ---------------------------------------------------------------- batched form
@@ -1103,8 +1232,9 @@ __global__ void frame_render_mode_kernel(FrameArgs fa, const s3r_presentation pr
             if (!pixel_in_rect(rca, vx, vy)) return true;
             BlockRay r;
             if (!block_ray(v, org, dir, *rb, r)) return true;
-            const ModeOut o = march_block_mode<kTex>(v, pr, bricks + rb->brick_off,
-                                                     bricks2 ? bricks2 + rb->brick_off : nullptr, r, depth, tf);
+            const BrickSampler<kTex> smp{bricks + rb->brick_off, bricks2 ? bricks2 + rb->brick_off : nullptr, dim_of(r),
+                                         tf, v.tf_n};
+            const ModeOut o = march_block_mode(v, pr, smp, r, depth);
             if (o.kind == ModeOut::kMax) {
                 if (!have_max || o.t > best) best = o.t;
                 have_max = true;
@@ -1382,6 +1512,18 @@ cudaError_t launch_render_block_mode(const s3r_view* view_host, const s3r_presen
     else
         render_block_mode_kernel<false><<<grid, block, smem, s>>>(*view_host, *pres, brick, brick2, rb,
                                                                   reinterpret_cast<const float4*>(tf), viewport);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_render_block_texture(const s3r_view* view_host, const s3r_presentation* pres, uint64_t field,
+                                       uint64_t field2, uint64_t tf_tex, const RenderBlock& rb, uint32_t* viewport,
+                                       cudaStream_t s)
+{
+    if (rb.rect[2] <= 0 || rb.rect[3] <= 0) return cudaSuccess;
+    dim3 block(16, 8);
+    dim3 grid((rb.rect[2] + 15) / 16, (rb.rect[3] + 7) / 8);
+    const TextureSampler smp{(cudaTextureObject_t)field, (cudaTextureObject_t)field2, (cudaTextureObject_t)tf_tex};
+    render_block_texture_kernel<<<grid, block, 0, s>>>(*view_host, *pres, smp, rb, viewport);
     return cudaGetLastError();
 }
 

@@ -167,6 +167,11 @@ uint32_t interp_plan_ctas_per_sm(uint32_t fmt, uint32_t tile_log2);
 cudaError_t launch_block_ranges(const PlanBlock* blocks, uint32_t nblocks, const float* sparse,
                                 const uint64_t* node_off_dev, float2* scale_offset, cudaStream_t s);
 
+// One block in any field mode (pres) sampled through the texture unit: field / field2 / tf_tex are
+// cudaTextureObject_t handles (3-D float field arrays, 1-D RGBA transfer-function array).
+cudaError_t launch_render_block_texture(const s3r_view* view_host, const s3r_presentation* pres, uint64_t field,
+                                       uint64_t field2, uint64_t tf_tex, const RenderBlock& rb, uint32_t* viewport,
+                                       cudaStream_t s);
 cudaError_t launch_render_block_mode(const s3r_view* view_host, const s3r_presentation* pres, const float* brick,
                                      const float* brick2, const RenderBlock& rb, const float* tf, uint32_t* viewport,
                                      cudaStream_t s);

@@ -19,6 +19,11 @@ from revise_gb300 import _lib, host, workloads
 pytestmark = pytest.mark.gpu
 
 TOL_IMAGE = 2e-3
+# Pixels the FP64 oracle flags -- a block's early-termination test (alpha > 0.996) lands within 1e-5 of the
+# threshold -- may end that block at a different sample in FP32 than in FP64.  The samples after a block's
+# alpha passes 0.996 change the pixel by at most the block's remaining transmittance, 1 - 0.996 + 1e-5, so
+# those pixels are checked against that bound instead of being left out.
+TOL_FLAGGED = 4.1e-3
 
 
 @pytest.fixture(scope="module")
@@ -57,10 +62,11 @@ def test_cfg3_graph_frame_vs_fp64_oracle(ctx, cfg3):
     ok = flags == 0
     err = np.abs(img[sel] - ref).max(axis=1)
     print(f"cfg3 frame vs FP64: max {err[ok].max():.2e}, mean {err[ok].mean():.2e}, "
-          f"{(~ok).sum()} of {sel.size} pixels flagged (block termination within 1e-5 of the threshold)")
+          f"{(~ok).sum()} of {sel.size} pixels flagged (block termination within 1e-5 of the threshold), "
+          f"max there {err[~ok].max() if (~ok).any() else 0:.2e}")
     assert ref[:, 3].max() > 0.5
     assert err[ok].max() <= TOL_IMAGE, err[ok].max()
-    assert ok.mean() > 0.99
+    assert err.max() <= TOL_FLAGGED, err.max()
 
 
 @pytest.mark.skipif(not refcu.available(), reason="reference CUDA cubins not built here")
@@ -98,9 +104,9 @@ def test_cfg3_worker_texture_path_vs_reference_cuda_worker(ctx, cfg3):
 def test_cfg4_brick_precision_vs_fp64(ctx, fmt):
     """The precision configuration: the cfg2 workload (64 blocks of depth 6, 1920x1080) with bricks stored
     as FP32, FP16 or BF16 (per-brick FP32 scale and offset), sampled and composited in FP32, against the
-    FP64 oracle on 2,000 covered and 500 random pixels: max and mean absolute RGBA error.  FP32 bricks meet
-    the 2e-3 image tolerance; the 16-bit bounds are the measured errors with a margin (their quantization
-    step is 2^-11 (FP16) and 2^-8 (BF16) of each brick's value range)."""
+    FP64 oracle on 2,000 covered and 500 random pixels: max and mean absolute RGBA error, all three within
+    the 2e-3 image tolerance (the 16-bit quantization step is 2^-11 (FP16) and 2^-8 (BF16) of each brick's
+    value range)."""
     import torch
     from revise_gb300.api import FramePlan
     w = workloads.cfg2()
@@ -117,9 +123,10 @@ def test_cfg4_brick_precision_vs_fp64(ctx, fmt):
     ref, flags = oracle.render_frame_f64(oracle.view_from(view), w, oracle.interp_workload(w), _rects(w, view),
                                          w.tf, np.stack([sel % w.W, w.H - 1 - sel // w.W], 1))
     ok = flags == 0
-    err = np.abs(img[sel] - ref)[ok]
+    err_all = np.abs(img[sel] - ref)
+    err = err_all[ok]
     name = {_lib.BRICK_F32: "FP32", _lib.BRICK_F16: "FP16", _lib.BRICK_BF16: "BF16"}[fmt]
-    print(f"cfg4 {name} bricks vs FP64: max {err.max():.3e}, mean {err.mean():.3e} (RGBA, {ok.sum()} pixels)")
-    bound = {_lib.BRICK_F32: TOL_IMAGE, _lib.BRICK_F16: 1e-2, _lib.BRICK_BF16: 5e-2}[fmt]
-    assert err.max() <= bound, err.max()
-    assert ok.mean() > 0.99
+    print(f"cfg4 {name} bricks vs FP64: max {err.max():.3e}, mean {err.mean():.3e} (RGBA, {ok.sum()} pixels); "
+          f"{(~ok).sum()} flagged pixels, max there {err_all[~ok].max() if (~ok).any() else 0:.3e}")
+    assert err.max() <= TOL_IMAGE, err.max()
+    assert err_all.max() <= TOL_FLAGGED, err_all.max()

@@ -10,6 +10,10 @@ from revise_gb300 import _lib, host, workloads
 pytestmark = pytest.mark.gpu
 
 TOL_IMAGE = 2e-3  # max abs per RGBA channel, float image vs the FP64 oracle
+# Pixels the FP64 oracle flags (a block's early-termination test within 1e-5 of alpha 0.996) may end that
+# block at another sample in FP32; what follows a block's alpha passing 0.996 moves the pixel by at most the
+# remaining transmittance, 1 - 0.996 + 1e-5: those pixels are checked against that bound.
+TOL_FLAGGED = 4.1e-3
 
 
 def _dev(a):
@@ -101,7 +105,7 @@ def test_frame_render_vs_fp64_oracle(ctx, name, filt):
     ok = flags == 0
     err = np.abs(img - ref).max(axis=1)
     assert err[ok].max() <= TOL_IMAGE, err[ok].max()
-    assert ok.mean() > 0.99
+    assert err.max() <= TOL_FLAGGED, err.max()
     plan.close()
 
 
@@ -115,8 +119,9 @@ def test_frame_render_opaque_tf_keeps_entry_segments(ctx):
     plan, view, img, _, _ = _frame(ctx, w)
     ov = oracle.view_from(view)
     ref, flags = oracle.render_frame_f64(ov, w, oracle.interp_workload(w), _rects(w, view), w.tf)
-    err = np.abs(img - ref).max(axis=1)[flags == 0]
-    assert err.max() <= TOL_IMAGE, err.max()
+    err = np.abs(img - ref).max(axis=1)
+    assert err[flags == 0].max() <= TOL_IMAGE, err[flags == 0].max()
+    assert err.max() <= TOL_FLAGGED, err.max()
     plan.close()
 
 
@@ -136,6 +141,7 @@ def test_frame_render_cfg2_sampled_pixels(ctx):
     ok = flags == 0
     err = np.abs(img[sel] - ref).max(axis=1)
     assert err[ok].max() <= TOL_IMAGE, err[ok].max()
+    assert err.max() <= TOL_FLAGGED, err.max()
     plan.close()
 
 
@@ -195,6 +201,7 @@ def test_16bit_bricks_image_error_is_bounded(ctx, fmt):
     ov = oracle.view_from(view)
     ref, flags = oracle.render_frame_f64(ov, w, oracle.interp_workload(w), _rects(w, view), w.tf)
     err = np.abs(img - ref)[flags == 0]
+    print(f"16-bit bricks ({'FP16' if fmt == _lib.BRICK_F16 else 'BF16'}), small scene vs FP64: max {err.max():.3e}")
     assert err.max() <= (0.02 if fmt == _lib.BRICK_F16 else 0.06)
     plan.close()
 
