@@ -593,7 +593,7 @@ struct ModeOut {
 // block's maximum above the threshold; the colour modes (Argb, ArgbLight,
 // DomainVoxels) and the isosurface modes the colour gathered with blendBehind;
 // multi-level modes with no level clear the pixel.
-template <class S>
+template <class S, int kMode = -1>
 __device__ __forceinline__ ModeOut march_block_mode(const s3r_view& v, const s3r_presentation& pr, const S& smp,
                                                     const BlockRay& r, uint32_t depth)
 {
@@ -627,7 +627,9 @@ __device__ __forceinline__ ModeOut march_block_mode(const s3r_view& v, const s3r
         return smp.field(second, tc.x, tc.y, tc.z);
     };
     constexpr float kMax = 0.996f; // AlphaThreshold / AlphaMaxThreshold
-    const uint32_t mode = pr.mode;
+    // kMode >= 0: the mode is fixed at compile time (one kernel per mode, as renderKernel<mode> is), so
+    // only its branch is compiled in and the registers are that mode's
+    const uint32_t mode = kMode >= 0 ? (uint32_t)kMode : pr.mode;
     if (mode == S3R_MODE_MAX_INTENSITY) {
         // renderMaxIntensityProjection.hpp:30-50; the pixel holds float bits
         float maxv = v.field_min - span;
@@ -872,6 +874,7 @@ __device__ __forceinline__ bool block_ray_fused(const s3r_view& v, const float o
 
 // One block in any field mode sampled through the texture unit (the field and
 // the transfer function as texture objects), on the fused ray set-up above.
+template <int kMode>
 __global__ void render_block_texture_kernel(const s3r_view v, const s3r_presentation pr, const TextureSampler smp,
                                             const RenderBlock rb, uint32_t* __restrict__ viewport)
 {
@@ -884,7 +887,8 @@ __global__ void render_block_texture_kernel(const s3r_view v, const s3r_presenta
     pixel_ray_fused(v, vx, vy, org, dir);
     BlockRay r;
     if (!block_ray_fused(v, org, dir, rb, r)) return;
-    store_mode_pixel(&viewport[(size_t)(v.H - 1 - vy) * v.W + vx], march_block_mode(v, pr, smp, r, rb.depth));
+    store_mode_pixel(&viewport[(size_t)(v.H - 1 - vy) * v.W + vx], march_block_mode<TextureSampler, kMode>(v, pr, smp, r,
+                                                                                                       rb.depth));
 }
 
 // ---------------------------------------------------------------- batched form
@@ -1523,7 +1527,36 @@ cudaError_t launch_render_block_texture(const s3r_view* view_host, const s3r_pre
     dim3 block(16, 8);
     dim3 grid((rb.rect[2] + 15) / 16, (rb.rect[3] + 7) / 8);
     const TextureSampler smp{(cudaTextureObject_t)field, (cudaTextureObject_t)field2, (cudaTextureObject_t)tf_tex};
-    render_block_texture_kernel<<<grid, block, 0, s>>>(*view_host, *pres, smp, rb, viewport);
+    switch (pres->mode) {
+    case S3R_MODE_ISOSURFACE:
+        render_block_texture_kernel<S3R_MODE_ISOSURFACE><<<grid, block, 0, s>>>(*view_host, *pres, smp, rb, viewport);
+        break;
+    case S3R_MODE_ISOSURFACES:
+        render_block_texture_kernel<S3R_MODE_ISOSURFACES><<<grid, block, 0, s>>>(*view_host, *pres, smp, rb, viewport);
+        break;
+    case S3R_MODE_MAX_INTENSITY:
+        render_block_texture_kernel<S3R_MODE_MAX_INTENSITY><<<grid, block, 0, s>>>(*view_host, *pres, smp, rb,
+                                                                                   viewport);
+        break;
+    case S3R_MODE_ARGB:
+        render_block_texture_kernel<S3R_MODE_ARGB><<<grid, block, 0, s>>>(*view_host, *pres, smp, rb, viewport);
+        break;
+    case S3R_MODE_ARGB_LIGHT:
+        render_block_texture_kernel<S3R_MODE_ARGB_LIGHT><<<grid, block, 0, s>>>(*view_host, *pres, smp, rb, viewport);
+        break;
+    case S3R_MODE_DOMAIN_VOXELS:
+        render_block_texture_kernel<S3R_MODE_DOMAIN_VOXELS><<<grid, block, 0, s>>>(*view_host, *pres, smp, rb,
+                                                                                   viewport);
+        break;
+    case S3R_MODE_VALUE_ON_ISOSURFACE:
+        render_block_texture_kernel<S3R_MODE_VALUE_ON_ISOSURFACE><<<grid, block, 0, s>>>(*view_host, *pres, smp, rb,
+                                                                                         viewport);
+        break;
+    default:
+        render_block_texture_kernel<S3R_MODE_VALUE_ON_ISOSURFACES><<<grid, block, 0, s>>>(*view_host, *pres, smp, rb,
+                                                                                          viewport);
+        break;
+    }
     return cudaGetLastError();
 }
 
