@@ -623,7 +623,9 @@ def measure_modes(ctx, torch, np, with_reference: bool):
             refcu = None
     out = {"workload": "cfg2: 4x4x4 blocks of depth 6 (17.6 M dense vertices), 1920x1080, 64 render launches "
                        "back to front, interpolation excluded; ms: s3r_render_block_texture (fields and transfer "
-                       "function in textures, sampled by the texture unit as the reference samples); "
+                       "function in textures, sampled by the texture unit as the reference samples), the 64 launches "
+                       "replayed from one CUDA graph, as reference_kernels_ms times the reference's renderKernel<mode> "
+                       "(per_launch_events: an event pair around each launch, host overhead included); "
                        "ms_software_texture_filter / ms_exact_filter: s3r_render_block on linear bricks; batched_ms: "
                        "the whole frame in one s3r_frame_render_mode launch (exact filter, FP32 compositing) on "
                        "resident bricks"}
@@ -679,7 +681,26 @@ def measure_modes(ctx, torch, np, with_reference: bool):
             return sum(x.elapsed_time(y) for x, y in evs)
 
         frame_tex()
-        ours = statistics.median([frame_tex() for _ in range(3)])
+        ours_events = statistics.median([frame_tex() for _ in range(3)])
+        # the same 64 launches back to back from one captured CUDA graph (no host overhead between launches),
+        # as the reference's kernels are timed below
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=side):
+            for b in oi:
+                ctx.render_block_texture(view, pres, texs[b], [int(x) for x in w.blocks[b, :3]], rects[b], tf_tex, vp,
+                                         tex2=texs2[b] if two else None, stream=side)
+        g.replay()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        ours = e0.elapsed_time(e1) / 5
+        del g
         view.filter = _lib.FILTER_EXACT
         frame()
         ours_exact = statistics.median([frame() for _ in range(3)])
@@ -697,12 +718,15 @@ def measure_modes(ctx, torch, np, with_reference: bool):
         batched()
         bms = statistics.median([batched() for _ in range(5)])
         view.filter = _lib.FILTER_TEXTURE
-        rec = {"ms": ours, "ms_software_texture_filter": ours_sw, "ms_exact_filter": ours_exact, "batched_ms": bms}
+        rec = {"ms": ours, "ms_per_launch_events": ours_events, "ms_software_texture_filter": ours_sw,
+               "ms_exact_filter": ours_exact, "batched_ms": bms}
         if refcu is not None:
             try:
-                rms = statistics.median([refcu.time_render(view, pres, w, oi, rects, u if two else None, clear)[0]
-                                         for _ in range(3)])
-                rec.update({"reference_kernels_ms": rms, "speedup": rms / ours, "speedup_batched": rms / bms})
+                rms = refcu.time_render_graph(view, pres, w, oi, rects, u if two else None)
+                rms_ev = statistics.median([refcu.time_render(view, pres, w, oi, rects, u if two else None, clear)[0]
+                                            for _ in range(3)])
+                rec.update({"reference_kernels_ms": rms, "reference_kernels_ms_per_launch_events": rms_ev,
+                            "speedup": rms / ours, "speedup_batched": rms / bms})
             except Exception as e:
                 rec["reference_kernels"] = f"unavailable: {type(e).__name__}: {e}"
         out[name] = rec

@@ -128,3 +128,26 @@ def time_render(view, pres, w, order_idx, rects, sparse2=None, clear=0):
                                     _p(s2, C.c_float) if s2 is not None else None, _p(rects, C.c_int32),
                                     _p(vp, C.c_uint32), C.byref(ms)))
     return ms.value, vp
+
+
+def time_render_graph(view, pres, w, order_idx, rects, sparse2=None, reps: int = 5):
+    """GPU time (ms) of the reference's renderKernel<pres.mode> over w's blocks in the given order, back to
+    back: each block's field interpolated into a texture of its own first (not timed), the launches
+    captured into one CUDA graph and replayed; ms per replay."""
+    lib = load()
+    blocks = np.ascontiguousarray(w.blocks[order_idx], dtype=np.uint32)
+    counts = np.diff(w.node_off.astype(np.int64))[order_idx]
+    node_off = np.concatenate([[0], np.cumsum(counts)]).astype(np.uint64)
+    n2i = np.ascontiguousarray(np.concatenate([w.block_nodes(int(b))[0] for b in order_idx]), dtype=np.uint16)
+    sparse = np.ascontiguousarray(np.concatenate([w.block_nodes(int(b))[1] for b in order_idx]), dtype=np.float32)
+    s2 = None
+    if sparse2 is not None:
+        s2 = np.ascontiguousarray(np.concatenate([sparse2[int(w.node_off[b]):int(w.node_off[b + 1])]
+                                                  for b in order_idx]), dtype=np.float32)
+    rects = np.ascontiguousarray(rects[order_idx], dtype=np.int32)
+    ms = C.c_double()
+    _check(lib.ref_cuda_time_render_graph(C.byref(view), C.byref(pres), C.c_uint32(blocks.shape[0]),
+                                          _p(blocks, C.c_uint32), _p(node_off, C.c_uint64), _p(n2i, C.c_uint16),
+                                          _p(sparse, C.c_float), _p(s2, C.c_float) if s2 is not None else None,
+                                          _p(rects, C.c_int32), C.c_uint32(reps), C.byref(ms)))
+    return ms.value

@@ -207,9 +207,9 @@ struct TfTexture {
     }
 } g_tf;
 
-int launch(CUfunction f, dim3 g, dim3 b, void** args)
+int launch(CUfunction f, dim3 g, dim3 b, void** args, CUstream stream = nullptr)
 {
-    CKD(cuLaunchKernel(f, g.x, g.y, g.z, b.x, b.y, b.z, 0, nullptr, args, nullptr));
+    CKD(cuLaunchKernel(f, g.x, g.y, g.z, b.x, b.y, b.z, 0, stream, args, nullptr));
     return 0;
 }
 
@@ -268,13 +268,14 @@ int interp_into_field(const uint16_t* n2i, const float* sparse, uint32_t n, uint
 
 // renderKernel<mode> for one block (DenseFieldRenderer_cu.cu:317-482); pres == nullptr: Argb.
 int render_block(const View& v, uint32_t depth, const uint32_t idx[3], const int32_t rect[4], uint32_t* viewport_dev,
-                 const Pres* pres = nullptr)
+                 const Pres* pres = nullptr, const Array3* f1 = &g_field, const Array3* f2 = &g_field2,
+                 CUstream stream = nullptr)
 {
     if (rect[2] <= 0 || rect[3] <= 0) return 0;
     RenderKernelParam p;
     std::memset(&p, 0, sizeof(p));
     p.viewport = {viewport_dev, v.W, v.H};
-    p.primaryField = {g_field.tex, depth, v.field_min, v.field_max};
+    p.primaryField = {f1->tex, depth, v.field_min, v.field_max};
     const float top = 5.f;
     const float h = top / (float)(1u << v.level);
     p.cube.halfSize = h;
@@ -308,14 +309,14 @@ int render_block(const View& v, uint32_t depth, const uint32_t idx[3], const int
             p.lights.sources[i].diffuse = make_float3(L.diffuse[0], L.diffuse[1], L.diffuse[2]);
             p.lights.sources[i].specular = make_float3(L.specular[0], L.specular[1], L.specular[2]);
         }
-        p.secondaryField = {g_field2.tex, depth, pres->secondary_min, pres->secondary_max};
+        p.secondaryField = {f2->tex, depth, pres->secondary_min, pres->secondary_max};
     }
     // chooseKernelDim1d(view.W, 32), chooseKernelDim1d(view.H, 1)
     const unsigned W = rect[2], H = rect[3];
     dim3 grid(W <= 32 ? 1 : blocks_for(W, 32), H <= 1 ? 1 : H);
     dim3 block(W <= 32 ? W : 32, H <= 1 ? H : 1);
     void* args[] = {&p};
-    return launch(kern, grid, block, args);
+    return launch(kern, grid, block, args, stream);
 }
 
 } // namespace
@@ -489,6 +490,69 @@ int ref_cuda_time_render(const void* view, const void* pres, uint32_t nblocks, c
     CKR(cudaEventDestroy(e1));
     CKR(cudaFree(d));
     *ms = total;
+    return 0;
+}
+
+// The same render launches timed back to back: every block's field interpolated into a texture of its
+// own first (not timed), then the launches captured once into a CUDA graph and the graph replayed `reps`
+// times; ms = GPU time per replay (CUDA events around the replays), free of per-launch host overhead.
+int ref_cuda_time_render_graph(const void* view, const void* pres, uint32_t nblocks, const uint32_t* blocks,
+                               const uint64_t* node_off, const uint16_t* n2i, const float* sparse,
+                               const float* sparse2, const int32_t* rects, uint32_t reps, double* ms)
+{
+    const View& v = *static_cast<const View*>(view);
+    const size_t npx = (size_t)v.W * v.H;
+    std::vector<Array3> f1(nblocks), f2(sparse2 ? nblocks : 0);
+    auto release = [&]() {
+        for (auto& a : f1) a.release();
+        for (auto& a : f2) a.release();
+    };
+    for (uint32_t i = 0; i < nblocks; ++i) {
+        const uint64_t a = node_off[i], b = node_off[i + 1];
+        const uint32_t depth = blocks[4 * i + 3];
+        if (interp_into(f1[i], n2i + 3 * a, sparse + a, (uint32_t)(b - a), depth)) return release(), 1;
+        if (sparse2 && interp_into(f2[i], n2i + 3 * a, sparse2 + a, (uint32_t)(b - a), depth)) return release(), 1;
+    }
+    uint32_t* d = nullptr;
+    CKR(cudaMalloc(&d, npx * 4));
+    CKR(cudaMemset(d, 0, npx * 4));
+    CKR(cudaDeviceSynchronize());
+    cudaStream_t s = nullptr;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    CKR(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    CKR(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    int rc = 0;
+    for (uint32_t i = 0; i < nblocks && !rc; ++i)
+        rc = render_block(v, blocks[4 * i + 3], blocks + 4 * i, rects + 4 * i, d, static_cast<const Pres*>(pres),
+                          &f1[i], sparse2 ? &f2[i] : &g_field2, (CUstream)s);
+    cudaError_t ce = cudaStreamEndCapture(s, &g);
+    if (rc || ce != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaStreamDestroy(s);
+        cudaFree(d);
+        release();
+        return rc ? rc : fail(std::string("capture: ") + cudaGetErrorString(ce));
+    }
+    CKR(cudaGraphInstantiate(&ge, g, 0));
+    cudaEvent_t e0, e1;
+    CKR(cudaEventCreate(&e0));
+    CKR(cudaEventCreate(&e1));
+    CKR(cudaGraphLaunch(ge, s)); // warm-up
+    CKR(cudaEventRecord(e0, s));
+    for (uint32_t r = 0; r < reps; ++r) CKR(cudaGraphLaunch(ge, s));
+    CKR(cudaEventRecord(e1, s));
+    CKR(cudaEventSynchronize(e1));
+    float t = 0;
+    CKR(cudaEventElapsedTime(&t, e0, e1));
+    *ms = t / (reps ? reps : 1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaGraphExecDestroy(ge);
+    cudaGraphDestroy(g);
+    cudaStreamDestroy(s);
+    cudaFree(d);
+    release();
     return 0;
 }
 
