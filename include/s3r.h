@@ -26,6 +26,7 @@
  *   s3r_default_light          the renderer's single light source (DenseFieldRenderer_cu.cu:440-445)
  *   s3r_block_cube,
  *   s3r_block_view_rect,
+ *   s3r_camera_from_view,
  *   s3r_camera_look_at         the host-side parameter set-up of renderDenseField (:317-409, :353-372)
  *   s3r_b2f_order              BackToFrontOrder<MacroBlock<3>>::range(eye) (include/BackToFrontOrder.hpp:61-359)
  *   s3r_split_index_cube,
@@ -171,6 +172,13 @@ typedef struct s3r_view {
  * ortho_height is the world height the viewport covers. */
 int s3r_camera_look_at(const double eye[3], const double center[3], const double up[3], double fovy_deg,
                        uint32_t W, uint32_t H, int32_t ortho, double ortho_height, s3r_camera* out);
+
+/* The camera the reference's renderer derives from VsRenderSharedState::cameraTransform
+ * (DenseFieldRenderer_cu.cu:353-372): view = the world -> eye transform of a rigid camera, column-major
+ * 4x4 floats; its inverse is taken as a rigid motion (rotation transposed), the screen axes normalized in
+ * float; h = 2 Lcam tan(fovY/2) with Lcam = 0.1, w = (h/H) W.  view_r / view_t keep the transform for the
+ * view rectangles. */
+int s3r_camera_from_view(const float view[16], float fovy_deg, uint32_t W, uint32_t H, s3r_camera* out);
 
 /* Cube of block idx at level (DenseFieldRenderer_cu.cu:337-350). */
 int s3r_block_cube(uint32_t level, const uint32_t idx[3], float center[3], float* half_size);

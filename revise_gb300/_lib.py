@@ -112,6 +112,7 @@ _SIGS = {
     "s3r_block_view_rect": (C.c_int, [C.POINTER(View), u32p, i32p]),
     "s3r_clear_viewport": (C.c_int, [vp, vp, C.c_uint32, C.c_uint32, C.c_uint32, vp]),
     "s3r_render_block_argb": (C.c_int, [vp, C.POINTER(View), vp, C.c_uint32, u32p, i32p, vp, vp, vp]),
+    "s3r_camera_from_view": (C.c_int, [C.POINTER(C.c_float), C.c_float, C.c_uint32, C.c_uint32, C.POINTER(Camera)]),
     "s3r_texture_create": (C.c_int, [vp, C.c_uint32, C.POINTER(vp)]),
     "s3r_texture_destroy": (C.c_int, [vp]),
     "s3r_texture_fill": (C.c_int, [vp, vp, vp, vp]),

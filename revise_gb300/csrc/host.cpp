@@ -911,6 +911,49 @@ int s3r_camera_look_at(const double eye[3], const double center[3], const double
     return S3R_OK;
 }
 
+int s3r_camera_from_view(const float m[16], float fovy_deg, uint32_t W, uint32_t H, s3r_camera* out)
+{
+    if (!m || !out || W == 0 || H == 0) return fail(nullptr, S3R_ERR_INVALID, "bad argument");
+    // m: the world -> eye transform, column-major (element (row r, column c) at m[4 c + r]): rotation R and
+    // translation T.  Its inverse (a rigid motion) has rotation R^T and translation -R^T T; the eye set-up of
+    // DenseFieldRenderer_cu.cu:353-372 reads the eye position -(R^T) T, the screen axes (columns of R^T,
+    // normalized) and the view direction (third column of R^T) from it, in float.
+    float R[3][3], T[3];
+    for (int r = 0; r < 3; ++r) {
+        for (int c = 0; c < 3; ++c) R[r][c] = m[4 * c + r];
+        T[r] = m[12 + r];
+    }
+    auto normalized = [](float v[3]) {
+        const float l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        if (l > 0) {
+            v[0] /= l;
+            v[1] /= l;
+            v[2] /= l;
+        }
+    };
+    std::memset(out, 0, sizeof(*out));
+    const float lcam = 0.01f * 2 * 5.f;
+    for (int r = 0; r < 3; ++r) // (-R^T) T, summed over the columns of -R^T in order
+        out->eye[r] = -R[0][r] * T[0] + -R[1][r] * T[1] + -R[2][r] * T[2];
+    float x[3] = {R[0][0], R[0][1], R[0][2]}, y[3] = {R[1][0], R[1][1], R[1][2]}, z[3] = {R[2][0], R[2][1], R[2][2]};
+    normalized(x);
+    normalized(y);
+    normalized(z);
+    for (int d = 0; d < 3; ++d) {
+        out->e1[d] = x[d];
+        out->e2[d] = y[d];
+        out->n[d] = z[d] * (-lcam);
+        out->view_r[d] = R[0][d];
+        out->view_r[3 + d] = R[1][d];
+        out->view_r[6 + d] = R[2][d];
+        out->view_t[d] = T[d];
+    }
+    out->h = (float)(2 * lcam * std::tan(0.5 * (double)fovy_deg * M_PI / 180));
+    const float pixel = out->h / (float)H;
+    out->w = pixel * (float)W;
+    return S3R_OK;
+}
+
 int s3r_block_cube(uint32_t level, const uint32_t idx[3], float center[3], float* half_size)
 {
     if (!idx || !center || !half_size || level > 12) return fail(nullptr, S3R_ERR_INVALID, "bad argument");

@@ -23,6 +23,36 @@ def camera_look_at(eye, center, up, fovy_deg: float, W: int, H: int, ortho: bool
     return cam
 
 
+def camera_from_view(view_matrix, fovy_deg: float, W: int, H: int) -> Camera:
+    """s3r_camera_from_view: the renderer's camera from a world -> eye transform (4x4, column-major floats,
+    the reference's VsRenderSharedState::cameraTransform)."""
+    lib = _lib.load()
+    m = np.ascontiguousarray(view_matrix, dtype=np.float32).reshape(16)
+    cam = Camera()
+    check(lib.s3r_camera_from_view(m.ctypes.data_as(C.POINTER(C.c_float)), float(fovy_deg), W, H, C.byref(cam)))
+    return cam
+
+
+def view_matrix_look_at(eye, center, up) -> np.ndarray:
+    """The world -> eye transform of s3r_camera_look_at's camera as 16 column-major floats (the rotation rows
+    and translation it keeps in view_r / view_t)."""
+    cam = camera_look_at(eye, center, up, 60.0, 2, 2)
+    m = np.zeros(16, np.float32)
+    r = np.array(cam.view_r[:], np.float32).reshape(3, 3)
+    for c in range(3):
+        m[4 * c:4 * c + 3] = r[:, c]
+    m[12:15] = np.array(cam.view_t[:], np.float32)
+    m[15] = 1.0
+    return m
+
+
+def relative_to_absolute(field_min: float, field_max: float, rel: float) -> float:
+    """The absolute field value of a relative one in float arithmetic, min + (max - min) rel
+    (relToAbsFieldValue, DenseFieldRenderer_cu.cu:591-595)."""
+    lo, hi, r = np.float32(field_min), np.float32(field_max), np.float32(rel)
+    return float(np.float32(lo + np.float32(np.float32(hi - lo) * r)))
+
+
 def make_view(cam: Camera, W: int, H: int, level: int, field_min: float, field_max: float, threshold: float,
               quality: float, tf_n: int, alpha_stop: float = 2.0, filter: int = _lib.FILTER_EXACT) -> View:
     """filter: _lib.FILTER_EXACT (exact FP32 filtering) or _lib.FILTER_TEXTURE (the texture
