@@ -99,7 +99,7 @@ def build_oracle(reference: str | None = None) -> None:
     if ref:
         _run(["make", "-s", "-C", str(oracle), "stage", f"REFERENCE={ref}"])
     if (oracle / "_ref" / "tree" / "include" / "s3dmm" / "DenseFieldInterpolator.hpp").exists():
-        _run(["make", "-s", "-C", str(oracle), "ref", "refcu", f"NVCC={cuda_home() / 'bin' / 'nvcc'}"])
+        _run(["make", "-s", "-C", str(oracle), "ref", "refcu", "refsetup", f"NVCC={cuda_home() / 'bin' / 'nvcc'}"])
     # the harness around the reference's CUDA kernels builds anywhere the cubins exist
     if (oracle / "_ref" / "ref_render.cubin").exists() and (oracle / "_ref" / "ref_interp.cubin").exists():
         _run(["make", "-s", "-C", str(oracle), "refcu-harness", f"NVCC={cuda_home() / 'bin' / 'nvcc'}"])
