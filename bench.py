@@ -10,9 +10,11 @@ seeded synthetic data with the configuration's shapes and distributions.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 --impl reference times the reference's CPU implementation of the path -- its
-dense-field generator (DenseFieldInterpolator<3>, restated in oracle/) -- on
-all host cores over a bounded sample of the same blocks.  The reference has no
-CPU ray caster, so that number covers interpolation only (which favours it).
+dense-field generator, DenseFieldInterpolator<3>, compiled from its own header
+(oracle/_ref, staged reference sources; the C restatement in oracle/ where that
+was not built) -- on all host cores over a bounded sample of the same blocks.
+The reference has no CPU ray caster, so that number covers interpolation only
+(which favours it).
 
 For N > 1 (torchrun), every rank runs the same frame on its own GPU (replicas:
 the path has no exchange step on one node), value = all ranks' vertices / the
@@ -70,26 +72,45 @@ def make_workload(name):
 
 
 # ------------------------------------------------------------------ CPU legs
+#
+# The reference's CPU dense-field generator is DenseFieldInterpolator<3>::interpolate
+# (include/s3dmm/DenseFieldInterpolator.hpp:198-419).  Where its header has been compiled here
+# (oracle/_ref/libs3r_ref.so, built from the staged reference sources) that code itself is timed
+# (kind "reference"); else the C restatement in oracle/ (kind "port").
 
-def _cpu_interp_blocks(args):
-    """Worker: interpolate the listed blocks with the oracle (the reference algorithm), return (vertices, seconds)."""
-    blocks, n2i_list, sp_list = args
+_W = {}
+
+
+def _cpu_worker_init(depths, n2i_list, sp_list, use_ref):
+    """Pool initializer: the sample's blocks, sent once per worker."""
     import oracle
-    t = time.perf_counter()
+    _W.update(depths=depths, n2i=n2i_list, sp=sp_list, fn=oracle.ref_interp if use_ref else oracle.interp_f32)
+    _W["fn"](n2i_list[0], sp_list[0], depths[0])  # load the library before the timed region
+
+
+def _cpu_interp_chunk(ids):
+    """Worker: interpolate the listed sample blocks, return the dense vertices produced."""
     v = 0
-    for d, n2i, sp in zip(blocks, n2i_list, sp_list):
-        oracle.interp_f32(n2i, sp, d)
+    for i in ids:
+        d = _W["depths"][i]
+        _W["fn"](_W["n2i"][i], _W["sp"][i], d)
         v += ((1 << d) + 1) ** 3
-    return v, time.perf_counter() - t
+    return v
+
+
+def _cpu_rate_guess():
+    """Dense vertices/s one host core interpolates (measured on this machine's hosts, for sizing samples):
+    ~15 M for the reference's header, ~60 M for the restatement."""
+    import oracle
+    return 15e6 if oracle.ref_available() else 60e6
 
 
 def _sample_blocks(w, seconds_budget, seed=0):
-    """A depth-stratified block sample whose CPU interpolation takes roughly the budget (single core)."""
+    """A random block sample whose CPU interpolation takes roughly the budget (single core)."""
     import numpy as np
     rng = np.random.default_rng(seed)
     order = rng.permutation(w.nblocks)
-    # ~60 M vertices/s for one core of the restated reference algorithm: size the sample to the budget
-    target = seconds_budget * 60e6
+    target = seconds_budget * _cpu_rate_guess()
     picked, tot = [], 0
     for b in order:
         d = int(w.blocks[b, 3])
@@ -100,26 +121,60 @@ def _sample_blocks(w, seconds_budget, seed=0):
     return picked
 
 
-def cpu_interp_rate(w, blocks, processes=1):
-    """Vertices/s of the oracle interpolator over `blocks` with `processes` workers (spawned)."""
-    jobs = [[] for _ in range(processes)]
-    for i, b in enumerate(blocks):
-        jobs[i % processes].append(b)
-    payload = []
-    for js in jobs:
-        payload.append(([int(w.blocks[b, 3]) for b in js], [w.block_nodes(b)[0] for b in js],
-                        [w.block_nodes(b)[1] for b in js]))
-    if processes == 1:
-        v, t = _cpu_interp_blocks(payload[0])
-        return v / t, t
-    import multiprocessing as mp
-    ctx = mp.get_context("spawn")
-    t0 = time.perf_counter()
-    with ctx.Pool(processes) as pool:
-        res = pool.map(_cpu_interp_blocks, payload)
-    wall = time.perf_counter() - t0
-    v = sum(r[0] for r in res)
-    return v / wall, wall
+class CpuInterp:
+    """The reference's CPU dense-field generator over a block sample on `processes` host processes: the
+    pool is started (spawn) and the sample sent to every worker once, before any timing; a timed step is
+    one map of the sample's blocks over the warm workers."""
+
+    def __init__(self, w, blocks, processes: int):
+        import oracle
+        self.kind = "reference" if oracle.ref_available() else "port"
+        self.depths = [int(w.blocks[b, 3]) for b in blocks]
+        self.vertices = sum(((1 << d) + 1) ** 3 for d in self.depths)
+        self.processes = processes
+        n2i = [w.block_nodes(b)[0] for b in blocks]
+        sp = [w.block_nodes(b)[1] for b in blocks]
+        order = sorted(range(len(blocks)), key=lambda i: -self.vertices_of(i))
+        self.chunks = [order[k::processes] for k in range(processes)]  # largest blocks dealt round-robin
+        self.pool = None
+        if processes == 1:
+            _cpu_worker_init(self.depths, n2i, sp, self.kind == "reference")
+        else:
+            import multiprocessing as mp
+            self.pool = mp.get_context("spawn").Pool(processes, initializer=_cpu_worker_init,
+                                                     initargs=(self.depths, n2i, sp, self.kind == "reference"))
+            self.pool.map(_cpu_interp_chunk, [[] for _ in range(processes)], chunksize=1)  # workers up
+
+    def vertices_of(self, i):
+        return ((1 << self.depths[i]) + 1) ** 3
+
+    def step(self):
+        """Vertices/s of one pass over the sample (wall time of the pass only)."""
+        t = time.perf_counter()
+        if self.pool is None:
+            v = _cpu_interp_chunk(self.chunks[0])
+        else:
+            v = sum(self.pool.map(_cpu_interp_chunk, self.chunks, chunksize=1))
+        return v / (time.perf_counter() - t)
+
+    def close(self):
+        if self.pool is not None:
+            self.pool.close()
+            self.pool.join()
+
+
+def _repo_native_libraries():
+    """The shared objects of this repository mapped into the process (what ran natively)."""
+    out = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                p = line.split()[-1] if line.strip() else ""
+                if p.endswith(".so") and str(ROOT) in p:
+                    out.add(str(Path(p).relative_to(ROOT)))
+    except OSError:
+        pass
+    return sorted(out)
 
 
 def run_reference(a):
@@ -132,13 +187,16 @@ def run_reference(a):
     cores = os.cpu_count() or 1
     budget = max(1.0, a.cpu_seconds / max(1, a.steps + a.warmup)) * cores
     blocks = _sample_blocks(w, budget, seed=1)
+    cpu = CpuInterp(w, blocks, cores)
     rates = []
     for i in range(a.warmup + a.steps):
-        r, _ = cpu_interp_rate(w, blocks, processes=cores)
+        r = cpu.step()
         if i >= a.warmup:
             rates.append(r)
+    cpu.close()
     value = statistics.median(rates) / 1e9
-    sample_v = sum(((1 << int(w.blocks[b, 3])) + 1) ** 3 for b in blocks)
+    what = ("the reference's DenseFieldInterpolator<3> compiled from its header (oracle/_ref/libs3r_ref.so)"
+            if cpu.kind == "reference" else "DenseFieldInterpolator<3> restated (oracle/s3r_oracle.c)")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": w.vertices / (value * 1e9) * 1e3, "higher_is_better": True,
@@ -146,37 +204,46 @@ def run_reference(a):
         "config": {"workload": f"{a.config}: {w.nblocks} blocks, depths {int(w.blocks[:, 3].min())}-"
                                f"{int(w.blocks[:, 3].max())}, {w.vertices} dense vertices",
                    "what": "dense-field generation only (the reference has no CPU ray caster)"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{len(blocks)} blocks ({sample_v} vertices) per step, all cores, "
-                                   "restated DenseFieldInterpolator<3> (oracle/s3r_oracle.c)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": cpu.kind,
+                         "sample": f"{len(blocks)} blocks ({cpu.vertices} vertices) per step, {cores} processes "
+                                   f"started once before the warm-up, {what}"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     if not a.no_extras:
         line["reference_cuda"] = reference_cuda_frames(w, a)
+    line["native_libraries"] = _repo_native_libraries()
     print(json.dumps(line))
     return 0
 
 
 def reference_cuda_frames(w, a):
-    """The reference's own GPU renderer on the same frame: its CUDA kernels (compiled
-    from its sources into oracle/_ref/*.cubin) driven block by block in back-to-front
-    order by the restated worker loop -- per block: upload of the sparse values,
-    the d-pass dense interpolation, renderKernel<Argb> into the shared viewport;
-    then the image read back and cropped.  Wall-clock ms per frame."""
+    """The reference's own GPU renderer on the same frame: its CUDA kernels (compiled from its sources into
+    oracle/_ref/*.cubin) driven block by block in back-to-front order by the restated worker loop -- per
+    block: upload of the sparse values, the d-pass dense interpolation, renderKernel<Argb> into the shared
+    viewport; then the image read back and cropped.  The camera, the block order (the reference's own
+    BackToFrontOrder, oracle/_ref/libs3r_ref.so) and the view rectangles come from the oracle side, not
+    from this library.  Wall-clock ms per frame."""
     try:
         import numpy as np
         import torch
+        import oracle
         from oracle import refcu
         if not (torch.cuda.is_available() and refcu.available()):
-            return {"unavailable": "reference cubins not built (they compile from the reference tree)"}
-        from revise_gb300 import host
-        view = host.view_for(w)
+            return {"unavailable": "reference cubins not built (they compile from the staged reference tree)"}
+        if not oracle.ref_available():
+            return {"unavailable": "the reference's BackToFrontOrder (oracle/_ref/libs3r_ref.so) is not built"}
+        cam = oracle.look_at_camera(w.eye, w.center, w.up, w.fovy, w.W, w.H)
+        view = refcu.harness_view(cam, w.W, w.H, w.level, w.field_min, w.field_max, w.threshold, w.quality,
+                                  w.tf.shape[0])
+        ov = oracle.orc_view(cam, w.W, w.H, w.level, w.field_min, w.field_max, w.threshold, w.quality,
+                             w.tf.shape[0], 1)
         refcu.set_tf(np.ascontiguousarray(w.tf, np.float32))
         m = 1 << w.level
-        order = host.b2f_order([0, 0, 0], [m, m, m], [-5.0] * 3, [5.0] * 3, w.eye)
+        order = oracle.ref_b2f_order([0, 0, 0], [m, m, m], [-5.0] * 3, [5.0] * 3, w.eye)
         idx = {tuple(b[:3]): i for i, b in enumerate(w.blocks.tolist())}
         oi = np.array([idx[tuple(b)] for b in order.tolist()])
-        rects = np.array([host.block_view_rect(view, w.blocks[b, :3]) for b in range(w.nblocks)], np.int32)
+        rects = np.array([oracle.block_view_rect(ov, cam["view_r"], cam["view_t"], w.blocks[b, :3])
+                          for b in range(w.nblocks)], np.int32)
         times = []
         for i in range(2 + max(1, min(a.steps, 5))):
             _, _, ms = refcu.worker(view, w, oi, rects)
@@ -398,11 +465,14 @@ def run_gb300(a):
     cpu = None
     if rank == 0 and not a.no_cpu:
         blocks = _sample_blocks(w, a.cpu_seconds, seed=2)
-        rate, secs = cpu_interp_rate(w, blocks, processes=1)
-        sv = sum(((1 << int(w.blocks[b, 3])) + 1) ** 3 for b in blocks)
-        cpu = {"value": rate / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"{len(blocks)} of {w.nblocks} blocks ({sv} vertices, {secs:.1f} s), one core, "
-                         "dense-field generation only (restated DenseFieldInterpolator<3>)"}
+        ci = CpuInterp(w, blocks, 1)
+        t0 = time.perf_counter()
+        rate = ci.step()
+        secs = time.perf_counter() - t0
+        cpu = {"value": rate / 1e9, "unit": UNIT, "cores": 1, "kind": ci.kind,
+               "sample": f"{len(blocks)} of {w.nblocks} blocks ({ci.vertices} vertices, {secs:.1f} s), one core, "
+                         "dense-field generation only (DenseFieldInterpolator<3>"
+                         + (", the reference's header compiled here)" if ci.kind == "reference" else ", restated)")}
 
     if rank == 0:
         value = world * V / (ms * 1e-3) / 1e9

@@ -123,6 +123,42 @@ def interp_workload(w, blocks=None, f64: bool = False) -> np.ndarray:
 
 # ---------------------------------------------------------------- geometry / render
 
+def look_at_camera(eye, center, up, fovy_deg: float, W: int, H: int) -> dict:
+    """The perspective camera of a look-at view, restated for the oracle side: the view matrix of the
+    OpenGL convention (camera looking along -Z: z = normalize(eye - center), x = normalize(up x z),
+    y = z x x, in double), then the eye set-up of DenseFieldRenderer_cu.cu:353-372 (n = -Lcam z with
+    Lcam = 0.1, h = 2 Lcam tan(fovY/2), pixel = h / H, w = pixel W) in float.  Keys: eye, e1, e2, n, w, h,
+    view_r (rows of the world -> eye rotation), view_t (its translation)."""
+    eye = np.asarray(eye, np.float64)
+    z = eye - np.asarray(center, np.float64)
+    z /= np.sqrt((z * z).sum())
+    u = np.asarray(up, np.float64)
+    x = np.array([u[1] * z[2] - u[2] * z[1], u[2] * z[0] - u[0] * z[2], u[0] * z[1] - u[1] * z[0]])
+    x /= np.sqrt((x * x).sum())
+    y = np.array([z[1] * x[2] - z[2] * x[1], z[2] * x[0] - z[0] * x[2], z[0] * x[1] - z[1] * x[0]])
+    lcam = np.float32(np.float32(np.float32(0.01) * np.float32(2)) * np.float32(5))
+    h = np.float32(2 * np.float64(lcam) * np.tan(0.5 * fovy_deg * np.pi / 180))
+    pixel = np.float32(h / np.float32(H))
+    rows = np.stack([x, y, z])
+    return {"eye": eye.astype(np.float32), "e1": x.astype(np.float32), "e2": y.astype(np.float32),
+            "n": (z.astype(np.float32) * -lcam).astype(np.float32), "h": h, "w": np.float32(pixel * np.float32(W)),
+            "view_r": rows.astype(np.float32).ravel(),
+            "view_t": np.array([-(r[0] * eye[0] + r[1] * eye[1] + r[2] * eye[2]) for r in rows], np.float32)}
+
+
+def orc_view(cam: dict, W: int, H: int, level: int, field_min, field_max, threshold, quality, tf_n: int,
+             filter: int = 0) -> OrcView:
+    """OrcView from a look_at_camera() camera and the frame parameters."""
+    o = OrcView()
+    for f in ("eye", "e1", "e2", "n"):
+        getattr(o.cam, f)[:] = [float(v) for v in cam[f]]
+    o.cam.w, o.cam.h, o.cam.ortho = float(cam["w"]), float(cam["h"]), 0
+    o.W, o.H, o.level = W, H, level
+    o.field_min, o.field_max, o.threshold, o.quality, o.tf_n = field_min, field_max, threshold, quality, tf_n
+    o.filter = filter
+    return o
+
+
 def block_view_rect(view: OrcView, r9, t3, idx) -> np.ndarray:
     rr = np.ascontiguousarray(r9, dtype=np.float32)
     tt = np.ascontiguousarray(t3, dtype=np.float32)

@@ -18,6 +18,29 @@ RENDER_CUBIN = HERE / "_ref" / "ref_render.cubin"
 _lib = None
 
 
+class HarnessView(C.Structure):
+    """The harness's view parameters (the field layout of the s3r_view the library's tests pass)."""
+    _fields_ = [("eye", C.c_float * 3), ("e1", C.c_float * 3), ("e2", C.c_float * 3), ("n", C.c_float * 3),
+                ("w", C.c_float), ("h", C.c_float), ("ortho", C.c_int32), ("reserved", C.c_int32),
+                ("view_r", C.c_float * 9), ("view_t", C.c_float * 3), ("W", C.c_uint32), ("H", C.c_uint32),
+                ("level", C.c_uint32), ("field_min", C.c_float), ("field_max", C.c_float), ("threshold", C.c_float),
+                ("quality", C.c_float), ("tf_n", C.c_uint32), ("alpha_stop", C.c_float), ("filter", C.c_uint32),
+                ("reserved2", C.c_uint32 * 2)]
+
+
+def harness_view(cam: dict, W: int, H: int, level: int, field_min, field_max, threshold, quality, tf_n: int,
+                 filter: int = 1) -> HarnessView:
+    """HarnessView from an oracle.look_at_camera() camera and the frame parameters."""
+    v = HarnessView()
+    for f in ("eye", "e1", "e2", "n", "view_r", "view_t"):
+        getattr(v, f)[:] = [float(x) for x in cam[f]]
+    v.w, v.h = float(cam["w"]), float(cam["h"])
+    v.W, v.H, v.level = W, H, level
+    v.field_min, v.field_max, v.threshold, v.quality, v.tf_n = field_min, field_max, threshold, quality, tf_n
+    v.alpha_stop, v.filter = 2.0, filter
+    return v
+
+
 def available() -> bool:
     return LIB.exists() and INTERP_CUBIN.exists() and RENDER_CUBIN.exists()
 

@@ -203,10 +203,31 @@ def _random_refinement(rng, lo=0.3, hi=0.7):
     return choose
 
 
+def color_table(xs, rgba, n: int) -> np.ndarray:
+    """(n, 4) float32 piecewise-linear RGBA table through the control points, in single precision exactly as
+    s3r_make_color_transfer (makeColorTransferVector) builds it; kept in numpy so that generating a workload
+    loads no native code."""
+    xs = np.asarray(xs, np.float64).astype(np.float32)
+    rgba = np.asarray(rgba, np.float64).reshape(-1, 4).astype(np.float32)
+    out = np.zeros((n, 4), np.float32)
+    xmin, xmax = xs[0], xs[-1]
+    out[0] = c1 = rgba[0]
+    i1 = 0
+    one = np.float32(1)
+    for ip in range(1, xs.size):
+        c2 = rgba[ip]
+        i2 = n - 1 if ip + 1 == xs.size else int(np.float32(np.float32(xs[ip] - xmin) / np.float32(xmax - xmin)) * np.float32(n))
+        for i in range(i1 + 1, min(i2, n - 1) + 1) if i2 > i1 else ():
+            t = np.float32(np.float32(i - i1) / np.float32(i2 - i1))
+            out[i] = np.float32(c1 * (one - t)) + np.float32(c2 * t)
+        c1 = c2
+        i1 = i2
+    return out
+
+
 def _tf_default(n=256):
-    from . import host
     xs, rgba = colormap_points()
-    return host.make_color_transfer(xs, rgba, n)
+    return color_table(xs, rgba, n)
 
 
 def cfg2(seed: int = 0, W: int = 1920, H: int = 1080) -> Workload:

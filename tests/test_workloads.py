@@ -35,3 +35,19 @@ def test_cfg1_matches_its_specification():
     f = np.sin(4 * np.pi * u[:, 0]) * np.cos(4 * np.pi * u[:, 1]) + u[:, 2]
     np.testing.assert_allclose(v[r < 0.45], f[r < 0.45], rtol=1e-6, atol=1e-6)
     assert w.tf.shape == (256, 4) and (w.field_min, w.field_max) == (-1.0, 2.0)
+
+
+def test_workload_color_table_equals_the_library_table():
+    """Workloads build their transfer-function tables in numpy (no native code loads while generating
+    inputs): bit-identical to s3r_make_color_transfer on the default and on random control points."""
+    from revise_gb300 import host
+    xs, rgba = workloads.colormap_points()
+    cases = [(xs, rgba, n) for n in (2, 5, 256, 512, 1000)]
+    rng = np.random.default_rng(0)
+    for _ in range(100):
+        x = np.unique(np.sort(rng.uniform(-3, 3, int(rng.integers(2, 8)))))
+        cases.append((x, rng.uniform(0, 1, (x.size, 4)), int(rng.integers(2, 600))))
+    for x, c, n in cases:
+        a = workloads.color_table(x, c, n)
+        b = np.asarray(host.make_color_transfer(x, c, n), np.float32)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), n
