@@ -7,10 +7,13 @@
 // DenseFieldInterpolatorTpl_cu_3 (include/s3dmm_cuda/DenseFieldInterpolatorTpl_cu_3.hpp:40-118):
 // constructed from a BlockTreeFieldProvider<3>, it reads a subtree's sparse
 // values (fieldValues), and interpolates them into the dense container.
-// Two containers are accepted:
+// Three containers are accepted:
 //   std::vector<dfield_real>&  host grid, the contract of DenseFieldInterpolator<3>
 //                              (values copied back after the GPU computes them);
-//   Gb300DenseField&           device grid that stays in HBM for the renderer adapter.
+//   Gb300DenseField&           device grid that stays in HBM;
+//   Gb300TextureField&         the grid as a 3-D texture (one per depth, kept), sampled by the texture
+//                              unit as the reference's renderer samples its Device3DArray
+//                              (the renderer adapter, DenseFieldRendererGb300.hpp).
 // Errors throw std::runtime_error, as the reference's CU_CHECK does.
 #pragma once
 
@@ -95,6 +98,25 @@ struct Gb300DenseField {
     const float* data() const { return buf.data; }
 };
 
+// A dense grid held as an s3r field texture: one texture per subtree depth, created on first use and kept.
+struct Gb300TextureField {
+    s3r_texture* tex[S3R_MAX_DEPTH + 1] = {};
+    unsigned int depth = 0;
+    Gb300TextureField() = default;
+    Gb300TextureField(const Gb300TextureField&) = delete;
+    Gb300TextureField& operator=(const Gb300TextureField&) = delete;
+    ~Gb300TextureField()
+    {
+        for (s3r_texture* t : tex) s3r_texture_destroy(t);
+    }
+    s3r_texture* at(s3r_ctx* ctx, unsigned int d)
+    {
+        if (!tex[d]) gb300::check(s3r_texture_create(ctx, d, &tex[d]), ctx, "s3r_texture_create");
+        return tex[d];
+    }
+    const s3r_texture* current() const { return tex[depth]; }
+};
+
 template <class ContainerRef>
 class DenseFieldInterpolatorGb300
 {
@@ -144,7 +166,13 @@ public:
         gb300::check_cuda(cudaMemcpy(m_values.data, m_host.data(), 4 * n, cudaMemcpyHostToDevice),
                           "cudaMemcpy values");
         const size_t e = (size_t(1) << depth) + 1;
-        if constexpr (std::is_same_v<std::decay_t<ContainerRef>, Gb300DenseField>) {
+        if constexpr (std::is_same_v<std::decay_t<ContainerRef>, Gb300TextureField>) {
+            if (depth > S3R_MAX_DEPTH) throw std::runtime_error("subtree depth exceeds S3R_MAX_DEPTH");
+            dense.depth = depth;
+            gb300::check(s3r_interp_dense_texture(ctx, m_n2i.data, m_values.data, uint32_t(n), dense.at(ctx, depth),
+                                                  nullptr),
+                         ctx, "s3r_interp_dense_texture");
+        } else if constexpr (std::is_same_v<std::decay_t<ContainerRef>, Gb300DenseField>) {
             dense.buf.reserve(e * e * e);
             dense.depth = depth;
             gb300::check(s3r_interp_dense(ctx, m_n2i.data, m_values.data, uint32_t(n), depth, dense.buf.data, nullptr),
