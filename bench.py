@@ -831,7 +831,8 @@ def measure_adjoint(ctx, torch, np):
     plan.interp(sp)
     dl = torch.rand_like(rgba) * 0.01
     dtf = torch.zeros(w.tf.size, device="cuda")
-    dd = torch.zeros(plan.store_elems(), device="cuda")
+    bricks, _ = plan.bricks()
+    dd = torch.zeros(bricks.numel(), device="cuda")
 
     fwd = event_ms(torch, lambda: plan.render(view, tf, rgba))
     bwd = event_ms(torch, lambda: plan.backward(view, tf, rgba, dl, dtf, dd))

@@ -420,10 +420,7 @@ int s3r_frame_plan(s3r_ctx* ctx, const s3r_frame_desc* desc, s3r_plan** out);
 int s3r_plan_destroy(s3r_plan* plan);
 int s3r_plan_info_get(const s3r_plan* plan, s3r_plan_info* out);
 /* Device pointer to the brick store and, per block, the offset of its first element (host, nblocks+1
- * entries).  The caller may write the store through the pointer: from this call until the next
- * interpolation into the plan, renders sample every region of every brick (the interpolation also records
- * which regions of 4^3 cells hold no sample the exact filter keeps, and renders of its bricks skip the
- * texel loads there).  Block b's vertex (x, y, z) is element vertex_off[b] + (z (2^d+1) + y) pitch[b] + x, with the
+ * entries).  Block b's vertex (x, y, z) is element vertex_off[b] + (z (2^d+1) + y) pitch[b] + x, with the
  * row pitch from s3r_plan_brick_pitches: 2^d+1 rounded up to whole 32-byte sectors (elements between
  * 2^d+1 and the pitch are never written nor read). */
 int s3r_plan_bricks(const s3r_plan* plan, void** bricks, const uint64_t** vertex_off);

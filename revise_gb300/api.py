@@ -216,8 +216,7 @@ class FramePlan:
         return i
 
     def bricks(self):
-        """Zero-copy device tensor of the brick store and the per-block vertex offsets.  The caller may write
-        the store through it: renders sample every region until the next interpolation (s3r_plan_bricks)."""
+        """Zero-copy device tensor of the brick store and the per-block vertex offsets."""
         p = C.c_void_p()
         off = _lib.u64p()
         check(self.lib.s3r_plan_bricks(self.h, C.byref(p), C.byref(off)))
@@ -225,16 +224,6 @@ class FramePlan:
         offs = np.ctypeslib.as_array(off, shape=(nb + 1,)).copy()
         dt = "f4" if self.fmt == _lib.BRICK_F32 else ("f2" if self.fmt == _lib.BRICK_F16 else "u2")
         return device_array(p.value, (int(offs[-1]),), dt, self), offs
-
-    def store_elems(self) -> int:
-        """Elements of the brick store (rows padded to the brick pitch)."""
-        return int(self.info.brick_bytes) // (4 if self.fmt == _lib.BRICK_F32 else 2)
-
-    def offsets(self) -> np.ndarray:
-        """Per block (and one past the last): the first element of its brick in the store."""
-        pit = self.pitches().astype(np.uint64)
-        e = (np.uint64(1) << self.blocks[:, 3].astype(np.uint64)) + np.uint64(1)
-        return np.concatenate([[0], np.cumsum(e * e * pit)]).astype(np.uint64)
 
     def pitches(self) -> np.ndarray:
         """Per block: the brick row pitch in elements (rows padded to whole 32-byte sectors)."""
@@ -248,7 +237,7 @@ class FramePlan:
         if store is None:
             store, offs = self.bricks()
         else:
-            offs = self.offsets()
+            offs = self.bricks()[1]
         e = (1 << int(self.blocks[b, 3])) + 1
         pitch = int(self.pitches()[b])
         a = int(offs[b])
@@ -261,7 +250,7 @@ class FramePlan:
         if store is None:
             store, offs = self.bricks()
         else:
-            offs = self.offsets()
+            offs = self.bricks()[1]
         pit = self.pitches()
         parts = []
         for b in range(self.blocks.shape[0]):

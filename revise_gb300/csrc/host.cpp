@@ -68,11 +68,6 @@ struct s3r_plan {
     uint64_t vertices = 0, nodes = 0, tiles = 0, entries = 0;
     uint64_t brick_elems = 0;          // elements of the brick store (rows padded to the pitch)
     std::vector<uint32_t> pitch;       // per block: brick row pitch in elements
-    std::vector<uint32_t> occ_off;     // per block: first byte of its occupancy map
-    uint64_t occ_bytes = 0;            // bytes of the occupancy maps of one brick store
-    uint8_t* occ_dev = nullptr;        // occupancy maps of the plan's brick store, written by each interpolation
-    uint8_t* occ_1 = nullptr;          // those of the second slot's brick store (s3r_frame_run_host)
-    bool occ_valid = false;            // occ_dev describes the brick store (false once the store's address is handed out)
     // device
     PlanBlock* blocks_dev = nullptr;
     uint2* items_dev = nullptr;
@@ -516,7 +511,6 @@ int plan_bin(s3r_plan* p, uint32_t tile_log2)
         pb[b].node_base = p->node_off[b];
         pb[b].dense_off = p->vertex_off[b];
         pb[b].pitch = p->pitch[b];
-        pb[b].occ_off = p->occ_off[b];
         const uint64_t m = 1ull << L;
         tiles_off[b + 1] = tiles_off[b] + m * m * m;
         coarse_off[b + 1] = coarse_off[b] + (m + 1) * (m + 1) * (m + 1);
@@ -758,8 +752,6 @@ int plan_launch_interp(s3r_plan* p, const float* sparse, cudaStream_t s, uint32_
     a.queue = p->queue_dev + slot;
     a.scale_offset = p->fmt == S3R_BRICK_F32 ? nullptr : so;
     a.out = slot ? p->bricks_1 : p->bricks;
-    a.occ = slot ? p->occ_1 : p->occ_dev;
-    if (!slot) p->occ_valid = true;
     S3R_CUDA(ctx, cudaMemsetAsync(a.queue, 0, sizeof(uint32_t), s));
     S3R_CUDA(ctx, launch_interp_plan(a, p->fmt, p->tile_log2, p->grid_ctas, s));
     ++*kernels;
@@ -779,7 +771,6 @@ int plan_launch_render(s3r_plan* p, const float* tf, float* rgba, uint32_t* argb
     fa.samples = samples;
     fa.scale_offset = p->fmt == S3R_BRICK_F32 ? nullptr : (slot ? p->scale_offset_1 : p->scale_offset_dev);
     fa.cover = p->cover_dev;
-    fa.occ = slot ? p->occ_1 : (p->occ_valid ? p->occ_dev : nullptr);
     S3R_CUDA(p->ctx, launch_frame_render(fa, p->last_view.W, p->last_view.H, p->last_view.tf_n, p->fmt,
                                          p->render_tile, p->last_view.filter, s));
     ++*kernels;
@@ -1510,7 +1501,6 @@ int s3r_frame_plan(s3r_ctx* ctx, const s3r_frame_desc* desc, s3r_plan** out)
     p->n2i.assign(desc->n2i, desc->n2i + 3 * p->nodes);
     p->vertex_off.assign(desc->nblocks + 1, 0);
     p->pitch.assign(desc->nblocks, 0);
-    p->occ_off.assign(desc->nblocks, 0);
     p->vertices = 0;
     const uint32_t elem_bytes = p->fmt == S3R_BRICK_F32 ? 4u : 2u;
     p->table_host.assign((size_t)m * m * m, RenderBlock{});
@@ -1541,10 +1531,6 @@ int s3r_frame_plan(s3r_ctx* ctx, const s3r_frame_desc* desc, s3r_plan** out)
         t.brick_off = p->vertex_off[b];
         t.pitch = pitch;
         t.block = b;
-        const uint64_t nm = occ_per_axis(bl[3]);
-        if (p->occ_bytes + nm * nm * nm > 0xffffffffull) return bail(fail(ctx, S3R_ERR_INVALID, "plan too large"));
-        p->occ_off[b] = t.occ_off = (uint32_t)p->occ_bytes;
-        p->occ_bytes += nm * nm * nm;
         const uint32_t lim = (uint32_t)(e - 1);
         for (uint64_t i = p->node_off[b]; i < p->node_off[b + 1]; ++i)
             if (p->n2i[3 * i] > lim || p->n2i[3 * i + 1] > lim || p->n2i[3 * i + 2] > lim)
@@ -1558,8 +1544,6 @@ int s3r_frame_plan(s3r_ctx* ctx, const s3r_frame_desc* desc, s3r_plan** out)
     if ((rc = upload(ctx, &p->node_off_dev, p->node_off))) return bail(rc);
     if ((e = cudaMalloc(&p->queue_dev, 2 * sizeof(uint32_t))) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "cudaMalloc(queue)"));
-    if ((e = cudaMalloc(&p->occ_dev, std::max<uint64_t>(p->occ_bytes, 1))) != cudaSuccess)
-        return bail(cuda_fail(ctx, e, "cudaMalloc(occupancy)"));
     if ((e = cudaMalloc(&p->scale_offset_dev, sizeof(float2) * p->nblocks)) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "cudaMalloc(scales)"));
     if ((e = cudaMalloc(&p->table_dev, sizeof(RenderBlock) * p->table_host.size())) != cudaSuccess)
@@ -1594,7 +1578,6 @@ int s3r_plan_destroy(s3r_plan* p)
         if (q) cudaFree(q);
     };
     f(p->bricks);
-    f(p->occ_dev);
     f(p->node_off_dev);
     f(p->queue_dev);
     f(p->scale_offset_dev);
@@ -1628,8 +1611,6 @@ int s3r_plan_info_get(const s3r_plan* p, s3r_plan_info* out)
 int s3r_plan_bricks(const s3r_plan* p, void** bricks, const uint64_t** vertex_off)
 {
     if (!p || !bricks || !vertex_off) return fail(nullptr, S3R_ERR_INVALID, "null pointer");
-    // the caller may write the store from now on: renders sample every region until the next interpolation
-    const_cast<s3r_plan*>(p)->occ_valid = false;
     *bricks = p->bricks;
     *vertex_off = p->vertex_off.data();
     return S3R_OK;
@@ -1805,10 +1786,8 @@ static void plan_destroy_host_pipeline(s3r_plan* p)
     p->hs_h2d = p->hs_d2h = nullptr;
     if (p->bricks_1) cudaFree(p->bricks_1);
     if (p->scale_offset_1) cudaFree(p->scale_offset_1);
-    if (p->occ_1) cudaFree(p->occ_1);
     p->bricks_1 = nullptr;
     p->scale_offset_1 = nullptr;
-    p->occ_1 = nullptr;
 }
 
 // The GPU work of one s3r_frame_run_host call on slot b: the copies and the frame, with the events that
@@ -1884,8 +1863,7 @@ int s3r_frame_run_host(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const
     if (!plan->bricks_1) {
         const size_t esz = plan->fmt == S3R_BRICK_F32 ? 4 : 2;
         if ((e = cudaMalloc(&plan->bricks_1, std::max<uint64_t>(plan->brick_elems, 1) * esz)) != cudaSuccess ||
-            (e = cudaMalloc(&plan->scale_offset_1, sizeof(float2) * std::max<uint32_t>(plan->nblocks, 1))) != cudaSuccess ||
-            (e = cudaMalloc(&plan->occ_1, std::max<uint64_t>(plan->occ_bytes, 1))) != cudaSuccess)
+            (e = cudaMalloc(&plan->scale_offset_1, sizeof(float2) * std::max<uint32_t>(plan->nblocks, 1))) != cudaSuccess)
             return cuda_fail(ctx, e, "cudaMalloc(second frame slot)");
     }
     const uint64_t pixels = (uint64_t)view->W * view->H;
@@ -2026,7 +2004,6 @@ int s3r_render_argb_backward(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view,
     fa.dl_drgba = dl_drgba;
     fa.dtf = dtf;
     fa.ddense = ddense;
-    fa.occ = plan->occ_valid ? plan->occ_dev : nullptr;
     const size_t nparts = (size_t)kDtfParts * 4 * view->tf_n;
     if (plan->dtf_part_floats < nparts) {
         // allocation: synchronizes the device once, on the first adjoint call (or a larger table)

@@ -358,20 +358,11 @@ template <bool kSlots> __device__ __forceinline__ void fill_cube(float v[27])
 // value") before any slot is overwritten, then turn masked sparse values to NaN.
 // kPairs: plan bricks, whose rows are padded to whole sectors (aligned rows, even pitch): a row's two
 // vertices of a cube go out as one store.  A plain (2^d+1)^3 grid (odd pitch) stores them one by one.
-// The occupancy bytes of the tile being computed (plan form): one per region of 4^3 cells (2^3 cubes), for
-// tiles of up to 32 cells.
-__shared__ uint8_t s_occ[(32 / 4) * (32 / 4) * (32 / 4)];
-// where they go: the map index of the tile's first region, and the block's regions per axis (written by
-// thread 0 before the tile's first barrier, so that nothing of it stays in registers through the tile)
-__shared__ uint32_t s_occ_base, s_occ_nm;
-
-// kOcc: a cube whose centre vertex is not NaN marks its region of s_occ as holding a live cell.
-template <uint32_t T, typename OutT, bool kPairs, bool kOcc>
+template <uint32_t T, typename OutT, bool kPairs>
 __device__ __forceinline__ void finest_store(const float* s, const uint32_t* flags, OutT* out, uint32_t e,
                                              uint32_t pitch, uint32_t ox, uint32_t oy, uint32_t oz, bool far_x,
                                              bool far_y, bool far_z, float inv_scale, float offset)
 {
-    constexpr uint32_t kRegions = T >= 4 ? T / 4 : 1; // occupancy regions per tile axis
     using S = SplitTile<T>;
     constexpr uint32_t H = S::H;
     constexpr uint32_t lh = (H >= 2) ? (31 - __builtin_clz(H)) : 0;
@@ -401,7 +392,6 @@ __device__ __forceinline__ void finest_store(const float* s, const uint32_t* fla
         } else {
             fill_cube<false>(v);
         }
-        if (kOcc && !isnan(v[13])) s_occ[(ci >> 1) + kRegions * ((cj >> 1) + kRegions * (ck >> 1))] = 1;
         OutT* base = out + (((oz + 2 * ck) * e + (oy + 2 * cj)) * pitch + (ox + 2 * ci));
         if constexpr (kPairs) {
 #pragma unroll
@@ -520,7 +510,7 @@ __device__ __forceinline__ void prefetch_values(Prefetch& pf, const TileArgs& a)
 }
 
 struct TileItem {
-    uint32_t d, k, L, tx, ty, tz, blk, pitch, occ_off;
+    uint32_t d, k, L, tx, ty, tz, blk, pitch;
     uint32_t slots; // the tile has flagged cubes, which read its midpoint slots
     uint64_t node_base, dense_off;
     uint32_t item;
@@ -532,8 +522,6 @@ template <uint32_t T, bool kGrid, typename OutT>
 __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* desc, uint32_t* flags, const TileItem& t,
                                          Prefetch& pf, const uint32_t* next_item)
 {
-    constexpr uint32_t kRegions = T >= 4 ? T / 4 : 1, kRegions3 = kRegions * kRegions * kRegions;
-    constexpr bool occ = !kGrid; // a plan's tiles write their block's occupancy map
     constexpr uint32_t E = T + 1, E3 = E * E * E;
     using S = SplitTile<T < 2 ? 2 : T>;
     auto at = [](uint32_t x, uint32_t y, uint32_t z) -> uint32_t {
@@ -582,12 +570,6 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
             for (uint32_t p = threadIdx.x; p < n4; p += kInterpThreads) s4[p] = nan4;
         }
         for (uint32_t q = threadIdx.x; q < 27 * L; q += kInterpThreads) desc[q] = qnan();
-        for (uint32_t q = threadIdx.x; q < kRegions3; q += kInterpThreads) s_occ[q] = 0;
-        if (threadIdx.x == 0) {
-            const uint32_t nm = occ_per_axis(d);
-            s_occ_nm = nm;
-            s_occ_base = t.occ_off + t.tx * kRegions + nm * (t.ty * kRegions + nm * (t.tz * kRegions));
-        }
         __syncthreads();
         auto place = [&](uint32_t loc, float v) {
             if (loc < E3) s[loc] = v;
@@ -639,20 +621,8 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
     OutT* out = reinterpret_cast<OutT*>(a.out) + t.dense_off;
     const bool far_x = t.tx == mL - 1, far_y = t.ty == mL - 1, far_z = t.tz == mL - 1;
     if constexpr (T >= 2) {
-        finest_store<T, OutT, !kGrid, occ>(s, flags, out, e, t.pitch, ox, oy, oz, far_x, far_y, far_z, inv_scale,
-                                           offset);
-        if constexpr (occ) {
-            // the tile's occupancy bytes into the block's map
-            __syncthreads();
-            const uint32_t nm = s_occ_nm, base = s_occ_base;
-            for (uint32_t q = threadIdx.x; q < kRegions3; q += kInterpThreads) {
-                const uint32_t i = q % kRegions, j = (q / kRegions) % kRegions, k = q / (kRegions * kRegions);
-                a.occ[base + i + nm * (j + nm * k)] = s_occ[q];
-            }
-        }
+        finest_store<T, OutT, !kGrid>(s, flags, out, e, t.pitch, ox, oy, oz, far_x, far_y, far_z, inv_scale, offset);
     } else {
-        if constexpr (occ)
-            if (threadIdx.x == 0) a.occ[t.occ_off] = 1; // a depth-0 block: its one cell, always sampled
         // depth-0 block: its 8 root corners
         for (uint32_t q = threadIdx.x; q < 8; q += kInterpThreads) {
             const uint32_t x = q & 1, y = (q >> 1) & 1, z = q >> 2;
@@ -697,7 +667,6 @@ __global__ void __launch_bounds__(kInterpThreads, 8) interp_tiles_kernel(TileArg
         t.slots = 1;
         t.node_base = 0;
         t.dense_off = 0;
-        t.occ_off = 0;
         if constexpr (kGrid) {
             t.d = a.grid_depth;
             t.k = a.grid_tile_log2 < t.d ? a.grid_tile_log2 : t.d;
@@ -716,7 +685,6 @@ __global__ void __launch_bounds__(kInterpThreads, 8) interp_tiles_kernel(TileArg
             t.node_base = b.node_base;
             t.dense_off = b.dense_off;
             t.pitch = b.pitch;
-            t.occ_off = b.occ_off;
         }
         const uint32_t mL = 1u << t.L;
         t.tx = tile & (mL - 1);

@@ -48,8 +48,6 @@ struct BlockRay {
     float factor;
     uint32_t n;     // vertices per axis, 2^depth+1
     uint32_t pitch; // row pitch of the brick in elements (>= n)
-    const uint8_t* occ; // the brick's occupancy map (exact filter, plan bricks), else nullptr
-    uint32_t occ_log2;  // occupancy regions per axis, log2
 };
 
 // A brick's extent and row pitch: vertex (x, y, z) is element (z n + y) pitch + x.
@@ -127,8 +125,6 @@ __device__ __forceinline__ bool block_ray(const s3r_view& v, const float org[3],
     r.n = n;
     r.pitch = rb.pitch ? rb.pitch : n;
     r.samples = s;
-    r.occ = nullptr;
-    r.occ_log2 = 0;
     return true;
 }
 
@@ -150,29 +146,6 @@ __device__ __forceinline__ void sample_cell(const BlockRay& r, int k, Cell& c)
         const int a = (int)fl, b = a + 1;
         c.i0[d] = (uint32_t)min(max(a, 0), hi);
         c.i1[d] = (uint32_t)min(max(b, 0), hi);
-    }
-}
-
-// True when the sample's cell lies in a region the interpolation found empty (every cell of it has a NaN
-// vertex, so the exact filter would skip the sample): its texels need not be loaded.  Samples whose cell is
-// clamped at the brick's edge (on its outer half-texel shell) are never skipped: their texels are a subset
-// of an edge cell's corners, not all of them.
-__device__ __forceinline__ bool cell_dead(const BlockRay& r, const Cell& c)
-{
-    if (!r.occ) return false;
-    if (c.i1[0] != c.i0[0] + 1 || c.i1[1] != c.i0[1] + 1 || c.i1[2] != c.i0[2] + 1) return false;
-    const uint32_t lg = r.occ_log2;
-    const uint32_t q = (c.i0[0] >> kOccCellsLog2) + ((c.i0[1] >> kOccCellsLog2) << lg) +
-                       ((c.i0[2] >> kOccCellsLog2) << (2 * lg));
-    return __ldg(r.occ + q) == 0;
-}
-
-// The occupancy map of a plan block, when the frame has one.
-__device__ __forceinline__ void attach_occupancy(const FrameArgs& fa, const RenderBlock& rb, BlockRay& r)
-{
-    if (fa.occ) {
-        r.occ = fa.occ + rb.occ_off;
-        r.occ_log2 = rb.depth >= kOccCellsLog2 ? rb.depth - kOccCellsLog2 : 0;
     }
 }
 
@@ -902,8 +875,6 @@ __device__ __forceinline__ bool block_ray_fused(const s3r_view& v, const float o
     r.n = n;
     r.pitch = n;
     r.samples = s;
-    r.occ = nullptr;
-    r.occ_log2 = 0;
     return true;
 }
 
@@ -1026,7 +997,6 @@ struct Premul {
 template <int Fmt> struct Texels {
     float t[8];
     float f[3];
-    bool dead; // in an empty region: not loaded, the sample is skipped
 };
 
 template <int Fmt>
@@ -1035,15 +1005,12 @@ __device__ __forceinline__ void fetch_texels(const void* brick, const BlockRay& 
     Cell c;
     sample_cell(r, k, c);
     const uint32_t n = r.n;
-    x.dead = cell_dead(r, c);
-    if (!x.dead) {
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const uint32_t xi = (q & 1) ? c.i1[0] : c.i0[0];
-            const uint32_t yi = (q & 2) ? c.i1[1] : c.i0[1];
-            const uint32_t zi = (q & 4) ? c.i1[2] : c.i0[2];
-            x.t[q] = Brick<Fmt>::get(brick, (zi * n + yi) * r.pitch + xi);
-        }
+    for (int q = 0; q < 8; ++q) {
+        const uint32_t xi = (q & 1) ? c.i1[0] : c.i0[0];
+        const uint32_t yi = (q & 2) ? c.i1[1] : c.i0[1];
+        const uint32_t zi = (q & 4) ? c.i1[2] : c.i0[2];
+        x.t[q] = Brick<Fmt>::get(brick, (zi * n + yi) * r.pitch + xi);
     }
 #pragma unroll
     for (int d = 0; d < 3; ++d) x.f[d] = c.f[d];
@@ -1087,7 +1054,7 @@ __device__ __forceinline__ Premul march_block(const s3r_view& v, const BlockRay&
             ++taken;
             if (i + 1 < r.samples) fetch_texels<Fmt>(brick, r, i, nxt);
             float val;
-            if (!cur.dead && filter_texels<Fmt>(cur, val)) {
+            if (filter_texels<Fmt>(cur, val)) {
                 if (Fmt != S3R_BRICK_F32) val = __fmaf_rn(scale, val, offset);
                 const float v01 = __fdiv_rn(__fsub_rn(val, v.field_min), span);
                 const float4 col = tf_lookup(tf, v.tf_n, v01).c;
@@ -1183,7 +1150,6 @@ __global__ void frame_render_kernel(FrameArgs fa)
             if (!pixel_in_rect(rca, vx, vy)) return true;
             BlockRay r;
             if (!block_ray(v, org, dir, *rb, r)) return true;
-            if (!kTex) attach_occupancy(fa, *rb, r);
             const char* base = reinterpret_cast<const char*>(fa.bricks);
             const size_t esz = Fmt == S3R_BRICK_F32 ? 4 : 2;
             float scale = 1.f, offset = 0.f;
@@ -1332,17 +1298,10 @@ __device__ __forceinline__ void cell_offsets(const Cell& c, Dim g, uint32_t off[
     }
 }
 
-// The cell's 8 texels; a cell in an empty region (cell_dead) is not loaded but given a NaN, which makes
-// filter_cell skip the sample as the loaded texels would.
-__device__ __forceinline__ void fetch_cell(const float* brick, const Cell& c, const BlockRay& r, float t[8])
+__device__ __forceinline__ void fetch_cell(const float* brick, const Cell& c, Dim g, float t[8])
 {
-    if (cell_dead(r, c)) {
-#pragma unroll
-        for (int q = 0; q < 8; ++q) t[q] = __int_as_float(0x7fc00000);
-        return;
-    }
     uint32_t off[8];
-    cell_offsets(c, dim_of(r), off);
+    cell_offsets(c, g, off);
 #pragma unroll
     for (int q = 0; q < 8; ++q) t[q] = __ldg(brick + off[q]);
 }
@@ -1434,7 +1393,6 @@ __global__ void __launch_bounds__(128, 4) frame_backward_kernel(FrameArgs fa)
                 if (!pixel_in_rect(rca, vx, vy)) return true;
                 BlockRay r;
                 if (!block_ray(v, org, dir, *rb, r)) return true;
-                attach_occupancy(fa, *rb, r);
                 const float* brick = reinterpret_cast<const float*>(fa.bricks) + rb->brick_off;
                 float* gdense = fa.ddense + rb->brick_off;
                 const float il = layer_exponent(depth, v.level, v.quality);
@@ -1528,18 +1486,18 @@ __global__ void __launch_bounds__(128, 4) frame_backward_kernel(FrameArgs fa)
                 float ta[8], tb[8];
                 if (r.samples > 1) {
                     sample_cell(r, 0, ca);
-                    fetch_cell(brick, ca, r, ta);
+                    fetch_cell(brick, ca, dim_of(r), ta);
                 }
                 for (int i = 1; i < r.samples; i += 2) {
                     if (i + 1 < r.samples) {
                         sample_cell(r, i, cb);
-                        fetch_cell(brick, cb, r, tb);
+                        fetch_cell(brick, cb, dim_of(r), tb);
                     }
                     if (!step_sample(ca, ta)) break;
                     if (i + 1 >= r.samples) break;
                     if (i + 2 < r.samples) {
                         sample_cell(r, i + 1, ca);
-                        fetch_cell(brick, ca, r, ta);
+                        fetch_cell(brick, ca, dim_of(r), ta);
                     }
                     if (!step_sample(cb, tb)) break;
                 }

@@ -23,19 +23,8 @@ struct PlanBlock {
     uint64_t node_base;   // first node of this block in the sparse value array
     uint64_t dense_off;   // first element of this block's brick
     uint32_t pitch;       // brick row pitch in elements (>= 2^d+1): vertex (x, y, z) at (z (2^d+1) + y) pitch + x
-    uint32_t occ_off;     // first byte of this block's occupancy map (see occ_per_axis)
+    uint32_t pad;
 };
-
-// Occupancy map of a plan brick: one byte per region of 4 x 4 x 4 cells (the whole block when it has fewer
-// cells per axis), x fastest; 0 when every cell of the region has a NaN among its 8 vertices -- the
-// interpolation kernel writes it with the brick: a region is empty when the centre vertex of each of its
-// 2 x 2 x 2-cell cubes is NaN, that vertex being a corner of all 8 of the cube's cells.  The exact-filter ray
-// cast skips the texel loads of samples that fall in an empty region: they would be skipped anyway.
-constexpr uint32_t kOccCellsLog2 = 2;
-inline __host__ __device__ uint32_t occ_per_axis(uint32_t depth)
-{
-    return depth >= kOccCellsLog2 ? 1u << (depth - kOccCellsLog2) : 1u;
-}
 
 // Row pitch of a batched plan's brick of depth d: 2^d+1 rounded up to whole
 // 32-byte sectors, so that every row -- and with it every block, whose size is
@@ -65,7 +54,6 @@ struct TileArgs {
     const float2* scale_offset;   // per block {scale, offset} for 16-bit bricks
     void* out;                    // brick store
     uint32_t* queue;              // work-queue counter, zeroed before the launch (nullptr: one item per CTA)
-    uint8_t* occ;                 // occupancy maps (plan form, always written)
     // single-block form
     const float* grid;
     uint32_t grid_depth;
@@ -100,7 +88,7 @@ struct RenderBlock {
     float texel;       // 2 half / n                                         (:169)
     uint32_t block;    // index into the plan's block list (per-brick scale/offset)
     uint32_t pitch;    // brick row pitch in elements; 0: 2^depth+1 (a plain dense grid)
-    uint32_t occ_off;  // first byte of the block's occupancy map in a plan
+    uint32_t pad;
 };
 
 // Per-block sampling constants of DenseFieldRenderer_cu.cu:168-181, with the
@@ -117,7 +105,6 @@ struct FrameArgs {
     unsigned long long* samples;   // optional
     const float2* scale_offset;    // per block {scale, offset} (16-bit bricks)
     const int32_t* cover;          // device {x0, y0, x1, y1}: union of the blocks' view rectangles
-    const uint8_t* occ;            // occupancy maps of the bricks (nullptr: sample every region)
     // adjoint
     const float* fwd_rgba;
     const float* dl_drgba;

@@ -33,7 +33,8 @@ def _gpu_grad(ctx, w, target_img, keep=None):
     if keep is not None:  # pixels whose sample sets float and FP64 arithmetic agree on
         dl = dl * torch.from_numpy(np.repeat(keep.astype(np.float32), 4)).cuda()
     dtf = torch.zeros(w.tf.size, device="cuda")
-    dd = torch.zeros(plan.store_elems(), device="cuda")
+    bricks, offs = plan.bricks()
+    dd = torch.zeros(bricks.numel(), device="cuda")
     plan.backward(view, tf, rgba, dl, dtf, dd)
     torch.cuda.synchronize()
     loss = 0.5 * float((dl.double() ** 2).sum())

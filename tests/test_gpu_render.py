@@ -274,42 +274,3 @@ def test_adjoint_rejects_texture_filter(ctx):
         plan.backward(view, tf, img, img, torch.zeros(w.tf.size, device="cuda"), torch.zeros(bricks.numel(), device="cuda"))
     assert e.value.code == _lib.S3R_ERR_UNSUPPORTED
     plan.close()
-
-
-@pytest.mark.parametrize("fmt", [_lib.BRICK_F32, _lib.BRICK_F16])
-def test_empty_region_skipping_is_exact(ctx, fmt):
-    """The interpolation records which 4^3-cell regions hold no sample the exact filter keeps, and the ray
-    cast skips their texel loads.  The image, and the adjoint's gradients, equal those of the same render
-    with the map switched off (s3r_plan_bricks hands the store out: renders then sample every region),
-    bit for bit, on a workload with masked nodes."""
-    import torch
-    from revise_gb300.api import FramePlan
-    w = workloads.cfg3(level=2)
-    view = host.view_for(w)
-    plan = FramePlan(ctx, w, fmt, tile_cells=16)
-    sp, tf = _dev(w.sparse), _dev(w.tf)
-    out = []
-    for skip in (True, False):
-        plan.interp(sp)
-        if not skip:
-            plan.bricks()  # the caller could now write the store: no region is skipped
-        rgba = torch.zeros(w.W * w.H * 4, device="cuda")
-        samples = torch.zeros(1, dtype=torch.int64, device="cuda")
-        plan.render(view, tf, rgba, None, samples)
-        grads = None
-        if fmt == _lib.BRICK_F32:
-            dl = torch.rand(rgba.shape, generator=torch.Generator().manual_seed(1)).cuda() * 0.01
-            dtf = torch.zeros(w.tf.size, device="cuda")
-            dd = torch.zeros(plan.store_elems(), device="cuda")
-            plan.backward(view, tf, rgba, dl, dtf, dd)
-            grads = (dtf, dd)
-        torch.cuda.synchronize()
-        out.append((rgba, int(samples.item()), grads))
-    (a, sa, ga), (b, sb, gb) = out
-    assert float(a.view(-1, 4)[:, 3].max()) > 0.1
-    assert torch.equal(a, b) and sa == sb
-    if ga is not None:
-        # the gradient sums run in a thread-dependent order (atomics): equal to rounding
-        assert torch.allclose(ga[0], gb[0], rtol=1e-5, atol=1e-6 * float(gb[0].abs().max()))
-        assert torch.allclose(ga[1], gb[1], rtol=1e-5, atol=1e-6 * float(gb[1].abs().max()))
-    plan.close()
