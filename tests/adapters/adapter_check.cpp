@@ -89,9 +89,11 @@ static int run_worker(const std::string& base, const std::string& in_path, const
     VsWorkerGb300 worker;
     worker.initialize("", false, "", 0);
     worker.setRenderSharedState(&st);
+    // the level's whole block cube; an index box's max is one past its last block, as the reference's
+    // splitter makes the boxes it hands to workers (BlockOrderUtil.hpp:45-47 takes 1 off it)
     const unsigned cubes = 1u << level;
     s3vs::SubtreeSetDescription subtrees(level, MultiIndex<3, unsigned int>{0, 0, 0},
-                                         MultiIndex<3, unsigned int>{cubes - 1, cubes - 1, cubes - 1});
+                                         MultiIndex<3, unsigned int>{cubes, cubes, cubes});
     silver_bullets::sync::CancelController cc;
     const auto part = worker.renderScenePart(subtrees, cc.checker());
     std::ofstream out(out_path, std::ios::binary);
