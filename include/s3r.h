@@ -388,6 +388,18 @@ int s3r_make_color_transfer(const double* xs, const double* rgba, uint32_t npoin
 #define S3R_BRICK_F16 1  /* value = offset + scale * half, per-brick FP32 scale/offset */
 #define S3R_BRICK_BF16 2 /* value = offset + scale * bfloat16 */
 
+/* Frame render forms (s3r_frame_desc.render_tile):
+ *   ids below S3R_RENDER_TILES_WALK: one thread (or 2, 4, 8 lanes) per pixel ray walks the block grid
+ *     front to back and composites every block it passes (4 CTA pixel shapes x 4 lane counts; several
+ *     lanes per ray merge partial composites in another association order, within 1e-5);
+ *   ids S3R_RENDER_TILES_WALK .. S3R_RENDER_TILES-1: block-major -- CTAs take pixel tiles of the
+ *     blocks' view rectangles (deepest blocks first) and march one block each, the per-block results
+ *     are blended per pixel in front-to-back order afterwards; the same image bit for bit as id 0, for
+ *     levels up to 7, at the cost of (3 * 2^level - 2) x W x H x 16 bytes of device memory per data slot.
+ * The autotuner times every form. */
+#define S3R_RENDER_TILES_WALK 16u
+#define S3R_RENDER_TILES 19u
+
 /* Static description of a block set: the topology part of a block tree level
  * (one BlockTreeNodes n2i list per block), fixed across time frames. */
 typedef struct s3r_frame_desc {
@@ -398,7 +410,7 @@ typedef struct s3r_frame_desc {
     const uint16_t* n2i;       /* host: node_off[nblocks] x {x, y, z} */
     uint32_t brick_format;     /* S3R_BRICK_* */
     uint32_t tile_cells;       /* interpolation tile edge in cells: 8, 16 or 32; 0 = autotuned */
-    uint32_t render_tile;      /* render CTA shape id; 0 = autotuned */
+    uint32_t render_tile;      /* render form and CTA shape id (< S3R_RENDER_TILES); 0 = autotuned */
     uint32_t reserved;
 } s3r_frame_desc;
 
@@ -430,9 +442,11 @@ int s3r_plan_brick_pitches(const s3r_plan* plan, const uint32_t** pitch);
 int s3r_plan_brick_scales(const s3r_plan* plan, const float** scale_offset);
 
 /* Project-written autotuner: times the interpolation of `sparse` with tiles of
- * 8, 16 and 32 cells and the frame render with each CTA shape, `reps` runs
- * each after one warm-up, keeps the fastest of both and re-bins the plan for
- * the chosen tile.  Synchronizes the stream; allocates; drops captured graphs. */
+ * 8, 16 and 32 cells and the frame render with each render form and CTA shape
+ * (S3R_RENDER_TILES), `reps` runs each after one warm-up, keeps the fastest of
+ * both and re-bins the plan for the chosen tile.  Several lanes per ray are
+ * skipped when view->alpha_stop < 1; a block-major form whose buffers do not fit
+ * is skipped.  Synchronizes the stream; allocates; drops captured graphs. */
 int s3r_plan_autotune(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const float* sparse, const float* tf,
                       uint32_t reps, void* stream);
 

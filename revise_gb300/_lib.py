@@ -22,6 +22,7 @@ MAX_DEPTH = 9
 
 BRICK_F32, BRICK_F16, BRICK_BF16 = 0, 1, 2
 FILTER_EXACT, FILTER_TEXTURE = 0, 1
+RENDER_TILES_WALK, RENDER_TILES = 16, 19  # render forms: per-ray walk ids, then block-major ids
 ABI_VERSION = 6
 
 u8p = C.POINTER(C.c_uint8)

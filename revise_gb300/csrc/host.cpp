@@ -100,6 +100,18 @@ struct s3r_plan {
     FrameGraph graphs[3];
     float* dtf_part = nullptr; // adjoint: kDtfParts copies of the transfer-function gradient
     size_t dtf_part_floats = 0;
+    // block-major render: the block cells deepest first, per item footprint the running tile counts over
+    // them (staged with the view), per data slot the per-rank block results and rank masks, and one
+    // work-queue counter per data slot
+    std::vector<uint32_t> seg_order;
+    uint32_t* seg_order_dev = nullptr;
+    uint32_t* seg_prefix_dev = nullptr; // kSegShapes x (nblocks + 1)
+    uint32_t* seg_prefix_pinned = nullptr;
+    uint32_t* seg_queue = nullptr;      // 2 counters
+    float4* seg_buf[2] = {nullptr, nullptr};
+    unsigned long long* seg_mask[2] = {nullptr, nullptr};
+    uint64_t seg_pixels = 0;            // pixels the buffers hold
+    uint32_t seg_words = 0;
     // s3r_frame_run_host: per slot a device copy of the frame's sparse values and its image, and the
     // streams and events that overlap frame k's copies with frames k-1 and k+1
     float* hs_sparse[2] = {nullptr, nullptr};
@@ -694,9 +706,53 @@ int plan_bin(s3r_plan* p, uint32_t tile_log2)
     return S3R_OK;
 }
 
+// The block-major render's per-rank results and rank masks for W x H pixels, in both data slots; called
+// before a frame is launched (or captured) with a block-major render tile.  Reallocation drops the captured
+// frames (they hold the old buffers).
+void plan_free_segments(s3r_plan* p)
+{
+    for (int b = 0; b < 2; ++b) {
+        if (p->seg_buf[b]) cudaFree(p->seg_buf[b]);
+        if (p->seg_mask[b]) cudaFree(p->seg_mask[b]);
+        p->seg_buf[b] = nullptr;
+        p->seg_mask[b] = nullptr;
+    }
+    p->seg_pixels = 0;
+}
+
+int plan_ensure_segments(s3r_plan* p, uint32_t W, uint32_t H)
+{
+    if (p->render_tile < (uint32_t)kRenderWalkTiles) return S3R_OK;
+    s3r_ctx* ctx = p->ctx;
+    const uint64_t npix = (uint64_t)W * H;
+    const uint32_t m = 1u << p->level;
+    const uint32_t words = (3 * m - 2 + 63) / 64;
+    if (words > kSegMaskWords)
+        return fail(ctx, S3R_ERR_UNSUPPORTED, "the block-major render covers levels up to 7");
+    if (p->seg_buf[0] && p->seg_pixels >= npix && p->seg_words == words) return S3R_OK;
+    S3R_CUDA(ctx, cudaDeviceSynchronize());
+    plan_free_segments(p);
+    plan_drop_graph(p);
+    for (int b = 0; b < 2; ++b) {
+        cudaError_t e;
+        if ((e = cudaMalloc(&p->seg_buf[b], (size_t)(3 * m - 2) * npix * sizeof(float4))) != cudaSuccess ||
+            (e = cudaMalloc(&p->seg_mask[b], (size_t)words * npix * sizeof(unsigned long long))) != cudaSuccess ||
+            (e = cudaMemset(p->seg_mask[b], 0, (size_t)words * npix * sizeof(unsigned long long))) != cudaSuccess) {
+            plan_free_segments(p);
+            (void)cudaGetLastError(); // an allocation failure leaves no error behind for later launches
+            return cuda_fail(ctx, e, "cudaMalloc(block-major render buffers)");
+        }
+    }
+    S3R_CUDA(ctx, cudaDeviceSynchronize());
+    p->seg_pixels = npix;
+    p->seg_words = words;
+    return S3R_OK;
+}
+
 int plan_stage_view(s3r_plan* p, const s3r_view* view, cudaStream_t s)
 {
     s3r_ctx* ctx = p->ctx;
+    if (int rc = plan_ensure_segments(p, view->W, view->H)) return rc;
     const bool same = p->have_view && std::memcmp(&p->last_view, view, sizeof(s3r_view)) == 0;
     if (same) return S3R_OK;
     // the staging buffers may still feed an earlier copy
@@ -718,6 +774,21 @@ int plan_stage_view(s3r_plan* p, const s3r_view* view, cudaStream_t s)
         }
     }
     if (cover[0] > cover[2]) cover[0] = cover[1] = cover[2] = cover[3] = 0;
+    // block-major render: per item footprint the running count of view-rectangle tiles, deepest blocks first
+    for (int f = 0; f < kSegShapes; ++f) {
+        uint32_t* pf = p->seg_prefix_pinned + (size_t)f * (p->nblocks + 1);
+        uint64_t run = 0;
+        for (uint32_t i = 0; i < p->nblocks; ++i) {
+            pf[i] = (uint32_t)run;
+            const int32_t* r = tb[p->seg_order[i]].rect;
+            if (r[2] > 0 && r[3] > 0)
+                run += (uint64_t)((r[2] + kSegShapeX[f] - 1) / kSegShapeX[f]) * ((r[3] + kSegShapeY[f] - 1) / kSegShapeY[f]);
+        }
+        if (run > 0xffffffffull) return fail(ctx, S3R_ERR_INVALID, "too many block-major render items");
+        pf[p->nblocks] = (uint32_t)run;
+    }
+    S3R_CUDA(ctx, cudaMemcpyAsync(p->seg_prefix_dev, p->seg_prefix_pinned,
+                                  (size_t)kSegShapes * (p->nblocks + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     std::memcpy(p->cover_pinned, cover, sizeof(cover));
     S3R_CUDA(ctx, cudaMemcpyAsync(p->cover_dev, p->cover_pinned, sizeof(cover), cudaMemcpyHostToDevice, s));
     *p->view_pinned = *view;
@@ -771,6 +842,24 @@ int plan_launch_render(s3r_plan* p, const float* tf, float* rgba, uint32_t* argb
     fa.samples = samples;
     fa.scale_offset = p->fmt == S3R_BRICK_F32 ? nullptr : (slot ? p->scale_offset_1 : p->scale_offset_dev);
     fa.cover = p->cover_dev;
+    if (p->render_tile >= (uint32_t)kRenderWalkTiles) {
+        const int data = slot ? 1 : 0;
+        if (!p->seg_buf[data] || p->seg_pixels < (uint64_t)p->last_view.W * p->last_view.H)
+            return fail(p->ctx, S3R_ERR_INVALID, "block-major render buffers not allocated for this view");
+        const uint32_t shape = p->render_tile - (uint32_t)kRenderWalkTiles;
+        SegArgs sa{};
+        sa.order = p->seg_order_dev;
+        sa.prefix = p->seg_prefix_dev + (size_t)shape * (p->nblocks + 1);
+        sa.nblocks = p->nblocks;
+        sa.words = p->seg_words;
+        sa.seg = p->seg_buf[data];
+        sa.mask = p->seg_mask[data];
+        sa.queue = p->seg_queue + data;
+        S3R_CUDA(p->ctx, launch_frame_segments(fa, sa, p->last_view.W, p->last_view.H, p->last_view.tf_n, p->fmt, shape,
+                                               p->last_view.filter, (uint32_t)p->ctx->sms, s));
+        *kernels += 2;
+        return S3R_OK;
+    }
     S3R_CUDA(p->ctx, launch_frame_render(fa, p->last_view.W, p->last_view.H, p->last_view.tf_n, p->fmt,
                                          p->render_tile, p->last_view.filter, s));
     ++*kernels;
@@ -1560,6 +1649,25 @@ int s3r_frame_plan(s3r_ctx* ctx, const s3r_frame_desc* desc, s3r_plan** out)
         return bail(cuda_fail(ctx, e, "cudaMallocHost(cover)"));
     if ((e = cudaEventCreateWithFlags(&p->staged, cudaEventDisableTiming)) != cudaSuccess)
         return bail(cuda_fail(ctx, e, "cudaEventCreate"));
+    // block-major render: blocks deepest first (most samples per ray), so that the longest work items start first
+    {
+        std::vector<uint32_t> idx(desc->nblocks);
+        for (uint32_t b = 0; b < desc->nblocks; ++b) idx[b] = b;
+        std::stable_sort(idx.begin(), idx.end(),
+                         [&](uint32_t a, uint32_t b) { return p->blocks[4 * a + 3] > p->blocks[4 * b + 3]; });
+        p->seg_order.resize(desc->nblocks);
+        for (uint32_t i = 0; i < desc->nblocks; ++i) {
+            const uint32_t* bl = &p->blocks[4 * idx[i]];
+            p->seg_order[i] = bl[0] + m * (bl[1] + m * bl[2]);
+        }
+        if ((rc = upload(ctx, &p->seg_order_dev, p->seg_order))) return bail(rc);
+        const size_t pf = (size_t)kSegShapes * (desc->nblocks + 1);
+        if ((e = cudaMalloc(&p->seg_prefix_dev, pf * sizeof(uint32_t))) != cudaSuccess ||
+            (e = cudaMallocHost(&p->seg_prefix_pinned, pf * sizeof(uint32_t))) != cudaSuccess ||
+            (e = cudaMalloc(&p->seg_queue, 2 * sizeof(uint32_t))) != cudaSuccess ||
+            (e = cudaMemset(p->seg_queue, 0, 2 * sizeof(uint32_t))) != cudaSuccess)
+            return bail(cuda_fail(ctx, e, "cudaMalloc(block-major render)"));
+    }
     if ((rc = plan_bin(p, tl))) return bail(rc);
     *out = p;
     return S3R_OK;
@@ -1588,6 +1696,11 @@ int s3r_plan_destroy(s3r_plan* p)
     if (p->cover_pinned) cudaFreeHost(p->cover_pinned);
     f(p->cover_dev);
     f(p->dtf_part);
+    f(p->seg_order_dev);
+    f(p->seg_prefix_dev);
+    f(p->seg_queue);
+    if (p->seg_prefix_pinned) cudaFreeHost(p->seg_prefix_pinned);
+    plan_free_segments(p);
     if (p->staged) cudaEventDestroy(p->staged);
     delete p;
     return S3R_OK;
@@ -1966,8 +2079,14 @@ int s3r_plan_autotune(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const 
     best = 3.4e38f;
     for (uint32_t shape = 0; shape < (uint32_t)kRenderTiles; ++shape) {
         // several lanes per ray only where rays composite every block (alpha_stop >= 1)
-        if (shape >= (uint32_t)kRenderShapes && view->alpha_stop < 1.f) break;
+        if (shape >= (uint32_t)kRenderShapes && shape < (uint32_t)kRenderWalkTiles && view->alpha_stop < 1.f) continue;
         plan->render_tile = shape;
+        if (shape >= (uint32_t)kRenderWalkTiles && plan_ensure_segments(plan, view->W, view->H) != S3R_OK) {
+            // no room for the block-major buffers: keep to the per-ray walk
+            ctx->err.clear();
+            set_thread_error("");
+            continue;
+        }
         float ms = 0;
         rc = timed([&](uint32_t* kk) { return plan_launch_render(plan, tf, img, nullptr, nullptr, s, kk); }, ms);
         if (rc) return cleanup(rc);
@@ -1978,6 +2097,11 @@ int s3r_plan_autotune(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const 
     }
     plan->render_tile = best_shape;
     plan_drop_graph(plan);
+    if (best_shape < (uint32_t)kRenderWalkTiles) {
+        // the per-ray walk won: release the block-major buffers
+        cudaStreamSynchronize(s);
+        plan_free_segments(plan);
+    }
     return cleanup(S3R_OK);
 }
 

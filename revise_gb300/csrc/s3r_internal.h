@@ -113,6 +113,19 @@ struct FrameArgs {
     float* dtf_part;      // kDtfParts zeroed copies of dtf (tf_n RGBA float4 each), summed into dtf afterwards
 };
 
+// The block-major frame render (render tile ids kRenderWalkTiles and up): its work
+// items and per-pixel block results.
+constexpr uint32_t kSegMaskWords = 6; // rank masks of up to 384 ranks: levels <= 7
+struct SegArgs {
+    const uint32_t* order;      // the plan's block cells, deepest first
+    const uint32_t* prefix;     // nblocks + 1 running counts of view-rectangle tiles in that order
+    uint32_t nblocks;
+    uint32_t words;             // mask words per pixel: ceil((3m - 2) / 64)
+    float4* seg;                // [rank][pixel] premultiplied block results
+    unsigned long long* mask;   // [word][pixel] ranks holding a result
+    uint32_t* queue;            // work-queue counter: 0 before the segment launch, zeroed again by the composite
+};
+
 // The adjoint spreads its transfer-function gradient over kDtfParts copies
 // (CTA index modulo kDtfCtaGroups, lane modulo kDtfLaneGroups) so that global
 // reductions to one table entry rarely meet; a last kernel sums the copies.
@@ -179,6 +192,10 @@ cudaError_t launch_render_block_argb(const s3r_view* view_host, const float* bri
                                      const float* tf, uint32_t* viewport, cudaStream_t s);
 cudaError_t launch_frame_render(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, uint32_t fmt,
                                 uint32_t tile_shape, uint32_t filter, cudaStream_t s);
+// The block-major form: segment kernel (persistent grid of ctas CTAs, 0: as many as fit on sms SMs) over
+// the work items of footprint `shape`, then the composite kernel over all W x H pixels.
+cudaError_t launch_frame_segments(const FrameArgs& a, const SegArgs& sa, uint32_t W, uint32_t H, uint32_t tf_n,
+                                  uint32_t fmt, uint32_t shape, uint32_t filter, uint32_t sms, cudaStream_t s);
 cudaError_t launch_frame_render_mode(const FrameArgs& a, const s3r_presentation& pres, const float* bricks2,
                                      uint32_t W, uint32_t H, uint32_t tf_n, uint32_t filter, cudaStream_t s);
 cudaError_t launch_frame_backward(const FrameArgs& a, uint32_t W, uint32_t H, uint32_t tf_n, cudaStream_t s);
@@ -190,11 +207,19 @@ cudaError_t launch_crop(const uint32_t* img, uint32_t W, const int32_t rect[4], 
 cudaError_t launch_compose(const s3r_image_part* parts_dev, uint32_t nparts, int32_t just_copy_first, uint32_t* dst,
                            int32_t dw, int32_t dh, int32_t offx, int32_t offy, cudaStream_t s);
 
-// Render CTA pixel shapes the autotuner chooses from: {x, y} pixels; a render
-// tile id is shape + kRenderShapes * log2(lanes per ray), lanes per ray 1..8.
+// Render CTA pixel shapes the autotuner chooses from: {x, y} pixels.  A render
+// tile id below kRenderWalkTiles is a per-ray walk (frame_render_kernel), shape +
+// kRenderShapes * log2(lanes per ray), lanes per ray 1..8; the kSegShapes ids
+// from kRenderWalkTiles up are the block-major form with item footprint
+// kSegShapeX x kSegShapeY pixels.
 constexpr int kRenderShapes = 4;
-constexpr int kRenderTiles = kRenderShapes * 4;
+constexpr int kRenderWalkTiles = kRenderShapes * 4;
+constexpr int kSegShapes = 3;
+constexpr int kRenderTiles = kRenderWalkTiles + kSegShapes;
 constexpr int kRenderShapeX[kRenderShapes] = {16, 32, 8, 16};
 constexpr int kRenderShapeY[kRenderShapes] = {8, 4, 8, 16};
+static_assert(kRenderWalkTiles == S3R_RENDER_TILES_WALK && kRenderTiles == S3R_RENDER_TILES, "render tile ids");
+constexpr int kSegShapeX[kSegShapes] = {16, 32, 8};
+constexpr int kSegShapeY[kSegShapes] = {8, 4, 16};
 
 } // namespace s3r

@@ -207,9 +207,9 @@ def test_16bit_bricks_image_error_is_bounded(ctx, fmt):
 
 
 def test_render_tiles_agree(ctx):
-    """Every CTA shape and lanes-per-ray choice renders the same cfg2 frame: R = 1
-    shapes bit-identical, R > 1 (partial composites merged by shuffles in another
-    association order) within 1e-5."""
+    """Every render form and CTA shape renders the same cfg2 frame: the per-ray walk
+    with R = 1 and the block-major forms bit-identical, R > 1 (partial composites
+    merged by shuffles in another association order) within 1e-5."""
     import torch
     from revise_gb300.api import FramePlan
     w = workloads.cfg2()
@@ -217,7 +217,7 @@ def test_render_tiles_agree(ctx):
     sp, tf = _dev(w.sparse), _dev(w.tf)
     rgba = torch.zeros(w.W * w.H * 4, device="cuda")
     base = None
-    for rt in range(16):
+    for rt in range(_lib.RENDER_TILES):
         plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=16, render_tile=rt)
         rgba.fill_(-1.0)
         plan.interp(sp)
@@ -230,17 +230,63 @@ def test_render_tiles_agree(ctx):
             base = img
             continue
         d = float((img - base).abs().max())
-        assert d == 0.0 if rt < 4 else d <= 1e-5, (rt, d)
+        assert d == 0.0 if (rt < 4 or rt >= _lib.RENDER_TILES_WALK) else d <= 1e-5, (rt, d)
 
 
-def test_graph_recaptured_when_viewport_tf_size_or_filter_change(ctx):
+@pytest.mark.parametrize("case", ["level5", "f16", "texture", "alpha_stop", "eye_inside"])
+def test_block_major_render_matches_walk(ctx, case):
+    """The block-major forms against the per-ray walk (render tile 0), bit for bit, RGBA and ARGB32:
+    a level-5 block set (94 front-to-back ranks: two mask words per pixel), 16-bit bricks, the
+    texture filter, a ray stop at alpha 0.9, and an eye inside the block grid (rays of both signs
+    along every axis); with no ray stop the sample counts agree too."""
+    import torch
+    from revise_gb300.api import FramePlan
+    fmt, filt, alpha_stop, eye = _lib.BRICK_F32, _lib.FILTER_EXACT, 2.0, None
+    if case == "level5":
+        w = workloads.small(seed=3, level=5, depths=(1, 2), W=160, H=120)
+    else:
+        w = workloads.small(seed=4, level=2, depths=(2, 3, 4), W=128, H=96)
+    if case == "f16":
+        fmt = _lib.BRICK_F16
+    elif case == "texture":
+        filt = _lib.FILTER_TEXTURE
+    elif case == "alpha_stop":
+        alpha_stop = 0.9
+    elif case == "eye_inside":
+        eye = (0.7, -0.4, 1.1)
+    view = host.view_for(w, alpha_stop=alpha_stop, filter=filt, eye=eye)
+    sp, tf = _dev(w.sparse), _dev(w.tf)
+    out = {}
+    for rt in [0, *range(_lib.RENDER_TILES_WALK, _lib.RENDER_TILES)]:
+        plan = FramePlan(ctx, w, fmt, tile_cells=16, render_tile=rt)
+        rgba = torch.full((w.W * w.H * 4,), -1.0, device="cuda")
+        argb = torch.zeros(w.W * w.H, dtype=torch.int32, device="cuda")
+        samples = torch.zeros(1, dtype=torch.int64, device="cuda")
+        plan.interp(sp)
+        plan.render(view, tf, rgba, argb, samples)
+        # twice: the second frame starts from the masks and counter the first one left
+        plan.render(view, tf, rgba, argb)
+        torch.cuda.synchronize()
+        out[rt] = (rgba.cpu().numpy(), argb.cpu().numpy(), int(samples.item()))
+        plan.close()
+    base_rgba, base_argb, base_samples = out[0]
+    assert base_rgba.min() >= 0.0 and (base_rgba[3::4] > 0).mean() > 0.02
+    for rt, (rgba, argb, samples) in out.items():
+        assert np.array_equal(rgba.view(np.uint32), base_rgba.view(np.uint32)), rt
+        assert np.array_equal(argb, base_argb), rt
+        if alpha_stop >= 1.0:
+            assert samples == base_samples, (rt, samples, base_samples)
+
+
+@pytest.mark.parametrize("render_tile", [0, _lib.RENDER_TILES_WALK])
+def test_graph_recaptured_when_viewport_tf_size_or_filter_change(ctx, render_tile):
     """Same buffers, different W x H, tf_n or filter between replays: each replay
     must equal a direct render of its own view (the graph's launch dimensions and
-    shared-memory size follow the view)."""
+    shared-memory size follow the view; the block-major buffers grow with W x H)."""
     import torch
     from revise_gb300.api import FramePlan
     w = workloads.small(seed=14, level=1, depths=(2, 3), W=96, H=72)
-    plan = FramePlan(ctx, w)
+    plan = FramePlan(ctx, w, render_tile=render_tile)
     sp = _dev(w.sparse)
     tf512 = _dev(host.make_color_transfer(*workloads.colormap_points(), 512))
     a = torch.zeros(128 * 96 * 4, device="cuda")

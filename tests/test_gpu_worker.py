@@ -126,15 +126,17 @@ def test_scene_part_from_plan_bricks_equals_native_loop(ctx, filt):
     plan.close()
 
 
-def test_frame_run_host_pipeline_matches_device_frames(ctx):
+@pytest.mark.parametrize("render_tile", [0, _lib.RENDER_TILES_WALK + 1])
+def test_frame_run_host_pipeline_matches_device_frames(ctx, render_tile):
     """s3r_frame_run_host over several frames with changing sparse values: every image equals the one
-    s3r_frame_run makes from device buffers (the two slots alternate and never mix frames)."""
+    s3r_frame_run makes from device buffers (the two slots alternate and never mix frames), with the
+    per-ray walk and with the block-major render (per-slot result buffers, masks and counters)."""
     import torch
     from revise_gb300 import host
     from revise_gb300.api import FramePlan
     w = workloads.small(seed=21, level=1, depths=(2, 3, 4), W=80, H=64)
     view = host.view_for(w)
-    plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=8)
+    plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=8, render_tile=render_tile)
     tf = torch.from_numpy(np.ascontiguousarray(w.tf)).cuda()
     rng = np.random.default_rng(3)
     frames = [(w.sparse * np.float32(1 + 0.1 * k) + np.float32(rng.normal())).astype(np.float32) for k in range(5)]
@@ -155,8 +157,9 @@ def test_frame_run_host_pipeline_matches_device_frames(ctx):
     plan.close()
 
 
+@pytest.mark.parametrize("render_tile", [0, _lib.RENDER_TILES_WALK])
 @pytest.mark.parametrize("fmt", [_lib.BRICK_F32, _lib.BRICK_F16, _lib.BRICK_BF16])
-def test_frame_run_host_view_change_and_tf_reuse(ctx, fmt):
+def test_frame_run_host_view_change_and_tf_reuse(ctx, fmt, render_tile):
     """s3r_frame_run_host with 16-bit bricks in both slots (the second slot's per-brick scales) and a view
     that changes mid-sequence (frames 0-2 one camera, 3-5 another, while the other slot is in flight);
     after every call the caller overwrites its transfer function on the same stream, which the frame
@@ -166,7 +169,7 @@ def test_frame_run_host_view_change_and_tf_reuse(ctx, fmt):
     from revise_gb300.api import FramePlan
     w = workloads.small(seed=23, level=1, depths=(2, 3, 4), W=80, H=64)
     views = [host.view_for(w), host.view_for(w, eye=(3.0, 12.0, 30.0))]
-    plan = FramePlan(ctx, w, fmt, tile_cells=8)
+    plan = FramePlan(ctx, w, fmt, tile_cells=8, render_tile=render_tile)
     tf0 = np.ascontiguousarray(w.tf)
     rng = np.random.default_rng(5)
     frames = [(w.sparse * np.float32(1 + 0.1 * k) + np.float32(rng.normal())).astype(np.float32) for k in range(6)]

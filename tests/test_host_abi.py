@@ -28,6 +28,18 @@ def test_library_loads_and_exports_every_declared_symbol(lib):
     assert set(_lib.EXPORTED) <= set(syms)
 
 
+def test_header_constants_match_the_bindings():
+    text = (ROOT / "include" / "s3r.h").read_text()
+
+    def define(name):
+        return int(re.search(rf"#define {name} (\d+)u?", text).group(1))
+
+    assert define("S3R_RENDER_TILES_WALK") == _lib.RENDER_TILES_WALK
+    assert define("S3R_RENDER_TILES") == _lib.RENDER_TILES
+    assert define("S3R_ABI_VERSION") == _lib.ABI_VERSION
+    assert define("S3R_MAX_DEPTH") == _lib.MAX_DEPTH
+
+
 def test_b2f_order_matches_reference(golden):
     for i in range(int(golden["b2f_count"])):
         a = golden[f"b2f_{i}_args"]
