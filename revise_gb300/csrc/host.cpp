@@ -104,9 +104,12 @@ struct s3r_plan {
     // them (staged with the view), per data slot the per-rank block results and rank masks, and one
     // work-queue counter per data slot
     std::vector<uint32_t> seg_order;
-    uint32_t* seg_order_dev = nullptr;
-    uint32_t* seg_prefix_dev = nullptr; // kSegShapes x (nblocks + 1)
-    uint32_t* seg_prefix_pinned = nullptr;
+    uint2* seg_items_pinned = nullptr;  // {cell, tile} per warp work item, staged with the view
+    uint2* seg_items_dev = nullptr;
+    uint64_t seg_items_cap = 0, seg_items_dev_cap = 0;
+    uint32_t* seg_count_pinned = nullptr;
+    uint32_t* seg_count_dev = nullptr;  // items staged
+    int seg_staged_shape = -1;          // the footprint the staged items are cut for
     uint32_t* seg_queue = nullptr;      // 2 counters
     float4* seg_buf[2] = {nullptr, nullptr};
     unsigned long long* seg_mask[2] = {nullptr, nullptr};
@@ -753,7 +756,9 @@ int plan_stage_view(s3r_plan* p, const s3r_view* view, cudaStream_t s)
 {
     s3r_ctx* ctx = p->ctx;
     if (int rc = plan_ensure_segments(p, view->W, view->H)) return rc;
-    const bool same = p->have_view && std::memcmp(&p->last_view, view, sizeof(s3r_view)) == 0;
+    const bool seg = p->render_tile >= (uint32_t)kRenderWalkTiles;
+    const bool same = p->have_view && std::memcmp(&p->last_view, view, sizeof(s3r_view)) == 0 &&
+                      (!seg || p->seg_staged_shape == (int)(p->render_tile - (uint32_t)kRenderWalkTiles));
     if (same) return S3R_OK;
     // the staging buffers may still feed an earlier copy
     S3R_CUDA(ctx, cudaEventSynchronize(p->staged));
@@ -774,21 +779,51 @@ int plan_stage_view(s3r_plan* p, const s3r_view* view, cudaStream_t s)
         }
     }
     if (cover[0] > cover[2]) cover[0] = cover[1] = cover[2] = cover[3] = 0;
-    // block-major render: per item footprint the running count of view-rectangle tiles, deepest blocks first
-    for (int f = 0; f < kSegShapes; ++f) {
-        uint32_t* pf = p->seg_prefix_pinned + (size_t)f * (p->nblocks + 1);
-        uint64_t run = 0;
+    // block-major render: the warp-sized tiles of every block's view rectangle, deepest blocks first
+    if (p->render_tile >= (uint32_t)kRenderWalkTiles) {
+        const int f = (int)(p->render_tile - (uint32_t)kRenderWalkTiles);
+        const int fx = kSegShapeX[f], fy = kSegShapeY[f];
+        uint64_t n = 0;
         for (uint32_t i = 0; i < p->nblocks; ++i) {
-            pf[i] = (uint32_t)run;
             const int32_t* r = tb[p->seg_order[i]].rect;
-            if (r[2] > 0 && r[3] > 0)
-                run += (uint64_t)((r[2] + kSegShapeX[f] - 1) / kSegShapeX[f]) * ((r[3] + kSegShapeY[f] - 1) / kSegShapeY[f]);
+            if (r[2] > 0 && r[3] > 0) n += (uint64_t)((r[2] + fx - 1) / fx) * ((r[3] + fy - 1) / fy);
         }
-        if (run > 0xffffffffull) return fail(ctx, S3R_ERR_INVALID, "too many block-major render items");
-        pf[p->nblocks] = (uint32_t)run;
+        if (n > 0xffffffffull) return fail(ctx, S3R_ERR_INVALID, "too many block-major render items");
+        cudaError_t e;
+        if (n > p->seg_items_cap) {
+            if (p->seg_items_pinned) cudaFreeHost(p->seg_items_pinned);
+            p->seg_items_pinned = nullptr;
+            p->seg_items_cap = 0;
+            if ((e = cudaMallocHost(&p->seg_items_pinned, n * sizeof(uint2))) != cudaSuccess)
+                return cuda_fail(ctx, e, "cudaMallocHost(block-major items)");
+            p->seg_items_cap = n;
+        }
+        if (n > p->seg_items_dev_cap) {
+            // frames in flight or captured may hold the old list
+            S3R_CUDA(ctx, cudaDeviceSynchronize());
+            plan_drop_graph(p);
+            if (p->seg_items_dev) cudaFree(p->seg_items_dev);
+            p->seg_items_dev = nullptr;
+            p->seg_items_dev_cap = 0;
+            if ((e = cudaMalloc(&p->seg_items_dev, n * sizeof(uint2))) != cudaSuccess)
+                return cuda_fail(ctx, e, "cudaMalloc(block-major items)");
+            p->seg_items_dev_cap = n;
+        }
+        uint2* it = p->seg_items_pinned;
+        for (uint32_t i = 0; i < p->nblocks; ++i) {
+            const uint32_t cell = p->seg_order[i];
+            const int32_t* r = tb[cell].rect;
+            if (r[2] <= 0 || r[3] <= 0) continue;
+            const uint32_t tiles = (uint32_t)(((r[2] + fx - 1) / fx) * ((r[3] + fy - 1) / fy));
+            for (uint32_t t = 0; t < tiles; ++t) *it++ = make_uint2(cell, t);
+        }
+        *p->seg_count_pinned = (uint32_t)n;
+        if (n) S3R_CUDA(ctx, cudaMemcpyAsync(p->seg_items_dev, p->seg_items_pinned, n * sizeof(uint2),
+                                             cudaMemcpyHostToDevice, s));
+        S3R_CUDA(ctx, cudaMemcpyAsync(p->seg_count_dev, p->seg_count_pinned, sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                      s));
+        p->seg_staged_shape = f;
     }
-    S3R_CUDA(ctx, cudaMemcpyAsync(p->seg_prefix_dev, p->seg_prefix_pinned,
-                                  (size_t)kSegShapes * (p->nblocks + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
     std::memcpy(p->cover_pinned, cover, sizeof(cover));
     S3R_CUDA(ctx, cudaMemcpyAsync(p->cover_dev, p->cover_pinned, sizeof(cover), cudaMemcpyHostToDevice, s));
     *p->view_pinned = *view;
@@ -848,9 +883,10 @@ int plan_launch_render(s3r_plan* p, const float* tf, float* rgba, uint32_t* argb
             return fail(p->ctx, S3R_ERR_INVALID, "block-major render buffers not allocated for this view");
         const uint32_t shape = p->render_tile - (uint32_t)kRenderWalkTiles;
         SegArgs sa{};
-        sa.order = p->seg_order_dev;
-        sa.prefix = p->seg_prefix_dev + (size_t)shape * (p->nblocks + 1);
-        sa.nblocks = p->nblocks;
+        if (p->seg_staged_shape != (int)shape || !p->seg_items_dev)
+            return fail(p->ctx, S3R_ERR_INVALID, "block-major render items not staged for this render tile");
+        sa.items = p->seg_items_dev;
+        sa.count = p->seg_count_dev;
         sa.words = p->seg_words;
         sa.seg = p->seg_buf[data];
         sa.mask = p->seg_mask[data];
@@ -1660,10 +1696,8 @@ int s3r_frame_plan(s3r_ctx* ctx, const s3r_frame_desc* desc, s3r_plan** out)
             const uint32_t* bl = &p->blocks[4 * idx[i]];
             p->seg_order[i] = bl[0] + m * (bl[1] + m * bl[2]);
         }
-        if ((rc = upload(ctx, &p->seg_order_dev, p->seg_order))) return bail(rc);
-        const size_t pf = (size_t)kSegShapes * (desc->nblocks + 1);
-        if ((e = cudaMalloc(&p->seg_prefix_dev, pf * sizeof(uint32_t))) != cudaSuccess ||
-            (e = cudaMallocHost(&p->seg_prefix_pinned, pf * sizeof(uint32_t))) != cudaSuccess ||
+        if ((e = cudaMalloc(&p->seg_count_dev, sizeof(uint32_t))) != cudaSuccess ||
+            (e = cudaMallocHost(&p->seg_count_pinned, sizeof(uint32_t))) != cudaSuccess ||
             (e = cudaMalloc(&p->seg_queue, 2 * sizeof(uint32_t))) != cudaSuccess ||
             (e = cudaMemset(p->seg_queue, 0, 2 * sizeof(uint32_t))) != cudaSuccess)
             return bail(cuda_fail(ctx, e, "cudaMalloc(block-major render)"));
@@ -1696,10 +1730,11 @@ int s3r_plan_destroy(s3r_plan* p)
     if (p->cover_pinned) cudaFreeHost(p->cover_pinned);
     f(p->cover_dev);
     f(p->dtf_part);
-    f(p->seg_order_dev);
-    f(p->seg_prefix_dev);
+    f(p->seg_items_dev);
+    f(p->seg_count_dev);
     f(p->seg_queue);
-    if (p->seg_prefix_pinned) cudaFreeHost(p->seg_prefix_pinned);
+    if (p->seg_items_pinned) cudaFreeHost(p->seg_items_pinned);
+    if (p->seg_count_pinned) cudaFreeHost(p->seg_count_pinned);
     plan_free_segments(p);
     if (p->staged) cudaEventDestroy(p->staged);
     delete p;
@@ -2081,7 +2116,8 @@ int s3r_plan_autotune(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const 
         // several lanes per ray only where rays composite every block (alpha_stop >= 1)
         if (shape >= (uint32_t)kRenderShapes && shape < (uint32_t)kRenderWalkTiles && view->alpha_stop < 1.f) continue;
         plan->render_tile = shape;
-        if (shape >= (uint32_t)kRenderWalkTiles && plan_ensure_segments(plan, view->W, view->H) != S3R_OK) {
+        // the block-major forms' buffers and their footprint's work items
+        if (shape >= (uint32_t)kRenderWalkTiles && plan_stage_view(plan, view, s) != S3R_OK) {
             // no room for the block-major buffers: keep to the per-ray walk
             ctx->err.clear();
             set_thread_error("");

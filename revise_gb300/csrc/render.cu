@@ -1230,85 +1230,90 @@ __device__ __forceinline__ uint32_t ray_rank(const float dir[3], uint32_t ix, ui
     return (dir[0] < 0.f ? m - 1 - ix : ix) + (dir[1] < 0.f ? m - 1 - iy : iy) + (dir[2] < 0.f ? m - 1 - iz : iz);
 }
 
-// Block-major ray cast: the work items are the CTA-sized pixel tiles of every
+// Block-major ray cast: the work items are the warp-sized pixel tiles of every
 // block's view rectangle, blocks in decreasing depth (most samples per ray
-// first), taken from a work-queue counter by a persistent grid.  A thread marches
-// its pixel's ray through the item's block exactly as frame_render_kernel does
-// (pixel_ray, block_ray, march_block) and stores the premultiplied result at the
-// block's front-to-back rank on that ray, marking the rank in the pixel's mask; a
-// zero result changes no composite and is not stored.  The warps of an item all
-// read one brick, their rays cross it side by side (similar sample counts), and
-// the deep blocks' items are spread over every SM -- the per-ray walk's lanes
+// first); each warp of a persistent grid takes items from a work-queue counter on
+// its own, fetching the next item while it marches the current one.  A lane
+// marches its pixel's ray through the item's block exactly as frame_render_kernel
+// does (pixel_ray, block_ray, march_block) and stores the premultiplied result at
+// the block's front-to-back rank on that ray, marking the rank in the pixel's
+// mask; a zero result changes no composite and is not stored.  The lanes of an
+// item read one brick, their rays cross it side by side (similar sample counts),
+// and the deep blocks' items spread over every SM -- the per-ray walk's lanes
 // instead each hold their own block sequence.  frame_composite_kernel then blends
 // every pixel's results in rank order with frame_render_kernel's arithmetic.
 template <int Fmt, bool kTex>
-__global__ void __launch_bounds__(128) frame_segments_kernel(FrameArgs fa, SegArgs sa)
+__global__ void __launch_bounds__(128, 8) frame_segments_kernel(FrameArgs fa, SegArgs sa, uint32_t fx)
 {
     extern __shared__ float4 tf[];
-    __shared__ uint32_t item_s, cell_s, tile_s;
     const s3r_view v = *fa.view;
     const uint32_t nthreads = blockDim.x * blockDim.y;
     const uint32_t tid = threadIdx.y * blockDim.x + threadIdx.x;
     for (uint32_t i = tid; i < v.tf_n; i += nthreads) tf[i] = reinterpret_cast<const float4*>(fa.tf)[i];
-    const uint32_t total = sa.prefix[sa.nblocks];
+    __syncthreads();
+    const uint32_t lane = tid & 31u;
+    const uint32_t fy = 32u / fx;
+    const uint32_t total = *sa.count;
     const uint32_t m = 1u << v.level;
     const uint64_t npix = (uint64_t)v.W * v.H;
     const float of = (v.threshold - v.field_min) / (v.field_max - v.field_min);
     uint32_t taken = 0;
-    for (;;) {
-        __syncthreads(); // the previous item's ids are read; the table is loaded
-        if (tid == 0) {
-            const uint32_t item = atomicAdd(sa.queue, 1u);
-            uint32_t cell = 0, tile = 0;
-            if (item < total) {
-                // the block whose tiles hold this item: the last j with prefix[j] <= item
-                uint32_t lo = 0, hi = sa.nblocks;
-                while (hi - lo > 1) {
-                    const uint32_t mid = (lo + hi) >> 1;
-                    if (sa.prefix[mid] <= item) lo = mid;
-                    else hi = mid;
-                }
-                cell = sa.order[lo];
-                tile = item - sa.prefix[lo];
-            }
-            item_s = item;
-            cell_s = cell;
-            tile_s = tile;
+    auto take = [&](uint32_t& item, uint2& desc) {
+        item = 0xffffffffu;
+        desc = make_uint2(0u, 0u);
+        if (lane == 0) {
+            item = atomicAdd(sa.queue, 1u);
+            if (item < total) desc = sa.items[item];
         }
-        __syncthreads();
-        if (item_s >= total) break;
-        const uint32_t cell = cell_s, tile = tile_s;
+    };
+    uint32_t item;
+    uint2 desc;
+    take(item, desc);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    desc.x = __shfl_sync(0xffffffffu, desc.x, 0);
+    desc.y = __shfl_sync(0xffffffffu, desc.y, 0);
+    while (item < total) {
+        uint32_t next;
+        uint2 ndesc;
+        take(next, ndesc); // in flight while this item is marched
+        const uint32_t cell = desc.x, tile = desc.y;
         const RenderBlock* rb = &fa.table[cell];
         const int4 rc = *reinterpret_cast<const int4*>(rb->rect);
-        const uint32_t tiles_x = ((uint32_t)rc.z + blockDim.x - 1) / blockDim.x;
-        const int32_t x = rc.x + (int32_t)((tile % tiles_x) * blockDim.x + threadIdx.x);
-        const int32_t y = rc.y + (int32_t)((tile / tiles_x) * blockDim.y + threadIdx.y);
-        if (x >= rc.x + rc.z || y >= rc.y + rc.w || x < 0 || y < 0 || x >= (int32_t)v.W || y >= (int32_t)v.H) continue;
-        float org[3], dir[3];
-        pixel_ray(v, (uint32_t)x, (uint32_t)y, org, dir);
-        BlockRay r;
-        if (!block_ray(v, org, dir, *rb, r)) continue;
-        const char* base = reinterpret_cast<const char*>(fa.bricks);
-        const size_t esz = Fmt == S3R_BRICK_F32 ? 4 : 2;
-        float scale = 1.f, offset = 0.f;
-        if (Fmt != S3R_BRICK_F32) {
-            const float2 so = fa.scale_offset[rb->block];
-            scale = so.x;
-            offset = so.y;
+        const uint32_t tiles_x = ((uint32_t)rc.z + fx - 1) / fx;
+        const int32_t x = rc.x + (int32_t)((tile % tiles_x) * fx + lane % fx);
+        const int32_t y = rc.y + (int32_t)((tile / tiles_x) * fy + lane / fx);
+        if (x < rc.x + rc.z && y < rc.y + rc.w && x >= 0 && y >= 0 && x < (int32_t)v.W && y < (int32_t)v.H) {
+            float org[3], dir[3];
+            pixel_ray(v, (uint32_t)x, (uint32_t)y, org, dir);
+            BlockRay r;
+            if (block_ray(v, org, dir, *rb, r)) {
+                const char* base = reinterpret_cast<const char*>(fa.bricks);
+                const size_t esz = Fmt == S3R_BRICK_F32 ? 4 : 2;
+                float scale = 1.f, offset = 0.f;
+                if (Fmt != S3R_BRICK_F32) {
+                    const float2 so = fa.scale_offset[rb->block];
+                    scale = so.x;
+                    offset = so.y;
+                }
+                const Premul p = march_block<Fmt, kTex>(v, r, base + rb->brick_off * esz, scale, offset, rb->depth,
+                                                        tf, of, taken);
+                if (!(p.r == 0.f && p.g == 0.f && p.b == 0.f && p.a == 0.f)) {
+                    const uint32_t ix = cell % m, iy = (cell / m) % m, iz = cell / (m * m);
+                    const uint32_t k = ray_rank(dir, ix, iy, iz, m);
+                    const uint64_t pix = (uint64_t)y * v.W + (uint32_t)x;
+                    sa.seg[(uint64_t)k * npix + pix] = make_float4(p.r, p.g, p.b, p.a);
+                    atomicOr(&sa.mask[(uint64_t)(k >> 6) * npix + pix], 1ull << (k & 63));
+                }
+            }
         }
-        const Premul p =
-            march_block<Fmt, kTex>(v, r, base + rb->brick_off * esz, scale, offset, rb->depth, tf, of, taken);
-        if (p.r == 0.f && p.g == 0.f && p.b == 0.f && p.a == 0.f) continue;
-        const uint32_t ix = cell % m, iy = (cell / m) % m, iz = cell / (m * m);
-        const uint32_t k = ray_rank(dir, ix, iy, iz, m);
-        const uint64_t pix = (uint64_t)y * v.W + (uint32_t)x;
-        sa.seg[(uint64_t)k * npix + pix] = make_float4(p.r, p.g, p.b, p.a);
-        atomicOr(&sa.mask[(uint64_t)(k >> 6) * npix + pix], 1ull << (k & 63));
+        item = __shfl_sync(0xffffffffu, next, 0);
+        desc.x = __shfl_sync(0xffffffffu, ndesc.x, 0);
+        desc.y = __shfl_sync(0xffffffffu, ndesc.y, 0);
     }
     if (fa.samples) {
         unsigned long long t = taken;
         for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if ((tid & 31) == 0 && t) atomicAdd(fa.samples, t);
+        if (lane == 0 && t) atomicAdd(fa.samples, t);
     }
 }
 
@@ -1762,8 +1767,8 @@ cudaError_t launch_frame_render(const FrameArgs& a, uint32_t W, uint32_t H, uint
 }
 
 template <int Fmt, bool kTex>
-cudaError_t launch_frame_segments_fmt(const FrameArgs& a, const SegArgs& sa, dim3 block, size_t smem, uint32_t sms,
-                                      cudaStream_t s)
+cudaError_t launch_frame_segments_fmt(const FrameArgs& a, const SegArgs& sa, uint32_t fx, dim3 block, size_t smem,
+                                      uint32_t sms, cudaStream_t s)
 {
     auto kernel = frame_segments_kernel<Fmt, kTex>;
     if (smem > 48 * 1024) {
@@ -1773,7 +1778,7 @@ cudaError_t launch_frame_segments_fmt(const FrameArgs& a, const SegArgs& sa, dim
     int per_sm = 0;
     cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, (int)(block.x * block.y), smem);
     if (err != cudaSuccess) return err;
-    kernel<<<sms * (uint32_t)(per_sm > 0 ? per_sm : 1), block, smem, s>>>(a, sa);
+    kernel<<<sms * (uint32_t)(per_sm > 0 ? per_sm : 1), block, smem, s>>>(a, sa, fx);
     return cudaGetLastError();
 }
 
@@ -1782,22 +1787,23 @@ cudaError_t launch_frame_segments(const FrameArgs& a, const SegArgs& sa, uint32_
 {
     if (sa.words > kSegMaskWords) return cudaErrorInvalidValue;
     shape %= kSegShapes;
-    const dim3 block(kSegShapeX[shape], kSegShapeY[shape]);
+    const uint32_t fx = (uint32_t)kSegShapeX[shape];
+    const dim3 block(128); // four warps, each on its own items
     const size_t smem = tf_n * sizeof(float4);
     const bool tex = filter == S3R_FILTER_TEXTURE;
     cudaError_t err;
     switch (fmt) {
     case S3R_BRICK_F32:
-        err = tex ? launch_frame_segments_fmt<S3R_BRICK_F32, true>(a, sa, block, smem, sms, s)
-                  : launch_frame_segments_fmt<S3R_BRICK_F32, false>(a, sa, block, smem, sms, s);
+        err = tex ? launch_frame_segments_fmt<S3R_BRICK_F32, true>(a, sa, fx, block, smem, sms, s)
+                  : launch_frame_segments_fmt<S3R_BRICK_F32, false>(a, sa, fx, block, smem, sms, s);
         break;
     case S3R_BRICK_F16:
-        err = tex ? launch_frame_segments_fmt<S3R_BRICK_F16, true>(a, sa, block, smem, sms, s)
-                  : launch_frame_segments_fmt<S3R_BRICK_F16, false>(a, sa, block, smem, sms, s);
+        err = tex ? launch_frame_segments_fmt<S3R_BRICK_F16, true>(a, sa, fx, block, smem, sms, s)
+                  : launch_frame_segments_fmt<S3R_BRICK_F16, false>(a, sa, fx, block, smem, sms, s);
         break;
     case S3R_BRICK_BF16:
-        err = tex ? launch_frame_segments_fmt<S3R_BRICK_BF16, true>(a, sa, block, smem, sms, s)
-                  : launch_frame_segments_fmt<S3R_BRICK_BF16, false>(a, sa, block, smem, sms, s);
+        err = tex ? launch_frame_segments_fmt<S3R_BRICK_BF16, true>(a, sa, fx, block, smem, sms, s)
+                  : launch_frame_segments_fmt<S3R_BRICK_BF16, false>(a, sa, fx, block, smem, sms, s);
         break;
     default: return cudaErrorInvalidValue;
     }

@@ -117,9 +117,9 @@ struct FrameArgs {
 // items and per-pixel block results.
 constexpr uint32_t kSegMaskWords = 6; // rank masks of up to 384 ranks: levels <= 7
 struct SegArgs {
-    const uint32_t* order;      // the plan's block cells, deepest first
-    const uint32_t* prefix;     // nblocks + 1 running counts of view-rectangle tiles in that order
-    uint32_t nblocks;
+    const uint2* items;         // {block cell, tile} per warp work item: the footprint-sized tiles of every
+                                // block's view rectangle, deepest blocks first
+    const uint32_t* count;      // items
     uint32_t words;             // mask words per pixel: ceil((3m - 2) / 64)
     float4* seg;                // [rank][pixel] premultiplied block results
     unsigned long long* mask;   // [word][pixel] ranks holding a result
@@ -219,7 +219,7 @@ constexpr int kRenderTiles = kRenderWalkTiles + kSegShapes;
 constexpr int kRenderShapeX[kRenderShapes] = {16, 32, 8, 16};
 constexpr int kRenderShapeY[kRenderShapes] = {8, 4, 8, 16};
 static_assert(kRenderWalkTiles == S3R_RENDER_TILES_WALK && kRenderTiles == S3R_RENDER_TILES, "render tile ids");
-constexpr int kSegShapeX[kSegShapes] = {16, 32, 8};
-constexpr int kSegShapeY[kSegShapes] = {8, 4, 16};
+constexpr int kSegShapeX[kSegShapes] = {8, 16, 4}; // one warp's pixels
+constexpr int kSegShapeY[kSegShapes] = {4, 2, 8};
 
 } // namespace s3r
