@@ -76,6 +76,10 @@ struct s3r_plan {
     uint32_t* entry_node_dev = nullptr;
     uint32_t* flags_dev = nullptr;
     uint32_t flag_words = 1;
+    uint32_t* centry_off_dev = nullptr; // per block the sparse nodes on its coarse grid
+    uint2* centry_dev = nullptr;
+    float* coarse_dev[2] = {nullptr, nullptr}; // per data slot: the blocks' coarse grids of the frame
+    bool any_coarse = false;
     uint32_t* queue_dev = nullptr;
     uint64_t* node_off_dev = nullptr;
     float2* scale_offset_dev = nullptr;
@@ -478,6 +482,13 @@ void plan_free_device(s3r_plan* p)
     f(p->entry_local_dev);
     f(p->entry_node_dev);
     f(p->flags_dev);
+    f(p->centry_off_dev);
+    f(p->centry_dev);
+    f(p->coarse_dev[0]);
+    f(p->coarse_dev[1]);
+    p->centry_off_dev = nullptr;
+    p->centry_dev = nullptr;
+    p->coarse_dev[0] = p->coarse_dev[1] = nullptr;
     p->blocks_dev = nullptr;
     p->items_dev = nullptr;
     p->entry_off_dev = nullptr;
@@ -507,9 +518,10 @@ template <class T> int upload(s3r_ctx* ctx, T** dst, const std::vector<T>& src)
 }
 
 // Bins every block's nodes by tile of 2^tile_log2 cells (closed tiles: nodes on
-// shared faces, edges and corners go to every tile containing them; lattice
-// points of the tile grid are left to the coarse descent), builds the coarse
-// index grids and the work-item list (largest tiles first), and uploads them.
+// shared faces, edges and corners go to every tile containing them; in a block
+// of several tiles the lattice points of the tile grid go to the block's coarse
+// grid instead, whose values every frame computes once per block), lists the
+// coarse-grid nodes and the work items (largest tiles first), and uploads them.
 int plan_bin(s3r_plan* p, uint32_t tile_log2)
 {
     s3r_ctx* ctx = p->ctx;
@@ -549,33 +561,6 @@ int plan_bin(s3r_plan* p, uint32_t tile_log2)
         lo = x == 0 ? 0 : (x - 1) / T;
         hi = std::min(x / T, m - 1);
     };
-    // Descent entries of every tile of block b: the sparse nodes on the 27
-    // points of each coarse cube containing the tile (level 0: all 27, deeper:
-    // the 19 midpoints), fn(tile, slot 27*level + point, node).  Needs the
-    // block's coarse grid complete.
-    auto for_descent = [&](uint32_t b, auto&& fn) {
-        const PlanBlock& B = pb[b];
-        const uint32_t L = B.coarse_log2;
-        if (L == 0) return;
-        const uint32_t m = 1u << L, m1 = m + 1;
-        for (uint32_t tz = 0; tz < m; ++tz)
-            for (uint32_t ty = 0; ty < m; ++ty)
-                for (uint32_t tx = 0; tx < m; ++tx) {
-                    const uint64_t t = tiles_off[b] + tx + m * (ty + m * tz);
-                    for (uint32_t l = 0; l < L; ++l) {
-                        const uint32_t cube = 1u << (L - l); // cube edge in tiles
-                        const uint32_t bx = tx & ~(cube - 1), by = ty & ~(cube - 1), bz = tz & ~(cube - 1);
-                        const uint32_t hc = cube >> 1;
-                        for (uint32_t q = 0; q < 27; ++q) {
-                            const uint32_t px = q % 3, py = (q / 3) % 3, pz = q / 9;
-                            if (l > 0 && !(px & 1) && !(py & 1) && !(pz & 1)) continue;
-                            const uint32_t gx = bx + hc * px, gy = by + hc * py, gz = bz + hc * pz;
-                            const int32_t node = coarse[B.coarse_off + gx + m1 * (gy + m1 * gz)];
-                            if (node >= 0) fn(t, 27 * l + q, node);
-                        }
-                    }
-                }
-    };
     // pass 1: counts and coarse grids
     parallel([&](uint32_t b) {
         const PlanBlock& B = pb[b];
@@ -594,7 +579,6 @@ int plan_bin(s3r_plan* p, uint32_t tile_log2)
                     for (uint32_t tx = xl; tx <= xh; ++tx)
                         ++count[tiles_off[b] + tx + m * (ty + m * tz)];
         }
-        for_descent(b, [&](uint64_t t, uint32_t, int32_t) { ++count[t]; });
     });
     // items: largest tiles first, then block order
     std::vector<uint64_t> order(ntiles);
@@ -675,13 +659,23 @@ int plan_bin(s3r_plan* p, uint32_t tile_log2)
                             flag_node(&flags[slot[t] * fwords], T / 2, x - tx * T, y - ty * T, z - tz * T);
                     }
         }
-        const uint32_t E3 = E * E * E;
-        for_descent(b, [&](uint64_t t, uint32_t slot, int32_t nd) {
-            const uint64_t e = cursor[t]++;
-            local[e] = (uint16_t)(E3 + slot);
-            node[e] = (uint32_t)nd;
-        });
+        (void)E;
     });
+    // the nodes on every block's coarse grid (the lattice of tile corners), once per block: the frame's
+    // block_prep_kernel fills the coarse grids from them
+    std::vector<uint32_t> centry_off(nb + 1, 0);
+    std::vector<uint2> centry;
+    for (uint32_t b = 0; b < nb; ++b) {
+        if (pb[b].coarse_log2 > 0) {
+            const uint64_t n = coarse_off[b + 1] - coarse_off[b];
+            for (uint64_t q = 0; q < n; ++q) {
+                const int32_t nd = coarse[coarse_off[b] + q];
+                if (nd >= 0) centry.push_back(make_uint2((uint32_t)q, (uint32_t)nd));
+            }
+        }
+        if (centry.size() > 0xffffffffull) return fail(ctx, S3R_ERR_INVALID, "too many coarse-grid nodes");
+        centry_off[b + 1] = (uint32_t)centry.size();
+    }
     // items whose tile holds no node at an odd position have no flagged cube, so nothing reads their
     // midpoint slots: the top bit of the tile field says "fill the slots"
     for (uint64_t it = 0; it < ntiles; ++it)
@@ -698,6 +692,14 @@ int plan_bin(s3r_plan* p, uint32_t tile_log2)
     if ((rc = upload(ctx, &p->entry_local_dev, local))) return rc;
     if ((rc = upload(ctx, &p->entry_node_dev, node))) return rc;
     if ((rc = upload(ctx, &p->flags_dev, flags))) return rc;
+    if ((rc = upload(ctx, &p->centry_off_dev, centry_off))) return rc;
+    if ((rc = upload(ctx, &p->centry_dev, centry))) return rc;
+    p->any_coarse = false;
+    for (uint32_t b = 0; b < nb; ++b) p->any_coarse |= pb[b].coarse_log2 > 0;
+    for (int q = 0; q < 2; ++q) {
+        cudaError_t e = cudaMalloc(&p->coarse_dev[q], std::max<uint64_t>(coarse_off[nb], 1) * sizeof(float));
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(coarse grids)");
+    }
     p->flag_words = fwords;
     p->tile_log2 = tile_log2;
     p->tiles = ntiles;
@@ -841,8 +843,17 @@ int plan_launch_interp(s3r_plan* p, const float* sparse, cudaStream_t s, uint32_
 {
     s3r_ctx* ctx = p->ctx;
     float2* so = slot ? p->scale_offset_1 : p->scale_offset_dev;
-    if (p->fmt != S3R_BRICK_F32) {
-        S3R_CUDA(ctx, launch_block_ranges(p->blocks_dev, p->nblocks, sparse, p->node_off_dev, so, s));
+    if (p->fmt != S3R_BRICK_F32 || p->any_coarse) {
+        // 16-bit scales and coarse grids
+        PrepArgs pa{};
+        pa.blocks = p->blocks_dev;
+        pa.node_off = p->node_off_dev;
+        pa.sparse = sparse;
+        pa.scale_offset = p->fmt != S3R_BRICK_F32 ? so : nullptr;
+        pa.coarse = p->coarse_dev[slot ? 1 : 0];
+        pa.centry_off = p->centry_off_dev;
+        pa.centry = p->centry_dev;
+        S3R_CUDA(ctx, launch_block_prep(pa, p->nblocks, s));
         ++*kernels;
     }
     TileArgs a{};
@@ -857,6 +868,7 @@ int plan_launch_interp(s3r_plan* p, const float* sparse, cudaStream_t s, uint32_
     a.sparse = sparse;
     a.queue = p->queue_dev + slot;
     a.scale_offset = p->fmt == S3R_BRICK_F32 ? nullptr : so;
+    a.coarse = p->coarse_dev[slot ? 1 : 0];
     a.out = slot ? p->bricks_1 : p->bricks;
     S3R_CUDA(ctx, cudaMemsetAsync(a.queue, 0, sizeof(uint32_t), s));
     S3R_CUDA(ctx, launch_interp_plan(a, p->fmt, p->tile_log2, p->grid_ctas, s));

@@ -469,28 +469,43 @@ constexpr uint32_t kPrefetch = 2; // entries per thread held in registers
 struct Prefetch {
     uint32_t item;
     uint32_t flag; // word threadIdx.x of the item's cube flags
+    uint32_t cidx; // threads 0-7: the coarse-grid index of tile corner threadIdx.x (0xffffffff: none)
+    float corner;
     uint32_t node_base, e0, e1; // a plan holds fewer than 2^32 nodes and entries
     uint32_t loc[kPrefetch];
     uint32_t node[kPrefetch];
     float val[kPrefetch];
 };
 
-// stage 1: the item's block, entry range and flag word
+// stage 1: the item's block, entry range, flag word and corner positions in the coarse grid
 __device__ __forceinline__ void prefetch_head(Prefetch& pf, const TileArgs& a, uint32_t item)
 {
     pf.item = item;
     pf.e0 = pf.e1 = 0;
+    pf.cidx = 0xffffffffu;
     if (item >= a.nitems) return;
-    const uint32_t blk = a.items[item].x;
-    pf.node_base = (uint32_t)a.blocks[blk].node_base;
+    const uint2 it = a.items[item];
+    const PlanBlock* B = &a.blocks[it.x];
+    pf.node_base = (uint32_t)B->node_base;
     pf.e0 = (uint32_t)a.entry_off[item];
     pf.e1 = (uint32_t)a.entry_off[item + 1];
     if (threadIdx.x < a.flag_words) pf.flag = a.flags[(uint64_t)item * a.flag_words + threadIdx.x];
+    if (threadIdx.x < 8) {
+        const uint32_t L = B->coarse_log2;
+        if (L > 0) {
+            const uint32_t tile = it.y & 0x7fffffffu, mL = 1u << L, E = mL + 1;
+            const uint32_t cx = (tile & (mL - 1)) + (threadIdx.x & 1);
+            const uint32_t cy = ((tile >> L) & (mL - 1)) + ((threadIdx.x >> 1) & 1);
+            const uint32_t cz = (tile >> (2 * L)) + (threadIdx.x >> 2);
+            pf.cidx = B->coarse_off + cx + E * (cy + E * cz);
+        }
+    }
 }
 
-// stage 2: positions and node indices of the first kPrefetch * kInterpThreads entries
+// stage 2: positions and node indices of the first kPrefetch * kInterpThreads entries, and the corners
 __device__ __forceinline__ void prefetch_index(Prefetch& pf, const TileArgs& a)
 {
+    if (pf.cidx != 0xffffffffu) pf.corner = a.coarse[pf.cidx];
 #pragma unroll
     for (uint32_t q = 0; q < kPrefetch; ++q) {
         const uint32_t i = pf.e0 + threadIdx.x + q * kInterpThreads;
@@ -569,11 +584,9 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
             }
             for (uint32_t p = threadIdx.x; p < n4; p += kInterpThreads) s4[p] = nan4;
         }
-        for (uint32_t q = threadIdx.x; q < 27 * L; q += kInterpThreads) desc[q] = qnan();
         __syncthreads();
         auto place = [&](uint32_t loc, float v) {
             if (loc < E3) s[loc] = v;
-            else desc[loc - E3] = v;
         };
         // the prefetched entries, then any beyond what the registers held
 #pragma unroll
@@ -581,15 +594,18 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
             if (pf.e0 + threadIdx.x + q * kInterpThreads < pf.e1) place(pf.loc[q], to_internal(pf.val[q]));
         for (uint32_t i = pf.e0 + threadIdx.x + kPrefetch * kInterpThreads; i < pf.e1; i += kInterpThreads)
             place(a.entry_local[i], to_internal(a.sparse[t.node_base + a.entry_node[i]]));
+        // a tile of a block with coarse levels: its corners from the block's coarse grid
+        if (pf.cidx != 0xffffffffu)
+            s[at((threadIdx.x & 1) * T, ((threadIdx.x >> 1) & 1) * T, (threadIdx.x >> 2) * T)] = pf.corner;
         prefetch_head(pf, a, *next_item); // the current item's entries are placed
     }
     __syncthreads();
-    // 2. tile corners from the coarse levels, then the tile cube's own midpoints
-    //    (its first level): warp 0, each level's 27 points in registers
-    if (L > 0 || T >= 4) {
+    // 2. single-grid form: tile corners from the coarse levels; then the tile cube's own
+    //    midpoints (its first level): warp 0, each level's 27 points in registers
+    if ((kGrid && L > 0) || T >= 4) {
         if (threadIdx.x < 32) {
             const uint32_t lane = threadIdx.x;
-            if (L > 0) {
+            if (kGrid && L > 0) {
                 const float corner = descend_regs(desc, d, L, ox, oy, oz, lane);
                 if (lane < 8) s[at((lane & 1) * T, ((lane >> 1) & 1) * T, (lane >> 2) * T)] = corner;
                 __syncwarp();
@@ -741,6 +757,67 @@ __global__ void block_range_kernel(const PlanBlock* blocks, const uint64_t* node
     }
 }
 
+// Per-block preparation of a plan frame, one CTA of kInterpThreads per block:
+//  * 16-bit bricks: the {scale, offset} of the block's valid sparse values (as block_range_kernel);
+//  * a block cut into 2^L > 1 tiles per axis: its coarse grid, the (2^L+1)^3 vertices at multiples of
+//    the tile edge, from the sparse nodes on it, filled level by level exactly as cube_level fills a
+//    tile (the reference's midpoint rules, sums in its order).  A midpoint of a coarse level depends
+//    only on the points of that level's cube, so the full grid holds the values a descent from the
+//    block's root along any one tile's path computes -- each tile then reads its 8 corners from it
+//    instead of descending itself, and the plan carries the coarse nodes once per block instead of
+//    once per tile.
+__global__ void __launch_bounds__(kInterpThreads) block_prep_kernel(PrepArgs a)
+{
+    const uint32_t b = blockIdx.x;
+    const PlanBlock B = a.blocks[b];
+    if (a.scale_offset) {
+        const uint64_t n0 = a.node_off[b], n1 = a.node_off[b + 1];
+        float lo = INFINITY, hi = -INFINITY;
+        for (uint64_t i = n0 + threadIdx.x; i < n1; i += kInterpThreads) {
+            const float v = a.sparse[i];
+            if (v != kNoField && !isnan(v)) {
+                lo = fminf(lo, v);
+                hi = fmaxf(hi, v);
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        __shared__ float slo[kInterpThreads / 32], shi[kInterpThreads / 32];
+        if ((threadIdx.x & 31) == 0) {
+            slo[threadIdx.x >> 5] = lo;
+            shi[threadIdx.x >> 5] = hi;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (uint32_t i = 1; i < kInterpThreads / 32; ++i) {
+                lo = fminf(lo, slo[i]);
+                hi = fmaxf(hi, shi[i]);
+            }
+            float scale = hi - lo;
+            if (!(scale > 0.f) || !isfinite(scale)) scale = 1.f;
+            if (!isfinite(lo)) lo = 0.f;
+            a.scale_offset[b] = make_float2(scale, lo);
+        }
+    }
+    const uint32_t L = B.coarse_log2;
+    if (L == 0) return;
+    const uint32_t T = 1u << L, E = T + 1, E3 = E * E * E;
+    float* g = a.coarse + B.coarse_off;
+    for (uint32_t p = threadIdx.x; p < E3; p += kInterpThreads) g[p] = qnan();
+    __syncthreads();
+    for (uint32_t i = a.centry_off[b] + threadIdx.x; i < a.centry_off[b + 1]; i += kInterpThreads) {
+        const uint2 ce = a.centry[i];
+        if (ce.x < E3) g[ce.x] = to_internal(a.sparse[B.node_base + ce.y]);
+    }
+    __syncthreads();
+    for (uint32_t j = 0; j < L; ++j) {
+        cube_level(g, E, T, j);
+        __syncthreads();
+    }
+}
+
 inline uint32_t ctas_for(uint64_t n, uint32_t threads)
 {
     uint64_t c = (n + threads - 1) / threads;
@@ -824,6 +901,13 @@ cudaError_t launch_interp_plan(const TileArgs& a, uint32_t fmt, uint32_t tile_lo
     case S3R_BRICK_BF16: return launch_tiles<false, __nv_bfloat16>(a, tile_log2_max, grid_ctas, s);
     default: return cudaErrorInvalidValue;
     }
+}
+
+cudaError_t launch_block_prep(const PrepArgs& a, uint32_t nblocks, cudaStream_t s)
+{
+    if (nblocks == 0) return cudaSuccess;
+    block_prep_kernel<<<nblocks, kInterpThreads, 0, s>>>(a);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_block_ranges(const PlanBlock* blocks, uint32_t nblocks, const float* sparse,

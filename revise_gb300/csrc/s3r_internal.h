@@ -19,7 +19,7 @@ struct PlanBlock {
     uint32_t depth;       // subtree depth d: (2^d+1)^3 vertices
     uint32_t tile_log2;   // k: tile edge 2^k cells (k <= d)
     uint32_t coarse_log2; // L = d - k: tiles per axis 2^L
-    uint32_t coarse_off;  // first entry of this block's coarse index grid ((2^L+1)^3 int32)
+    uint32_t coarse_off;  // first vertex of this block's coarse grid ((2^L+1)^3 values)
     uint64_t node_base;   // first node of this block in the sparse value array
     uint64_t dense_off;   // first element of this block's brick
     uint32_t pitch;       // brick row pitch in elements (>= 2^d+1): vertex (x, y, z) at (z (2^d+1) + y) pitch + x
@@ -54,6 +54,9 @@ struct TileArgs {
     const float2* scale_offset;   // per block {scale, offset} for 16-bit bricks
     void* out;                    // brick store
     uint32_t* queue;              // work-queue counter, zeroed before the launch (nullptr: one item per CTA)
+    const float* coarse;          // plan form: per block cut into 2^L > 1 tiles per axis its coarse grid (the
+                                  // (2^L+1)^3 vertices at multiples of the tile edge, internal values), from
+                                  // block_prep_kernel: a tile reads its 8 corners there
     // single-block form
     const float* grid;
     uint32_t grid_depth;
@@ -177,6 +180,18 @@ cudaError_t launch_interp_grid(const float* grid, uint32_t depth, float* dense, 
 cudaError_t launch_interp_plan(const TileArgs& a, uint32_t fmt, uint32_t tile_log2_max, uint32_t grid_ctas,
                                cudaStream_t s);
 uint32_t interp_plan_ctas_per_sm(uint32_t fmt, uint32_t tile_log2);
+// Per-block preparation of a plan frame (interp.cu), one CTA per block: the 16-bit {scale, offset} when
+// scale_offset is set, and the coarse grid of every block with coarse levels.
+struct PrepArgs {
+    const PlanBlock* blocks;
+    const uint64_t* node_off;     // nblocks + 1
+    const float* sparse;
+    float2* scale_offset;         // nullptr: F32 bricks
+    float* coarse;                // coarse grids, at PlanBlock::coarse_off
+    const uint32_t* centry_off;   // nblocks + 1: the sparse nodes on each block's coarse grid
+    const uint2* centry;          // {coarse grid index, node index within the block}
+};
+cudaError_t launch_block_prep(const PrepArgs& a, uint32_t nblocks, cudaStream_t s);
 cudaError_t launch_block_ranges(const PlanBlock* blocks, uint32_t nblocks, const float* sparse,
                                 const uint64_t* node_off_dev, float2* scale_offset, cudaStream_t s);
 
