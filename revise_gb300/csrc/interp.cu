@@ -323,12 +323,14 @@ __device__ __forceinline__ void flag_cubes(uint32_t* flags, uint32_t H, uint32_t
 // The 19 midpoints of one 2x2x2 cube from its 8 corners (v[p], p = a + 3b + 9c,
 // a, b, c in {0, 1, 2}); kSlots: v also holds sparse values (or NaN) at the
 // midpoints, which are kept.  Edges, then faces, then the centre, stencil sums
-// in the reference's order.
-template <bool kSlots> __device__ __forceinline__ void fill_cube(float v[27])
+// in the reference's order.  kLowZDone: the cube's z = 0 face is final already
+// (the z = 2 face of the cube below it), only the points above it are filled.
+template <bool kSlots, bool kLowZDone = false> __device__ __forceinline__ void fill_cube(float v[27])
 {
 #pragma unroll
     for (int p = 0; p < 27; ++p) {
         const int a = p % 3, b = (p / 3) % 3, cc = p / 9;
+        if (kLowZDone && cc == 0) continue;
         if ((a & 1) + (b & 1) + (cc & 1) == 1 && (!kSlots || isnan(v[p]))) {
             const int st = (a & 1) ? 1 : ((b & 1) ? 3 : 9);
             v[p] = kHalf * (v[p - st] + v[p + st]);
@@ -337,6 +339,7 @@ template <bool kSlots> __device__ __forceinline__ void fill_cube(float v[27])
 #pragma unroll
     for (int p = 0; p < 27; ++p) {
         const int a = p % 3, b = (p / 3) % 3, cc = p / 9;
+        if (kLowZDone && cc == 0) continue;
         if ((a & 1) + (b & 1) + (cc & 1) == 2 && (!kSlots || isnan(v[p]))) {
             const int s1 = (a & 1) ? 1 : 3;
             const int s2 = (cc & 1) ? 9 : 3;
@@ -346,18 +349,117 @@ template <bool kSlots> __device__ __forceinline__ void fill_cube(float v[27])
     if (!kSlots || isnan(v[13])) v[13] = kSixth * (v[12] + v[14] + v[10] + v[16] + v[4] + v[22]);
 }
 
-// The finest level of a tile, written straight to HBM: one thread per 2x2x2
-// cube (H^3 cubes, consecutive along x within a warp).  A cube reads its 8
-// corners from the even sub-array; only cubes flagged as holding a sparse
-// midpoint also read their 19 midpoint slots.  It computes its midpoints in
-// registers and stores the vertices it owns -- its low octant, plus the far
-// side where it is the last cube of the block along an axis -- with the
-// 16-bit encoding fused into the store.  Masked corners become NaN as they are
-// loaded, so unflagged cubes produce NaN directly (a NaN in a stencil sum gives
-// NaN as +inf gives +inf); flagged cubes test their slots for NaN ("no sparse
-// value") before any slot is overwritten, then turn masked sparse values to NaN.
+// One finest-level cube (ci, cj, ck) of a tile: reads its corners from the even
+// sub-array -- kFirst: all 8; else the upper 4, its z = 0 face being the z = 2
+// face of the cube below it, already in v -- and, when flagged as holding a
+// sparse midpoint, its midpoint slots (above the z = 0 face unless kFirst);
+// computes its midpoints in registers and stores the vertices it owns: its low
+// octant, plus the far side where it is the last cube of the block along an
+// axis, with the 16-bit encoding fused into the store.  Masked corners become
+// NaN as they are loaded, so unflagged cubes produce NaN directly (a NaN in a
+// stencil sum gives NaN as +inf gives +inf); flagged cubes test their slots for
+// NaN ("no sparse value") before any slot is overwritten, then turn masked
+// sparse values to NaN.  A reused face went through the same steps in the cube
+// below, so every vertex gets the value a fresh cube would give it.
 // kPairs: plan bricks, whose rows are padded to whole sectors (aligned rows, even pitch): a row's two
 // vertices of a cube go out as one store.  A plain (2^d+1)^3 grid (odd pitch) stores them one by one.
+template <uint32_t T, typename OutT, bool kPairs, bool kFirst>
+__device__ __forceinline__ void finest_cube(const float* s, bool has, uint32_t ci, uint32_t cj, uint32_t ck, float v[27],
+                                            OutT* base, uint32_t pitch, uint32_t e, uint32_t e2, bool lx, bool ly,
+                                            bool lz, float inv_scale, float offset)
+{
+    using S = SplitTile<T>;
+#pragma unroll
+    for (int p = 0; p < 27; ++p) {
+        const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
+        if (!kFirst && cc < 2) continue;
+        if (!((a | b | cc) & 1)) v[p] = inf_to_nan(s[S::idx(0, ci + (a >> 1), cj + (b >> 1), ck + (cc >> 1))]);
+    }
+    if (has) {
+#pragma unroll
+        for (int p = 0; p < 27; ++p) {
+            const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
+            if (!kFirst && cc == 0) continue;
+            const uint32_t cls = (a & 1) | ((b & 1) << 1) | ((cc & 1) << 2);
+            if (cls) v[p] = s[S::idx(cls, ci + (a >> 1), cj + (b >> 1), ck + (cc >> 1))];
+        }
+        fill_cube<true, !kFirst>(v);
+#pragma unroll
+        for (int p = 0; p < 27; ++p) {
+            if (!kFirst && p / 9 == 0) continue;
+            if ((p % 3) & 1 || ((p / 3) % 3) & 1 || (p / 9) & 1) v[p] = inf_to_nan(v[p]);
+        }
+    } else {
+        fill_cube<false, !kFirst>(v);
+    }
+    if constexpr (kPairs) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const uint32_t b = r & 1, cc = r >> 1;
+            Store2<OutT>::put_nan(base + b * pitch + cc * e2, v[3 * b + 9 * cc], v[1 + 3 * b + 9 * cc], inv_scale,
+                                  offset);
+        }
+    } else {
+#pragma unroll
+        for (int p = 0; p < 27; ++p) {
+            const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
+            if (a < 2 && b < 2 && cc < 2) Store<OutT>::put_nan(base, a + b * pitch + cc * e2, v[p], inv_scale, offset);
+        }
+    }
+    // the far side where this is the block's last cube along an axis: the x = 2 face (with its
+    // y = 2 / z = 2 edges where those are far too), then y = 2 (x < 2), then z = 2 (x, y < 2)
+    auto far_put = [&](int p) {
+        const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
+        if constexpr (std::is_same<OutT, float>::value && T >= 8) {
+            if (a == 2 && pitch >= e + 7) {
+                // a padded brick (plan layout, d >= 3): x = 2^d starts a sector of its own
+                // (rows are 32-byte aligned, 2^d is a multiple of 8, the pitch is 2^d + 8):
+                // write the whole sector, the padding as NaN
+                float4* q = reinterpret_cast<float4*>(base + a + b * pitch + cc * e2);
+                q[0] = make_float4(v[p], qnan(), qnan(), qnan());
+                q[1] = make_float4(qnan(), qnan(), qnan(), qnan());
+                return;
+            }
+        }
+        Store<OutT>::put_nan(base, a + b * pitch + cc * e2, v[p], inv_scale, offset);
+    };
+    if (lx) {
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+            for (int c2 = 0; c2 < 3; ++c2)
+                if ((bb < 2 || ly) && (c2 < 2 || lz)) far_put(2 + 3 * bb + 9 * c2);
+    }
+    if (ly) {
+#pragma unroll
+        for (int c2 = 0; c2 < 3; ++c2) {
+            if (c2 == 2 && !lz) continue;
+            if constexpr (kPairs) {
+                Store2<OutT>::put_nan(base + 2 * pitch + c2 * e2, v[6 + 9 * c2], v[7 + 9 * c2], inv_scale, offset);
+            } else {
+                far_put(6 + 9 * c2);
+                far_put(7 + 9 * c2);
+            }
+        }
+    }
+    if (lz) {
+#pragma unroll
+        for (int b2 = 0; b2 < 2; ++b2) {
+            if constexpr (kPairs) {
+                Store2<OutT>::put_nan(base + b2 * pitch + 2 * e2, v[3 * b2 + 18], v[1 + 3 * b2 + 18], inv_scale,
+                                      offset);
+            } else {
+                far_put(3 * b2 + 18);
+                far_put(1 + 3 * b2 + 18);
+            }
+        }
+    }
+}
+
+// The finest level of a tile, written straight to HBM: its H^3 2x2x2 cubes in
+// runs of Z along z, one run per thread (runs consecutive along x within a
+// warp), so that each cube after the first of a run takes its z = 0 face from
+// the one below; Z makes the runs about as many as the CTA's threads.
 template <uint32_t T, typename OutT, bool kPairs>
 __device__ __forceinline__ void finest_store(const float* s, const uint32_t* flags, OutT* out, uint32_t e,
                                              uint32_t pitch, uint32_t ox, uint32_t oy, uint32_t oz, bool far_x,
@@ -366,96 +468,33 @@ __device__ __forceinline__ void finest_store(const float* s, const uint32_t* fla
     using S = SplitTile<T>;
     constexpr uint32_t H = S::H;
     constexpr uint32_t lh = (H >= 2) ? (31 - __builtin_clz(H)) : 0;
-    constexpr uint32_t ncubes = H * H * H;
+    constexpr uint32_t per = H * H * H / kInterpThreads;
+    constexpr uint32_t Z = per >= H ? H : (per >= 1 ? per : 1);
+    constexpr uint32_t lzr = 31 - __builtin_clz(Z);
+    constexpr uint32_t nruns = H * H * H / Z;
     const uint32_t e2 = e * pitch; // slab stride (a brick holds fewer than 2^32 elements)
 #pragma unroll 1
-    for (uint32_t c = threadIdx.x; c < ncubes; c += kInterpThreads) {
-        const uint32_t ci = c & (H - 1), cj = (c >> lh) & (H - 1), ck = c >> (2 * lh);
+    for (uint32_t rr = threadIdx.x; rr < nruns; rr += kInterpThreads) {
+        const uint32_t ci = rr & (H - 1), cj = (rr >> lh) & (H - 1), ck0 = (rr >> (2 * lh)) << lzr;
+        const bool lx = far_x && ci == H - 1, ly = far_y && cj == H - 1;
         float v[27];
-        const bool has = (flags[c >> 5] >> (c & 31)) & 1u;
-#pragma unroll
-        for (int p = 0; p < 27; ++p) {
-            const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
-            if (!((a | b | cc) & 1)) v[p] = inf_to_nan(s[S::idx(0, ci + (a >> 1), cj + (b >> 1), ck + (cc >> 1))]);
+        OutT* base = out + (((oz + 2 * ck0) * e + (oy + 2 * cj)) * pitch + (ox + 2 * ci));
+        {
+            const uint32_t c = ci + H * (cj + H * ck0);
+            const bool has = (flags[c >> 5] >> (c & 31)) & 1u;
+            finest_cube<T, OutT, kPairs, true>(s, has, ci, cj, ck0, v, base, pitch, e, e2, lx, ly,
+                                               far_z && ck0 == H - 1, inv_scale, offset);
         }
-        if (has) {
+#pragma unroll 1
+        for (uint32_t z = 1; z < Z; ++z) {
+            const uint32_t ck = ck0 + z;
+            const uint32_t c = ci + H * (cj + H * ck);
+            const bool has = (flags[c >> 5] >> (c & 31)) & 1u;
 #pragma unroll
-            for (int p = 0; p < 27; ++p) {
-                const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
-                const uint32_t cls = (a & 1) | ((b & 1) << 1) | ((cc & 1) << 2);
-                if (cls) v[p] = s[S::idx(cls, ci + (a >> 1), cj + (b >> 1), ck + (cc >> 1))];
-            }
-            fill_cube<true>(v);
-#pragma unroll
-            for (int p = 0; p < 27; ++p)
-                if ((p % 3) & 1 || ((p / 3) % 3) & 1 || (p / 9) & 1) v[p] = inf_to_nan(v[p]);
-        } else {
-            fill_cube<false>(v);
-        }
-        OutT* base = out + (((oz + 2 * ck) * e + (oy + 2 * cj)) * pitch + (ox + 2 * ci));
-        if constexpr (kPairs) {
-#pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                const uint32_t b = r & 1, cc = r >> 1;
-                Store2<OutT>::put_nan(base + b * pitch + cc * e2, v[3 * b + 9 * cc], v[1 + 3 * b + 9 * cc], inv_scale,
-                                      offset);
-            }
-        } else {
-#pragma unroll
-            for (int p = 0; p < 27; ++p) {
-                const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
-                if (a < 2 && b < 2 && cc < 2)
-                    Store<OutT>::put_nan(base, a + b * pitch + cc * e2, v[p], inv_scale, offset);
-            }
-        }
-        const bool lx = far_x && ci == H - 1, ly = far_y && cj == H - 1, lz = far_z && ck == H - 1;
-        // the far side where this is the block's last cube along an axis: the x = 2 face (with its
-        // y = 2 / z = 2 edges where those are far too), then y = 2 (x < 2), then z = 2 (x, y < 2)
-        auto far_put = [&](int p) {
-            const uint32_t a = p % 3, b = (p / 3) % 3, cc = p / 9;
-            if constexpr (std::is_same<OutT, float>::value && T >= 8) {
-                if (a == 2 && pitch >= e + 7) {
-                    // a padded brick (plan layout, d >= 3): x = 2^d starts a sector of its own
-                    // (rows are 32-byte aligned, 2^d is a multiple of 8, the pitch is 2^d + 8):
-                    // write the whole sector, the padding as NaN
-                    float4* q = reinterpret_cast<float4*>(base + a + b * pitch + cc * e2);
-                    q[0] = make_float4(v[p], qnan(), qnan(), qnan());
-                    q[1] = make_float4(qnan(), qnan(), qnan(), qnan());
-                    return;
-                }
-            }
-            Store<OutT>::put_nan(base, a + b * pitch + cc * e2, v[p], inv_scale, offset);
-        };
-        if (lx) {
-#pragma unroll
-            for (int bb = 0; bb < 3; ++bb)
-#pragma unroll
-                for (int c2 = 0; c2 < 3; ++c2)
-                    if ((bb < 2 || ly) && (c2 < 2 || lz)) far_put(2 + 3 * bb + 9 * c2);
-        }
-        if (ly) {
-#pragma unroll
-            for (int c2 = 0; c2 < 3; ++c2) {
-                if (c2 == 2 && !lz) continue;
-                if constexpr (kPairs) {
-                    Store2<OutT>::put_nan(base + 2 * pitch + c2 * e2, v[6 + 9 * c2], v[7 + 9 * c2], inv_scale, offset);
-                } else {
-                    far_put(6 + 9 * c2);
-                    far_put(7 + 9 * c2);
-                }
-            }
-        }
-        if (lz) {
-#pragma unroll
-            for (int b2 = 0; b2 < 2; ++b2) {
-                if constexpr (kPairs) {
-                    Store2<OutT>::put_nan(base + b2 * pitch + 2 * e2, v[3 * b2 + 18], v[1 + 3 * b2 + 18], inv_scale,
-                                          offset);
-                } else {
-                    far_put(3 * b2 + 18);
-                    far_put(1 + 3 * b2 + 18);
-                }
-            }
+            for (int p = 0; p < 9; ++p) v[p] = v[p + 18];
+            base += 2 * e2;
+            finest_cube<T, OutT, kPairs, false>(s, has, ci, cj, ck, v, base, pitch, e, e2, lx, ly,
+                                                far_z && ck == H - 1, inv_scale, offset);
         }
     }
 }
@@ -574,7 +613,6 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
         {
             const float4 nan4 = make_float4(qnan(), qnan(), qnan(), qnan());
             float4* s4 = reinterpret_cast<float4*>(s);
-#pragma unroll 1
             // the even sub-array always (the coarse levels test it for NaN); the midpoint slots only
             // where a flagged cube will read them
             uint32_t n4 = (E3 + 3) / 4;
@@ -582,6 +620,7 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
                 constexpr uint32_t G3 = S::G * S::G * S::G;
                 if (!t.slots) n4 = (G3 + 3) / 4;
             }
+#pragma unroll 1
             for (uint32_t p = threadIdx.x; p < n4; p += kInterpThreads) s4[p] = nan4;
         }
         __syncthreads();
