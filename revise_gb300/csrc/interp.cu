@@ -349,6 +349,43 @@ template <bool kSlots, bool kLowZDone = false> __device__ __forceinline__ void f
     if (!kSlots || isnan(v[13])) v[13] = kSixth * (v[12] + v[14] + v[10] + v[16] + v[4] + v[22]);
 }
 
+// cube_level with the grid stride, tile size and level known at compile time (the coarse levels
+// inside a tile): the 27 point offsets become immediates and the cube loop is unrolled.
+template <uint32_t E, uint32_t T, uint32_t J> __device__ __forceinline__ void cube_level_ct(float* s)
+{
+    constexpr uint32_t m = 1u << J, sz = T >> J, hs = sz >> 1;
+    constexpr uint32_t st0 = hs, st1 = E * hs, st2 = E * E * hs;
+    constexpr uint32_t ncubes = 1u << (3 * J);
+#pragma unroll
+    for (uint32_t c0 = 0; c0 < ncubes; c0 += kInterpThreads) {
+        const uint32_t c = c0 + threadIdx.x;
+        if (ncubes % kInterpThreads != 0 && c >= ncubes) break;
+        const uint32_t ci = c & (m - 1), cj = (c >> J) & (m - 1), ck = c >> (2 * J);
+        const uint32_t base = ci * sz + E * (cj * sz + E * (ck * sz));
+        float v[27];
+#pragma unroll
+        for (int p = 0; p < 27; ++p) v[p] = s[base + (p % 3) * st0 + ((p / 3) % 3) * st1 + (p / 9) * st2];
+        fill_cube<true>(v);
+        const bool lx = ci == m - 1, ly = cj == m - 1, lz = ck == m - 1;
+#pragma unroll
+        for (int p = 0; p < 27; ++p) {
+            const int a = p % 3, b = (p / 3) % 3, cc = p / 9;
+            if ((a & 1) + (b & 1) + (cc & 1) == 0) continue;
+            if ((a < 2 || lx) && (b < 2 || ly) && (cc < 2 || lz)) s[base + a * st0 + b * st1 + cc * st2] = v[p];
+        }
+    }
+}
+
+// The coarse levels 1 .. K-2 of a tile of T = 2^K cells on its even sub-array (G^3, a tile of T/2 cells).
+template <uint32_t G, uint32_t H, uint32_t J, uint32_t K> __device__ __forceinline__ void tile_levels(float* s)
+{
+    if constexpr (J + 1 < K) {
+        cube_level_ct<G, H, J>(s);
+        __syncthreads();
+        tile_levels<G, H, J + 1, K>(s);
+    }
+}
+
 // One finest-level cube (ci, cj, ck) of a tile: reads its corners from the even
 // sub-array -- kFirst: all 8; else the upper 4, its z = 0 face being the z = 2
 // face of the cube below it, already in v -- and, when flagged as holding a
@@ -655,13 +692,7 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
     }
     if constexpr (!kGrid) prefetch_index(pf, a);
     // 3. the remaining coarser levels on the even sub-array (a tile of T/2 cells)
-    if constexpr (T >= 8) {
-        constexpr uint32_t kk = 31 - __builtin_clz(T);
-        for (uint32_t j = 1; j + 1 < kk; ++j) {
-            cube_level(s, S::G, S::H, j);
-            __syncthreads();
-        }
-    }
+    if constexpr (T >= 8) tile_levels<S::G, S::H, 1, 31 - __builtin_clz(T)>(s);
     // 4. the finest level, straight to HBM, while the next item's entries load
     if constexpr (!kGrid) prefetch_values(pf, a);
     float inv_scale = 1.f, offset = 0.f;
