@@ -59,7 +59,7 @@
 extern "C" {
 #endif
 
-#define S3R_ABI_VERSION 6
+#define S3R_ABI_VERSION 7
 
 /* status codes */
 #define S3R_OK 0
@@ -441,8 +441,13 @@ int s3r_plan_brick_pitches(const s3r_plan* plan, const uint32_t** pitch);
 /* Per-brick {scale, offset} pairs (device, 2 floats per block; F16/BF16 only, else NULL). */
 int s3r_plan_brick_scales(const s3r_plan* plan, const float** scale_offset);
 
+/* The interpolation tile edge (cells) of the plan's blocks of depth `depth`: the
+ * plan's tile_cells capped by the depth, or the autotuner's choice for that depth. */
+int s3r_plan_tile_cells(const s3r_plan* plan, uint32_t depth, uint32_t* cells);
+
 /* Project-written autotuner: times the interpolation of `sparse` with tiles of
- * 8, 16 and 32 cells and the frame render with each render form and CTA shape
+ * 8, 16 and 32 cells, then per block depth (deepest first) a tile one step
+ * smaller for that depth's blocks alone, and the frame render with each render form and CTA shape
  * (S3R_RENDER_TILES), `reps` runs each after one warm-up, keeps the fastest of
  * both and re-bins the plan for the chosen tile.  Several lanes per ray are
  * skipped when view->alpha_stop < 1; a block-major form whose buffers do not fit

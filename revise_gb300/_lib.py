@@ -23,7 +23,7 @@ MAX_DEPTH = 9
 BRICK_F32, BRICK_F16, BRICK_BF16 = 0, 1, 2
 FILTER_EXACT, FILTER_TEXTURE = 0, 1
 RENDER_TILES_WALK, RENDER_TILES = 16, 19  # render forms: per-ray walk ids, then block-major ids
-ABI_VERSION = 6
+ABI_VERSION = 7
 
 u8p = C.POINTER(C.c_uint8)
 u16p = C.POINTER(C.c_uint16)
@@ -147,6 +147,7 @@ _SIGS = {
     "s3r_plan_destroy": (C.c_int, [vp]),
     "s3r_plan_info_get": (C.c_int, [vp, C.POINTER(PlanInfo)]),
     "s3r_plan_bricks": (C.c_int, [vp, C.POINTER(vp), C.POINTER(u64p)]),
+    "s3r_plan_tile_cells": (C.c_int, [vp, C.c_uint32, u32p]),
     "s3r_plan_brick_pitches": (C.c_int, [vp, C.POINTER(u32p)]),
     "s3r_frame_run_host": (C.c_int, [vp, vp, C.POINTER(View), vp, vp, vp, vp]),
     "s3r_frame_host_sync": (C.c_int, [vp, vp]),

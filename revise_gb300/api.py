@@ -307,6 +307,12 @@ class FramePlan:
         self.ctx._check(self.lib.s3r_frame_host_sync(self.ctx.h, self.h))
         self._host_inflight = []
 
+    def tile_cells(self, depth: int) -> int:
+        """Interpolation tile edge (cells) of this plan's blocks of the given depth."""
+        c = C.c_uint32()
+        check(self.lib.s3r_plan_tile_cells(self.h, depth, C.byref(c)))
+        return int(c.value)
+
     def autotune(self, view: View, sparse_dev, tf_dev, reps: int = 3, stream=None):
         self.ctx._check(self.lib.s3r_plan_autotune(self.ctx.h, self.h, C.byref(view), ptr(sparse_dev), ptr(tf_dev),
                                                    reps, _stream(stream)))

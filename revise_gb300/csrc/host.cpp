@@ -59,7 +59,8 @@ struct s3r_plan {
     s3r_ctx* ctx = nullptr;
     s3r_frame_desc desc{};
     uint32_t nblocks = 0, level = 0, fmt = 0;
-    uint32_t tile_log2 = 4;
+    uint32_t tile_log2 = 4;             // the largest tile edge (log2 cells) over the blocks
+    uint8_t tile_by_depth[S3R_MAX_DEPTH + 1] = {}; // per block depth: its tile edge (log2), capped by the depth
     uint32_t render_tile = 0;
     std::vector<uint32_t> blocks;      // 4 per block
     std::vector<uint64_t> node_off;    // nblocks+1
@@ -522,15 +523,21 @@ template <class T> int upload(s3r_ctx* ctx, T** dst, const std::vector<T>& src)
 // of several tiles the lattice points of the tile grid go to the block's coarse
 // grid instead, whose values every frame computes once per block), lists the
 // coarse-grid nodes and the work items (largest tiles first), and uploads them.
-int plan_bin(s3r_plan* p, uint32_t tile_log2)
+// by_depth: per block depth the tile edge (log2 cells) of that depth's blocks; NULL: tile_log2 for all.
+int plan_bin(s3r_plan* p, uint32_t tile_log2, const uint8_t* by_depth = nullptr)
 {
     s3r_ctx* ctx = p->ctx;
     const uint32_t nb = p->nblocks;
     std::vector<PlanBlock> pb(nb);
     std::vector<uint64_t> tiles_off(nb + 1, 0), coarse_off(nb + 1, 0);
+    uint8_t tl_of[S3R_MAX_DEPTH + 1];
+    for (uint32_t d = 0; d <= S3R_MAX_DEPTH; ++d)
+        tl_of[d] = (uint8_t)std::min<uint32_t>(by_depth ? by_depth[d] : tile_log2, d);
+    tile_log2 = 0;
+    for (uint32_t b = 0; b < nb; ++b) tile_log2 = std::max<uint32_t>(tile_log2, tl_of[p->blocks[4 * b + 3]]);
     for (uint32_t b = 0; b < nb; ++b) {
         const uint32_t d = p->blocks[4 * b + 3];
-        const uint32_t k = std::min(tile_log2, d);
+        const uint32_t k = tl_of[d];
         const uint32_t L = d - k;
         pb[b].depth = d;
         pb[b].tile_log2 = k;
@@ -702,6 +709,7 @@ int plan_bin(s3r_plan* p, uint32_t tile_log2)
     }
     p->flag_words = fwords;
     p->tile_log2 = tile_log2;
+    std::memcpy(p->tile_by_depth, tl_of, sizeof(tl_of));
     p->tiles = ntiles;
     p->entries = nentries;
     // persistent grid: the CTAs that fit on every SM at once, fed by the work queue
@@ -1768,6 +1776,14 @@ int s3r_plan_info_get(const s3r_plan* p, s3r_plan_info* out)
     return S3R_OK;
 }
 
+int s3r_plan_tile_cells(const s3r_plan* p, uint32_t depth, uint32_t* cells)
+{
+    if (!p || !cells) return fail(nullptr, S3R_ERR_INVALID, "null pointer");
+    if (depth > S3R_MAX_DEPTH) return fail(nullptr, S3R_ERR_INVALID, "depth exceeds S3R_MAX_DEPTH");
+    *cells = 1u << p->tile_by_depth[depth];
+    return S3R_OK;
+}
+
 int s3r_plan_bricks(const s3r_plan* p, void** bricks, const uint64_t** vertex_off)
 {
     if (!p || !bricks || !vertex_off) return fail(nullptr, S3R_ERR_INVALID, "null pointer");
@@ -2117,7 +2133,24 @@ int s3r_plan_autotune(s3r_ctx* ctx, s3r_plan* plan, const s3r_view* view, const 
             best_tl = tl;
         }
     }
-    if ((rc = plan_bin(plan, best_tl))) return cleanup(rc);
+    // then per block depth (deepest first): a smaller tile for that depth's blocks alone, kept when faster
+    // (never a larger one: the largest tile sets every CTA's shared memory)
+    uint8_t by_depth[S3R_MAX_DEPTH + 1];
+    for (uint32_t d = 0; d <= S3R_MAX_DEPTH; ++d) by_depth[d] = (uint8_t)std::min(best_tl, d);
+    bool present[S3R_MAX_DEPTH + 1] = {};
+    for (uint32_t b = 0; b < plan->nblocks; ++b) present[plan->blocks[4 * b + 3]] = true;
+    for (int d = S3R_MAX_DEPTH; d >= 4; --d) {
+        if (!present[d] || by_depth[d] <= 3) continue;
+        const uint8_t keep = by_depth[d];
+        by_depth[d] = (uint8_t)(keep - 1);
+        if ((rc = plan_bin(plan, best_tl, by_depth))) return cleanup(rc);
+        float ms = 0;
+        rc = timed([&](uint32_t* k) { return plan_launch_interp(plan, sparse, s, k); }, ms);
+        if (rc) return cleanup(rc);
+        if (ms < best) best = ms;
+        else by_depth[d] = keep;
+    }
+    if ((rc = plan_bin(plan, best_tl, by_depth))) return cleanup(rc);
     uint32_t k = 0;
     if ((rc = plan_launch_interp(plan, sparse, s, &k))) return cleanup(rc);
     ctx->launches += k;
