@@ -51,6 +51,8 @@ def parse():
                          "the small case for kernel captures")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--render-tile", type=int, default=None,
+                    help="render form and CTA shape id (s3r.h S3R_RENDER_TILES); implies --no-autotune")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the adjoint, 16-bit and reference-CUDA measurements")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
@@ -342,7 +344,7 @@ def run_gb300(a):
     w = make_workload(a.config)
     ctx = Context(dev)
     view = host.view_for(w)
-    plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=16)
+    plan = FramePlan(ctx, w, _lib.BRICK_F32, tile_cells=16, render_tile=a.render_tile or 0)
     stream = torch.cuda.current_stream()
     sparse = torch.from_numpy(w.sparse).cuda()
     tf = torch.from_numpy(np.ascontiguousarray(w.tf)).cuda()
@@ -351,9 +353,11 @@ def run_gb300(a):
     argb = torch.zeros(W * H, dtype=torch.int32, device="cuda")
     samples = torch.zeros(1, dtype=torch.int64, device="cuda")
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device="cuda")
-    if not a.no_autotune:
+    if not a.no_autotune and a.render_tile is None:
         plan.autotune(view, sparse, tf, reps=3)
     info = plan.info
+    depths = sorted({int(d) for d in w.blocks[:, 3]})
+    tiles_by_depth = {str(d): plan.tile_cells(d) for d in depths}
     V = int(info.vertices)
     alg_bytes = 10 * int(info.nodes) + 4 * V  # n2i + values per node, one dense write per vertex
 
@@ -459,8 +463,20 @@ def run_gb300(a):
     achieved = alg_bytes / (t_interp * 1e-3) / 1e9
     traffic = None
     tp = ROOT / "profiles" / "interp_tiles_cfg3_traffic.json"
-    if tp.exists():
+    if tp.exists() and a.config == "cfg3":
         traffic = json.loads(tp.read_text()).get("dram_bytes_per_launch")
+    # the render: DRAM bytes per frame and L2 hit rate from the committed ncu capture of the same
+    # render form on this workload, over this run's CUDA-event time
+    render_roof = None
+    rp = ROOT / "profiles" / "frame_render_cfg3_traffic.json"
+    if rp.exists() and a.config == "cfg3":
+        rj = json.loads(rp.read_text())
+        form = rj.get("render_tiles", {}).get(str(int(info.render_tile)))
+        if form:
+            gbs = form["dram_bytes_per_frame"] / (t_render * 1e-3) / 1e9
+            render_roof = {"bound": "hbm", "kernels": form["kernels"], "traffic": form["dram_bytes_per_frame"],
+                           "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm, "peak_source": peak_note,
+                           "l2_hit_rate": form.get("l2_hit_rate"), "how": rj.get("how")}
 
     cpu = None
     if rank == 0 and not a.no_cpu:
@@ -486,11 +502,14 @@ def run_gb300(a):
                                    "interpolate + ray-cast per frame, CUDA graph",
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                        "l2": "L2 flushed (2x129 MB write) between timed steps; 2.5 GB brick store per step",
-                       "tile_cells": int(info.tile_cells), "render_tile": int(info.render_tile)},
+                       "tile_cells": int(info.tile_cells), "tile_cells_by_depth": tiles_by_depth,
+                       "render_tile": int(info.render_tile),
+                       "render_form": "block-major" if int(info.render_tile) >= _lib.RENDER_TILES_WALK else "per-ray walk"},
             "ms_per_frame": ms, "frames_per_s": 1e3 / ms,
             "interp": {"ms": t_interp, "gvertices_per_s": V / (t_interp * 1e-3) / 1e9,
                        "algorithmic_bytes": alg_bytes},
-            "render": {"ms": t_render, "gsamples_per_s": nsamp / (t_render * 1e-3) / 1e9, "samples": nsamp},
+            "render": {"ms": t_render, "gsamples_per_s": nsamp / (t_render * 1e-3) / 1e9, "samples": nsamp,
+                       "roofline": render_roof},
             "roofline": {"bound": "hbm", "kernel": "interp_tiles_kernel (batched tile interpolation)",
                          "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "peak_source": peak_note, "traffic": traffic},
@@ -828,6 +847,7 @@ def measure_adjoint(ctx, torch, np):
     sp = torch.from_numpy(w.sparse).cuda()
     tf = torch.from_numpy(np.ascontiguousarray(w.tf)).cuda()
     rgba = torch.zeros(w.W * w.H * 4, device="cuda")
+    plan.autotune(view, sp, tf, reps=3)  # the forward is the fastest render form for this view
     plan.interp(sp)
     dl = torch.rand_like(rgba) * 0.01
     dtf = torch.zeros(w.tf.size, device="cuda")
@@ -836,9 +856,10 @@ def measure_adjoint(ctx, torch, np):
 
     fwd = event_ms(torch, lambda: plan.render(view, tf, rgba))
     bwd = event_ms(torch, lambda: plan.backward(view, tf, rgba, dl, dtf, dd))
+    rt = int(plan.info.render_tile)
     plan.close()
     return {"workload": "cfg5: 2x2x2 blocks depth 6, 512x512", "forward_render_ms": fwd, "backward_ms": bwd,
-            "adjoint_forward_ratio": bwd / fwd}
+            "adjoint_forward_ratio": bwd / fwd, "forward_render_tile": rt}
 
 
 def measure_worker_loop(ctx, torch, np, w):
@@ -896,13 +917,22 @@ def measure_extras(ctx, torch, np):
     v2 = host.view_for(w2)
     sp2 = torch.from_numpy(w2.sparse).cuda()
     tf2 = torch.from_numpy(np.ascontiguousarray(w2.tf)).cuda()
-    img = torch.zeros(w2.W * w2.H * 4, device="cuda")
     prec = {}
+    imgs = {}
     for name, fmt in (("f32", _lib.BRICK_F32), ("f16", _lib.BRICK_F16), ("bf16", _lib.BRICK_BF16)):
+        img = torch.zeros(w2.W * w2.H * 4, device="cuda")
         p = FramePlan(ctx, w2, fmt)
+        p.autotune(v2, sp2, tf2, reps=3)
         ms = event_ms(torch, lambda: p.run(v2, sp2, tf2, img))
-        prec[name] = {"ms_per_frame": ms, "frames_per_s": 1e3 / ms}
+        imgs[name] = img
+        prec[name] = {"ms_per_frame": ms, "frames_per_s": 1e3 / ms, "render_tile": int(p.info.render_tile)}
         p.close()
+    for name in ("f16", "bf16"):
+        # image error of the 16-bit bricks against the FP32-brick image of the same frame (RGBA, per channel);
+        # against the FP64 oracle the test suite states it (tests/test_gpu_render.py)
+        d = (imgs[name] - imgs["f32"]).abs()
+        prec[name].update({"max_abs_err_vs_f32": float(d.max()), "mean_abs_err_vs_f32": float(d.mean()),
+                           "frames_per_s_vs_f32": prec["f32"]["ms_per_frame"] / prec[name]["ms_per_frame"]})
     out["precision_cfg2"] = prec
     return out
 
