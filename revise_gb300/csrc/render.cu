@@ -466,14 +466,24 @@ __device__ __forceinline__ float dot3(F3 a, F3 b) { return a.x * b.x + a.y * b.y
 __device__ __forceinline__ F3 normalize3(F3 a) { return a * (1.f / sqrtf(dot3(a, a))); }
 __device__ __forceinline__ float clamp01(float x) { return fmaxf(0.f, fminf(1.f, x)); }
 
+// x^100 in double by squaring (x^64 x^32 x^4): eight multiplications, whose
+// few-ulp double error almost never reaches the float the result is rounded to;
+// a general double pow costs several times that on this GPU's FP64 units.
+__device__ __forceinline__ double pow100(double x)
+{
+    const double x2 = x * x, x4 = x2 * x2, x8 = x4 * x4, x16 = x8 * x8, x32 = x16 * x16, x64 = x32 * x32;
+    return x64 * x32 * x4;
+}
+
 // Blinn-Phong term of one light (cuda_lighting.hpp:26-50): material ambient 1,
 // diffuse = the transfer-function colour, specular 0.5, shininess 100; the
-// reference's max(., 0.0) and pow promote to double.
+// reference's max(., 0.0) and pow promote to double (the max is exact in float,
+// the power is formed in double as above).
 __device__ __forceinline__ F3 blinn(F3 N, F3 V, F3 L, const s3r_light& light, F3 kd)
 {
-    const float diff = (float)fmax((double)dot3(L, N), 0.0);
+    const float diff = fmaxf(dot3(L, N), 0.f);
     const F3 H = normalize3(L + V);
-    const float spec = diff > 0.f ? (float)pow(fmax((double)dot3(H, N), 0.0), 100.0) : 0.f;
+    const float spec = diff > 0.f ? (float)pow100(fmax((double)dot3(H, N), 0.0)) : 0.f;
     return f3(light.ambient) + kd * f3(light.diffuse) * diff + F3{0.5f, 0.5f, 0.5f} * f3(light.specular) * spec;
 }
 
