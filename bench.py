@@ -528,6 +528,19 @@ def run_gb300(a):
             "cpu_baseline": cpu,
         }
         line.update(extras)
+        # the key figures once more, last, so that a reader of only the end of the line sees them
+        summ = {"ms_per_frame": ms, "interp_ms": t_interp, "interp_roofline_frac": achieved / hbm, "render_ms": t_render,
+                "render_roofline_frac": render_roof["frac"] if render_roof else None,
+                "e2e_ms_per_frame": t_e2e}
+        if "adjoint" in extras:
+            summ["adjoint_forward_ratio"] = extras["adjoint"]["adjoint_forward_ratio"]
+        sp = [v["speedup"] for v in extras.get("modes", {}).values() if isinstance(v, dict) and "speedup" in v]
+        if sp:
+            summ["per_block_modes_speedup_min_max"] = [min(sp), max(sp)]
+        pc = extras.get("precision_cfg2")
+        if pc:
+            summ["cfg2_ms_f32_f16_bf16"] = [pc[k]["ms_per_frame"] for k in ("f32", "f16", "bf16")]
+        line["summary"] = summ
         print(json.dumps(line))
     plan.close()
     ctx.close()
