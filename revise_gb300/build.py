@@ -59,7 +59,7 @@ def build_library(force: bool = False, ptxas_verbose: bool = False) -> Path:
     cuda = cuda_home()
     nvcc = str(cuda / "bin" / "nvcc")
     BUILD.mkdir(exist_ok=True)
-    headers = [INCLUDE / "s3r.h", CSRC / "s3r_internal.h"]
+    headers = [INCLUDE / "s3r.h", CSRC / "s3r_internal.h", CSRC / "interp_tile.cuh"]
     jobs = []
     objs = []
     for src in CUDA_SOURCES:
