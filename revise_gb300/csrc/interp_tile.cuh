@@ -1,6 +1,6 @@
 // Device code of the tile interpolation (the hierarchical midpoint fill of one tile in shared memory and
-// its finest level written to HBM), shared by the tile interpolation kernels (interp.cu) and the fused
-// frame kernel (render.cu).  See interp.cu for the algorithm and its reference.
+// its finest level written to HBM), kept apart from the kernels (interp.cu) so that another kernel can run
+// tiles too.  See interp.cu for the algorithm and its reference.
 #pragma once
 
 #include "s3r_internal.h"
