@@ -65,10 +65,11 @@ def test_frame_mode_vs_oracle(ctx, name, filt):
         assert np.array_equal(argb[m].view(np.float32), got[m, 0]) and np.isnan(argb[~m].view(np.float32)).all()
         return
     d = np.abs(got - want).max(1)
+    print(f"{name} filter {filt}: {(d > 2e-3).sum()} of {d.size} pixels beyond 2e-3, max {d.max():.3e}, "
+          f"median {np.median(d):.2e}")
     assert (want[:, 3] > 0).mean() > 0.03
-    # FP32 both sides in the same order; isolated pixels move where a sample or an isosurface
-    # crossing decision flips on the last ulp (the per-block path's 1-LSB cases)
-    assert (d > 2e-3).mean() <= 0.02, (d > 2e-3).mean()
+    # FP32 both sides in the same order: every pixel within the image tolerance (measured: at most 2.8e-5)
+    assert d.max() <= 2e-3, d.max()
     assert np.median(d) <= 1e-5
 
 

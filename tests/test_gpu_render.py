@@ -196,13 +196,17 @@ def test_alpha_stop_bounded_difference(ctx):
 
 @pytest.mark.parametrize("fmt", [_lib.BRICK_F16, _lib.BRICK_BF16])
 def test_16bit_bricks_image_error_is_bounded(ctx, fmt):
+    """16-bit bricks on a small mixed-depth scene against the FP64 oracle: FP16 within the 2e-3 image
+    tolerance (measured 4.2e-4); BF16, whose 8-bit significand holds a brick value to 2^-9 of its brick's
+    range and moves the transfer-function lookup by as much, within 5e-3 (measured 3.9e-3; on the
+    configuration-4 scene, cfg2, BF16 stays within 2e-3: tests/test_gpu_headline.py)."""
     w = workloads.small(seed=9, level=1, depths=(3, 4, 5), W=96, H=64)
     plan, view, img, _, _ = _frame(ctx, w, fmt=fmt)
     ov = oracle.view_from(view)
     ref, flags = oracle.render_frame_f64(ov, w, oracle.interp_workload(w), _rects(w, view), w.tf)
     err = np.abs(img - ref)[flags == 0]
     print(f"16-bit bricks ({'FP16' if fmt == _lib.BRICK_F16 else 'BF16'}), small scene vs FP64: max {err.max():.3e}")
-    assert err.max() <= (0.02 if fmt == _lib.BRICK_F16 else 0.06)
+    assert err.max() <= (2e-3 if fmt == _lib.BRICK_F16 else 5e-3)
     plan.close()
 
 
