@@ -252,8 +252,16 @@ def reference_cuda_frames(w, a):
             if i >= 2:
                 times.append(ms)
         ms = statistics.median(times)
-        return {"ms_per_frame": ms, "frames_per_s": 1e3 / ms, "frames": len(times),
-                "what": "reference CUDA kernels, reference worker loop (per-block H2D, interpolate, render)"}
+        out = {"ms_per_frame": ms, "frames_per_s": 1e3 / ms, "frames": len(times),
+               "what": "reference CUDA kernels, reference worker loop (per-block H2D, interpolate, render)"}
+        try:
+            im, rm = refcu.worker_kernel_ms(view, w, oi, rects)
+            out["kernel_ms"] = {"interpolation": im, "render": rm, "total": im + rm,
+                                "how": "the same loop with every kernel launch bracketed by CUDA events and waited "
+                                       "for: kernel time only, host copies and launch gaps excluded"}
+        except Exception as e:  # the wall-clock figure stands without it
+            out["kernel_ms"] = {"unavailable": f"{type(e).__name__}: {e}"}
+        return out
     except Exception as e:  # the CPU line stands without it
         return {"unavailable": f"{type(e).__name__}: {e}"}
 

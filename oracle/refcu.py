@@ -114,6 +114,23 @@ def worker(view, w, order_idx, rects):
     return vp, tuple(crop[:]), ms.value
 
 
+def worker_kernel_ms(view, w, order_idx, rects):
+    """The reference worker loop with each kernel launch timed by CUDA events: (interpolation kernels ms,
+    renderKernel<Argb> ms) summed over the blocks, host copies excluded."""
+    lib = load()
+    blocks = np.ascontiguousarray(w.blocks[order_idx], dtype=np.uint32)
+    counts = np.diff(w.node_off.astype(np.int64))[order_idx]
+    node_off = np.concatenate([[0], np.cumsum(counts)]).astype(np.uint64)
+    n2i = np.ascontiguousarray(np.concatenate([w.block_nodes(int(b))[0] for b in order_idx]), dtype=np.uint16)
+    sparse = np.ascontiguousarray(np.concatenate([w.block_nodes(int(b))[1] for b in order_idx]), dtype=np.float32)
+    rects = np.ascontiguousarray(rects[order_idx], dtype=np.int32)
+    im, rm = C.c_double(), C.c_double()
+    _check(lib.ref_cuda_worker_kernel_ms(C.byref(view), C.c_uint32(blocks.shape[0]), _p(blocks, C.c_uint32),
+                                        _p(node_off, C.c_uint64), _p(n2i, C.c_uint16), _p(sparse, C.c_float),
+                                        _p(rects, C.c_int32), C.byref(im), C.byref(rm)))
+    return im.value, rm.value
+
+
 def render_block_mode(view, pres, n2i, sparse, depth, idx, rect, viewport, sparse2=None):
     """renderKernel<pres.mode> for one block into a host ARGB32 viewport (in place);
     pres: a revise_gb300._lib.Presentation; sparse2: the secondary field's node values."""

@@ -207,9 +207,30 @@ struct TfTexture {
     }
 } g_tf;
 
+// Kernel-only timing of the worker loop (ref_cuda_worker_kernel_ms): when g_timed is set, every launch is
+// bracketed by CUDA events and its time added to g_kernel_ms[g_phase] (0: interpolation, 1: render).
+bool g_timed = false;
+int g_phase = 0;
+double g_kernel_ms[2] = {0.0, 0.0};
+
 int launch(CUfunction f, dim3 g, dim3 b, void** args, CUstream stream = nullptr)
 {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (g_timed) {
+        CKR(cudaEventCreate(&e0));
+        CKR(cudaEventCreate(&e1));
+        CKR(cudaEventRecord(e0, (cudaStream_t)stream));
+    }
     CKD(cuLaunchKernel(f, g.x, g.y, g.z, b.x, b.y, b.z, 0, stream, args, nullptr));
+    if (g_timed) {
+        CKR(cudaEventRecord(e1, (cudaStream_t)stream));
+        CKR(cudaEventSynchronize(e1));
+        float t = 0.f;
+        CKR(cudaEventElapsedTime(&t, e0, e1));
+        g_kernel_ms[g_phase] += t;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
     return 0;
 }
 
@@ -448,6 +469,35 @@ int ref_cuda_worker(const void* view, uint32_t nblocks, const uint32_t* blocks, 
     }
     *ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return 0;
+}
+
+// The same worker loop with every kernel launch timed by CUDA events (each launch waited for, so the
+// figures are kernel-only: no host copies, no launch overlap): interp_ms sums the interpolation kernels
+// (fill, scatter, the d level passes, NaN transform), render_ms the renderKernel<Argb> launches.
+int ref_cuda_worker_kernel_ms(const void* view, uint32_t nblocks, const uint32_t* blocks, const uint64_t* node_off,
+                              const uint16_t* n2i, const float* sparse, const int32_t* rects, double* interp_ms,
+                              double* render_ms)
+{
+    const View& v = *static_cast<const View*>(view);
+    const size_t npx = (size_t)v.W * v.H;
+    uint32_t* d = nullptr;
+    CKR(cudaMalloc(&d, npx * 4));
+    CKR(cudaMemset(d, 0, npx * 4));
+    g_kernel_ms[0] = g_kernel_ms[1] = 0.0;
+    g_timed = true;
+    int rc = 0;
+    for (uint32_t i = 0; i < nblocks && !rc; ++i) {
+        const uint64_t a = node_off[i], b = node_off[i + 1];
+        g_phase = 0;
+        rc = interp_into_field(n2i + 3 * a, sparse + a, (uint32_t)(b - a), blocks[4 * i + 3]);
+        g_phase = 1;
+        if (!rc) rc = render_block(v, blocks[4 * i + 3], blocks + 4 * i, rects + 4 * i, d);
+    }
+    g_timed = false;
+    cudaFree(d);
+    *interp_ms = g_kernel_ms[0];
+    *render_ms = g_kernel_ms[1];
+    return rc;
 }
 
 } // extern "C"
