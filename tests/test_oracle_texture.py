@@ -142,3 +142,31 @@ def test_oracle_field_modes_reproduce_reference_cuda_images(name):
     d = np.abs(img.view(np.uint8).reshape(-1, 4).astype(int) - ref.view(np.uint8).reshape(-1, 4).astype(int)).max(1)
     assert (ref >> 24).astype(bool).mean() > 0.03
     assert d.max() <= lsb and (d > 0).mean() <= frac, (d.max(), (d > 0).mean())
+
+
+@pytest.mark.parametrize("variant", tv.VARIANTS)
+def test_reference_renderer_deviation_from_fp64(variant):
+    """The reference's own CUDA images (renderKernel<Argb>, texture unit, ARGB8 after every block) against the
+    FP64 frame oracle (exact trilinear filtering, float composition): reported beside the 2e-3 bound the
+    batched float path is held to.  Without masked nodes ("linear") the reference stays within two ARGB8
+    steps of FP64 -- each block's blend truncates to 1/255.999 -- but most covered pixels are beyond 2e-3;
+    with masked nodes the texture unit keeps samples next to masked texels that exact filtering drops, and
+    whole pixels differ."""
+    ref = _load("refcu_render.npz")[variant]
+    w = tv.workload(variant)
+    view = host.view_for(w)
+    ov = oracle.view_from(view)
+    dense = oracle.interp_workload(w)
+    rects = [host.block_view_rect(view, [int(x) for x in w.blocks[b, :3]]) for b in range(w.nblocks)]
+    img, flags = oracle.render_frame_f64(ov, w, dense, rects, w.tf, f64=True)
+    rf = np.stack([(ref >> 16) & 255, (ref >> 8) & 255, ref & 255, ref >> 24], 1).astype(np.float64) / 255.0
+    covered = (img[:, 3] > 0) | (rf[:, 3] > 0)
+    err = np.abs(rf - img).max(1)[covered & (flags == 0)]
+    print(f"reference vs FP64, {variant}: {err.size} covered pixels, max {err.max():.2e}, median "
+          f"{np.median(err):.2e}, beyond 2e-3 {(err > 2e-3).mean():.1%}")
+    assert err.size > 0.5 * w.W * w.H
+    assert np.median(err) <= 1.0 / 255
+    if variant == "linear":
+        assert 2e-3 < err.max() <= 2.0 / 255
+    else:
+        assert err.max() > 0.1
