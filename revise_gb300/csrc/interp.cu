@@ -55,6 +55,42 @@ __global__ void scatter_kernel(float* grid, uint32_t e, const uint16_t* n2i, con
     grid[((uint64_t)z * e + y) * e + x] = sparse[i];
 }
 
+// Work item `item` of the batched plan (kGrid: tile `item` of the single grid) as the tile it names.
+template <bool kGrid> __device__ __forceinline__ TileItem decode_item(const TileArgs& a, uint32_t item)
+{
+    TileItem t;
+    uint32_t tile;
+    t.item = item;
+    t.blk = 0;
+    t.slots = 1;
+    t.node_base = 0;
+    t.dense_off = 0;
+    if constexpr (kGrid) {
+        t.d = a.grid_depth;
+        t.k = a.grid_tile_log2 < t.d ? a.grid_tile_log2 : t.d;
+        t.L = t.d - t.k;
+        t.pitch = (1u << t.d) + 1u;
+        tile = item;
+    } else {
+        const uint2 it = a.items[item];
+        t.blk = it.x;
+        tile = it.y & 0x7fffffffu;
+        t.slots = it.y >> 31;
+        const PlanBlock b = a.blocks[t.blk];
+        t.d = b.depth;
+        t.k = b.tile_log2;
+        t.L = b.coarse_log2;
+        t.node_base = b.node_base;
+        t.dense_off = b.dense_off;
+        t.pitch = b.pitch;
+    }
+    const uint32_t mL = 1u << t.L;
+    t.tx = tile & (mL - 1);
+    t.ty = (tile >> t.L) & (mL - 1);
+    t.tz = tile >> (2 * t.L);
+    return t;
+}
+
 template <bool kGrid, typename OutT>
 __global__ void __launch_bounds__(kInterpThreads, 8) interp_tiles_kernel(TileArgs a)
 {
@@ -64,6 +100,7 @@ __global__ void __launch_bounds__(kInterpThreads, 8) interp_tiles_kernel(TileArg
     __shared__ uint32_t flags[(16 * 16 * 16) / 32]; // one bit per finest cube, tiles up to 32 cells
     __shared__ uint32_t item_s, next_s[2];
     const uint32_t nitems = a.nitems;
+    const Crew<kInterpThreads> cw{threadIdx.x};
     // Work items come from the queue counter when there is one (zeroed before
     // the launch), else item blockIdx.x once per CTA.  The next item is taken
     // at the start of the current one so its entries can be prefetched.  The
@@ -75,54 +112,63 @@ __global__ void __launch_bounds__(kInterpThreads, 8) interp_tiles_kernel(TileArg
     uint32_t item = item_s;
     Prefetch pf;
     if constexpr (!kGrid) {
-        prefetch_head(pf, a, item);
-        prefetch_index(pf, a);
-        prefetch_values(pf, a);
+        prefetch_head<kInterpThreads>(pf, a, item, threadIdx.x);
+        prefetch_index<kInterpThreads>(pf, a, threadIdx.x);
+        prefetch_values<kInterpThreads>(pf, a, threadIdx.x);
     }
     for (uint32_t iter = 0;; ++iter) {
         if (item >= nitems) break;
         uint32_t* next_p = &next_s[iter & 1];
         if (threadIdx.x == 0) *next_p = a.queue ? atomicAdd(a.queue, 1u) : nitems;
-        TileItem t;
-        uint32_t tile;
-        t.item = item;
-        t.blk = 0;
-        t.slots = 1;
-        t.node_base = 0;
-        t.dense_off = 0;
-        if constexpr (kGrid) {
-            t.d = a.grid_depth;
-            t.k = a.grid_tile_log2 < t.d ? a.grid_tile_log2 : t.d;
-            t.L = t.d - t.k;
-            t.pitch = (1u << t.d) + 1u;
-            tile = item;
-        } else {
-            const uint2 it = a.items[item];
-            t.blk = it.x;
-            tile = it.y & 0x7fffffffu;
-            t.slots = it.y >> 31;
-            const PlanBlock b = a.blocks[t.blk];
-            t.d = b.depth;
-            t.k = b.tile_log2;
-            t.L = b.coarse_log2;
-            t.node_base = b.node_base;
-            t.dense_off = b.dense_off;
-            t.pitch = b.pitch;
-        }
-        const uint32_t mL = 1u << t.L;
-        t.tx = tile & (mL - 1);
-        t.ty = (tile >> t.L) & (mL - 1);
-        t.tz = tile >> (2 * t.L);
+        const TileItem t = decode_item<kGrid>(a, item);
+        auto next = [next_p] { return *next_p; };
         switch (t.k) {
-        case 0: run_tile<1, kGrid, OutT>(a, s, desc, flags, t, pf, next_p); break;
-        case 1: run_tile<2, kGrid, OutT>(a, s, desc, flags, t, pf, next_p); break;
-        case 2: run_tile<4, kGrid, OutT>(a, s, desc, flags, t, pf, next_p); break;
-        case 3: run_tile<8, kGrid, OutT>(a, s, desc, flags, t, pf, next_p); break;
-        case 4: run_tile<16, kGrid, OutT>(a, s, desc, flags, t, pf, next_p); break;
-        default: run_tile<32, kGrid, OutT>(a, s, desc, flags, t, pf, next_p); break;
+        case 0: run_tile<1, kGrid, OutT>(a, s, desc, flags, t, pf, cw, next); break;
+        case 1: run_tile<2, kGrid, OutT>(a, s, desc, flags, t, pf, cw, next); break;
+        case 2: run_tile<4, kGrid, OutT>(a, s, desc, flags, t, pf, cw, next); break;
+        case 3: run_tile<8, kGrid, OutT>(a, s, desc, flags, t, pf, cw, next); break;
+        case 4: run_tile<16, kGrid, OutT>(a, s, desc, flags, t, pf, cw, next); break;
+        default: run_tile<32, kGrid, OutT>(a, s, desc, flags, t, pf, cw, next); break;
         }
         __syncthreads();
         item = *next_p;
+    }
+}
+
+// Plans whose tiles are all of 8 cells or fewer: one warp per tile.  Each warp holds its own split tile
+// (9^3 floats) and flag words in shared memory, takes its own items from the queue and synchronizes only
+// with itself, so an SM keeps 32 tiles in flight instead of 8 CTAs' worth: a tile is a chain of short
+// dependent phases (fill, placement, tile cube, coarse level, finest level), and more chains per SM hide
+// more of their latency.  Same tile code, same results as the CTA kernel.
+constexpr uint32_t kWarpTileFloats = ((9 * 9 * 9 + 3) / 4) * 4; // tile_smem_bytes(3) / 4
+template <typename OutT> __global__ void __launch_bounds__(kInterpThreads, 8) interp_warp_tiles_kernel(TileArgs a)
+{
+    constexpr uint32_t kWarps = kInterpThreads / 32;
+    __shared__ float4 s_all[kWarps][kWarpTileFloats / 4];
+    __shared__ uint32_t flags_all[kWarps][2]; // 8-cell tiles: 64 finest cubes
+    const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float* s = reinterpret_cast<float*>(s_all[w]);
+    uint32_t* flags = flags_all[w];
+    const Crew<32> cw{lane};
+    const uint32_t nitems = a.nitems;
+    uint32_t item = lane == 0 ? atomicAdd(a.queue, 1u) : 0u;
+    item = __shfl_sync(0xffffffffu, item, 0);
+    Prefetch pf;
+    prefetch_head<32>(pf, a, item, lane);
+    prefetch_index<32>(pf, a, lane);
+    prefetch_values<32>(pf, a, lane);
+    while (item < nitems) {
+        const uint32_t nxt = lane == 0 ? atomicAdd(a.queue, 1u) : 0u; // read by the warp once placed
+        const TileItem t = decode_item<false>(a, item);
+        auto next = [nxt] { return __shfl_sync(0xffffffffu, nxt, 0); };
+        switch (t.k) {
+        case 0: run_tile<1, false, OutT>(a, s, nullptr, flags, t, pf, cw, next); break;
+        case 1: run_tile<2, false, OutT>(a, s, nullptr, flags, t, pf, cw, next); break;
+        case 2: run_tile<4, false, OutT>(a, s, nullptr, flags, t, pf, cw, next); break;
+        default: run_tile<8, false, OutT>(a, s, nullptr, flags, t, pf, cw, next); break;
+        }
+        __syncwarp();
+        item = __shfl_sync(0xffffffffu, nxt, 0);
     }
 }
 
@@ -235,6 +281,12 @@ inline uint32_t ctas_for(uint64_t n, uint32_t threads)
 template <bool kGrid, typename OutT>
 cudaError_t launch_tiles(const TileArgs& a, uint32_t tile_log2_max, uint32_t grid_ctas, cudaStream_t s)
 {
+    if constexpr (!kGrid) {
+        if (tile_log2_max <= 3 && a.queue) {
+            interp_warp_tiles_kernel<OutT><<<grid_ctas, kInterpThreads, 0, s>>>(a);
+            return cudaGetLastError();
+        }
+    }
     const size_t smem = tile_smem_bytes(tile_log2_max);
     auto kern = interp_tiles_kernel<kGrid, OutT>;
     if (smem > 48 * 1024) {
@@ -282,7 +334,8 @@ cudaError_t launch_interp_grid(const float* grid, uint32_t depth, float* dense, 
 
 uint32_t interp_plan_ctas_per_sm(uint32_t fmt, uint32_t tile_log2)
 {
-    const size_t smem = tile_smem_bytes(tile_log2);
+    const bool warp = tile_log2 <= 3; // the warp-per-tile kernel (static shared memory only)
+    const size_t smem = warp ? 0 : tile_smem_bytes(tile_log2);
     int n = 0;
     cudaError_t e = cudaErrorInvalidValue;
     auto occ = [&](auto kern) {
@@ -290,9 +343,11 @@ uint32_t interp_plan_ctas_per_sm(uint32_t fmt, uint32_t tile_log2)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, kInterpThreads, smem);
     };
     switch (fmt) {
-    case S3R_BRICK_F32: occ(interp_tiles_kernel<false, float>); break;
-    case S3R_BRICK_F16: occ(interp_tiles_kernel<false, __half>); break;
-    case S3R_BRICK_BF16: occ(interp_tiles_kernel<false, __nv_bfloat16>); break;
+    case S3R_BRICK_F32: warp ? occ(interp_warp_tiles_kernel<float>) : occ(interp_tiles_kernel<false, float>); break;
+    case S3R_BRICK_F16: warp ? occ(interp_warp_tiles_kernel<__half>) : occ(interp_tiles_kernel<false, __half>); break;
+    case S3R_BRICK_BF16:
+        warp ? occ(interp_warp_tiles_kernel<__nv_bfloat16>) : occ(interp_tiles_kernel<false, __nv_bfloat16>);
+        break;
     default: break;
     }
     return (e == cudaSuccess && n > 0) ? (uint32_t)n : 1u;

@@ -94,6 +94,18 @@ __device__ __forceinline__ float to_internal(float v) { return v == kNoField ? _
 // Descent slots: 27 points (3x3x3, x fastest) per coarse level.
 constexpr int kMaxDescentLevels = S3R_MAX_DEPTH;
 
+// The threads that run one tile: a CTA of kInterpThreads (kN = kInterpThreads, CTA barriers) or one warp
+// (kN = 32, warp barriers; the warp-per-tile kernel for tiles of up to 8 cells).  tid is the thread's
+// index among them.
+template <uint32_t kN> struct Crew {
+    uint32_t tid;
+    __device__ __forceinline__ void sync() const
+    {
+        if constexpr (kN == 32) __syncwarp();
+        else __syncthreads();
+    }
+};
+
 // One 27-point level held in registers: lane p < 27 holds point p (x fastest)
 // of a cube -- the 8 corners known, each midpoint its sparse value or NaN --
 // and gets it filled: edges from their two ends, faces from their four edges,
@@ -310,15 +322,16 @@ template <bool kSlots, bool kLowZDone = false> __device__ __forceinline__ void f
 
 // cube_level with the grid stride, tile size and level known at compile time (the coarse levels
 // inside a tile): the 27 point offsets become immediates and the cube loop is unrolled.
-template <uint32_t E, uint32_t T, uint32_t J> __device__ __forceinline__ void cube_level_ct(float* s)
+template <uint32_t E, uint32_t T, uint32_t J, uint32_t kN>
+__device__ __forceinline__ void cube_level_ct(float* s, uint32_t tid)
 {
     constexpr uint32_t m = 1u << J, sz = T >> J, hs = sz >> 1;
     constexpr uint32_t st0 = hs, st1 = E * hs, st2 = E * E * hs;
     constexpr uint32_t ncubes = 1u << (3 * J);
 #pragma unroll
-    for (uint32_t c0 = 0; c0 < ncubes; c0 += kInterpThreads) {
-        const uint32_t c = c0 + threadIdx.x;
-        if (ncubes % kInterpThreads != 0 && c >= ncubes) break;
+    for (uint32_t c0 = 0; c0 < ncubes; c0 += kN) {
+        const uint32_t c = c0 + tid;
+        if (ncubes % kN != 0 && c >= ncubes) break;
         const uint32_t ci = c & (m - 1), cj = (c >> J) & (m - 1), ck = c >> (2 * J);
         const uint32_t base = ci * sz + E * (cj * sz + E * (ck * sz));
         float v[27];
@@ -336,12 +349,13 @@ template <uint32_t E, uint32_t T, uint32_t J> __device__ __forceinline__ void cu
 }
 
 // The coarse levels 1 .. K-2 of a tile of T = 2^K cells on its even sub-array (G^3, a tile of T/2 cells).
-template <uint32_t G, uint32_t H, uint32_t J, uint32_t K> __device__ __forceinline__ void tile_levels(float* s)
+template <uint32_t G, uint32_t H, uint32_t J, uint32_t K, uint32_t kN>
+__device__ __forceinline__ void tile_levels(float* s, Crew<kN> cw)
 {
     if constexpr (J + 1 < K) {
-        cube_level_ct<G, H, J>(s);
-        __syncthreads();
-        tile_levels<G, H, J + 1, K>(s);
+        cube_level_ct<G, H, J, kN>(s, cw.tid);
+        cw.sync();
+        tile_levels<G, H, J + 1, K, kN>(s, cw);
     }
 }
 
@@ -456,21 +470,21 @@ __device__ __forceinline__ void finest_cube(const float* s, bool has, uint32_t c
 // runs of Z along z, one run per thread (runs consecutive along x within a
 // warp), so that each cube after the first of a run takes its z = 0 face from
 // the one below; Z makes the runs about as many as the CTA's threads.
-template <uint32_t T, typename OutT, bool kPairs>
+template <uint32_t T, typename OutT, bool kPairs, uint32_t kN>
 __device__ __forceinline__ void finest_store(const float* s, const uint32_t* flags, OutT* out, uint32_t e,
                                              uint32_t pitch, uint32_t ox, uint32_t oy, uint32_t oz, bool far_x,
-                                             bool far_y, bool far_z, float inv_scale, float offset)
+                                             bool far_y, bool far_z, float inv_scale, float offset, uint32_t tid)
 {
     using S = SplitTile<T>;
     constexpr uint32_t H = S::H;
     constexpr uint32_t lh = (H >= 2) ? (31 - __builtin_clz(H)) : 0;
-    constexpr uint32_t per = H * H * H / kInterpThreads;
+    constexpr uint32_t per = H * H * H / kN;
     constexpr uint32_t Z = per >= H ? H : (per >= 1 ? per : 1);
     constexpr uint32_t lzr = 31 - __builtin_clz(Z);
     constexpr uint32_t nruns = H * H * H / Z;
     const uint32_t e2 = e * pitch; // slab stride (a brick holds fewer than 2^32 elements)
 #pragma unroll 1
-    for (uint32_t rr = threadIdx.x; rr < nruns; rr += kInterpThreads) {
+    for (uint32_t rr = tid; rr < nruns; rr += kN) {
         const uint32_t ci = rr & (H - 1), cj = (rr >> lh) & (H - 1), ck0 = (rr >> (2 * lh)) << lzr;
         const bool lx = far_x && ci == H - 1, ly = far_y && cj == H - 1;
         float v[27];
@@ -503,8 +517,8 @@ __device__ __forceinline__ void finest_store(const float* s, const uint32_t* fla
 constexpr uint32_t kPrefetch = 2; // entries per thread held in registers
 struct Prefetch {
     uint32_t item;
-    uint32_t flag; // word threadIdx.x of the item's cube flags
-    uint32_t cidx; // threads 0-7: the coarse-grid index of tile corner threadIdx.x (0xffffffff: none)
+    uint32_t flag; // word tid of the item's cube flags
+    uint32_t cidx; // threads 0-7: the coarse-grid index of tile corner tid (0xffffffff: none)
     float corner;
     uint32_t node_base, e0, e1; // a plan holds fewer than 2^32 nodes and entries
     uint32_t loc[kPrefetch];
@@ -513,7 +527,8 @@ struct Prefetch {
 };
 
 // stage 1: the item's block, entry range, flag word and corner positions in the coarse grid
-__device__ __forceinline__ void prefetch_head(Prefetch& pf, const TileArgs& a, uint32_t item)
+template <uint32_t kN>
+__device__ __forceinline__ void prefetch_head(Prefetch& pf, const TileArgs& a, uint32_t item, uint32_t tid)
 {
     pf.item = item;
     pf.e0 = pf.e1 = 0;
@@ -524,26 +539,26 @@ __device__ __forceinline__ void prefetch_head(Prefetch& pf, const TileArgs& a, u
     pf.node_base = (uint32_t)B->node_base;
     pf.e0 = (uint32_t)a.entry_off[item];
     pf.e1 = (uint32_t)a.entry_off[item + 1];
-    if (threadIdx.x < a.flag_words) pf.flag = a.flags[(uint64_t)item * a.flag_words + threadIdx.x];
-    if (threadIdx.x < 8) {
+    if (tid < a.flag_words) pf.flag = a.flags[(uint64_t)item * a.flag_words + tid];
+    if (tid < 8) {
         const uint32_t L = B->coarse_log2;
         if (L > 0) {
             const uint32_t tile = it.y & 0x7fffffffu, mL = 1u << L, E = mL + 1;
-            const uint32_t cx = (tile & (mL - 1)) + (threadIdx.x & 1);
-            const uint32_t cy = ((tile >> L) & (mL - 1)) + ((threadIdx.x >> 1) & 1);
-            const uint32_t cz = (tile >> (2 * L)) + (threadIdx.x >> 2);
+            const uint32_t cx = (tile & (mL - 1)) + (tid & 1);
+            const uint32_t cy = ((tile >> L) & (mL - 1)) + ((tid >> 1) & 1);
+            const uint32_t cz = (tile >> (2 * L)) + (tid >> 2);
             pf.cidx = B->coarse_off + cx + E * (cy + E * cz);
         }
     }
 }
 
-// stage 2: positions and node indices of the first kPrefetch * kInterpThreads entries, and the corners
-__device__ __forceinline__ void prefetch_index(Prefetch& pf, const TileArgs& a)
+// stage 2: positions and node indices of the first kPrefetch * kN entries, and the corners
+template <uint32_t kN> __device__ __forceinline__ void prefetch_index(Prefetch& pf, const TileArgs& a, uint32_t tid)
 {
     if (pf.cidx != 0xffffffffu) pf.corner = a.coarse[pf.cidx];
 #pragma unroll
     for (uint32_t q = 0; q < kPrefetch; ++q) {
-        const uint32_t i = pf.e0 + threadIdx.x + q * kInterpThreads;
+        const uint32_t i = pf.e0 + tid + q * kN;
         if (i < pf.e1) {
             pf.loc[q] = a.entry_local[i];
             pf.node[q] = a.entry_node[i];
@@ -552,11 +567,11 @@ __device__ __forceinline__ void prefetch_index(Prefetch& pf, const TileArgs& a)
 }
 
 // stage 3: their node values
-__device__ __forceinline__ void prefetch_values(Prefetch& pf, const TileArgs& a)
+template <uint32_t kN> __device__ __forceinline__ void prefetch_values(Prefetch& pf, const TileArgs& a, uint32_t tid)
 {
 #pragma unroll
     for (uint32_t q = 0; q < kPrefetch; ++q)
-        if (pf.e0 + threadIdx.x + q * kInterpThreads < pf.e1) pf.val[q] = a.sparse[pf.node_base + pf.node[q]];
+        if (pf.e0 + tid + q * kN < pf.e1) pf.val[q] = a.sparse[pf.node_base + pf.node[q]];
 }
 
 struct TileItem {
@@ -568,9 +583,11 @@ struct TileItem {
 
 // One tile of T = 2^k cells.  Tiles of T >= 2 use the split layout; T = 1
 // (depth-0 blocks) is a plain 2x2x2 copy of the root corners.
-template <uint32_t T, bool kGrid, typename OutT>
+// cw: the CTA or the warp running the tile; next_item(): the next work item's number (read once the current
+// item's entries are placed, so that its first prefetch stage goes out behind this tile's work).
+template <uint32_t T, bool kGrid, typename OutT, uint32_t kN, class NextFn>
 __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* desc, uint32_t* flags, const TileItem& t,
-                                         Prefetch& pf, const uint32_t* next_item)
+                                         Prefetch& pf, Crew<kN> cw, NextFn next_item)
 {
     constexpr uint32_t E = T + 1, E3 = E * E * E;
     using S = SplitTile<T < 2 ? 2 : T>;
@@ -583,22 +600,22 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
     const uint32_t e = (1u << d) + 1u;
     constexpr uint32_t nflags = T >= 2 ? (S::H * S::H * S::H + 31) / 32 : 0;
     if constexpr (kGrid) {
-        for (uint32_t q = threadIdx.x; q < nflags; q += kInterpThreads) flags[q] = 0u;
+        for (uint32_t q = cw.tid; q < nflags; q += kN) flags[q] = 0u;
     } else {
-        if (threadIdx.x < nflags) flags[threadIdx.x] = pf.flag; // the plan's flags, prefetched
+        if (cw.tid < nflags) flags[cw.tid] = pf.flag; // the plan's flags, prefetched
     }
     // 1. the tile's sparse values (NaN elsewhere) and the descent's
     if constexpr (kGrid) {
-        __syncthreads(); // flags cleared
+        cw.sync(); // flags cleared
 #pragma unroll 1
-        for (uint32_t p = threadIdx.x; p < E3; p += kInterpThreads) {
+        for (uint32_t p = cw.tid; p < E3; p += kN) {
             const uint32_t lx = p % E, r = p / E, ly = r % E, lz = r / E;
             const float v = to_internal(a.grid[((uint64_t)(oz + lz) * e + (oy + ly)) * e + (ox + lx)]);
             s[at(lx, ly, lz)] = v;
             if constexpr (T >= 2)
                 if (!isnan(v)) flag_cubes(flags, S::H, lx, ly, lz);
         }
-        for (uint32_t q = threadIdx.x; q < 27 * L; q += kInterpThreads) {
+        for (uint32_t q = cw.tid; q < 27 * L; q += kN) {
             const uint32_t l = q / 27, p = q % 27;
             const uint32_t size = 1u << (d - l), hs = size >> 1;
             const uint32_t bx = ox & ~(size - 1), by = oy & ~(size - 1), bz = oz & ~(size - 1);
@@ -617,29 +634,29 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
                 if (!t.slots) n4 = (G3 + 3) / 4;
             }
 #pragma unroll 1
-            for (uint32_t p = threadIdx.x; p < n4; p += kInterpThreads) s4[p] = nan4;
+            for (uint32_t p = cw.tid; p < n4; p += kN) s4[p] = nan4;
         }
-        __syncthreads();
+        cw.sync();
         auto place = [&](uint32_t loc, float v) {
             if (loc < E3) s[loc] = v;
         };
         // the prefetched entries, then any beyond what the registers held
 #pragma unroll
         for (uint32_t q = 0; q < kPrefetch; ++q)
-            if (pf.e0 + threadIdx.x + q * kInterpThreads < pf.e1) place(pf.loc[q], to_internal(pf.val[q]));
-        for (uint32_t i = pf.e0 + threadIdx.x + kPrefetch * kInterpThreads; i < pf.e1; i += kInterpThreads)
+            if (pf.e0 + cw.tid + q * kN < pf.e1) place(pf.loc[q], to_internal(pf.val[q]));
+        for (uint32_t i = pf.e0 + cw.tid + kPrefetch * kN; i < pf.e1; i += kN)
             place(a.entry_local[i], to_internal(a.sparse[t.node_base + a.entry_node[i]]));
         // a tile of a block with coarse levels: its corners from the block's coarse grid
         if (pf.cidx != 0xffffffffu)
-            s[at((threadIdx.x & 1) * T, ((threadIdx.x >> 1) & 1) * T, (threadIdx.x >> 2) * T)] = pf.corner;
-        prefetch_head(pf, a, *next_item); // the current item's entries are placed
+            s[at((cw.tid & 1) * T, ((cw.tid >> 1) & 1) * T, (cw.tid >> 2) * T)] = pf.corner;
+        prefetch_head<kN>(pf, a, next_item(), cw.tid); // the current item's entries are placed
     }
-    __syncthreads();
+    cw.sync();
     // 2. single-grid form: tile corners from the coarse levels; then the tile cube's own
     //    midpoints (its first level): warp 0, each level's 27 points in registers
     if ((kGrid && L > 0) || T >= 4) {
-        if (threadIdx.x < 32) {
-            const uint32_t lane = threadIdx.x;
+        if (kN == 32 || cw.tid < 32) {
+            const uint32_t lane = cw.tid & 31;
             if (kGrid && L > 0) {
                 const float corner = descend_regs(desc, d, L, ox, oy, oz, lane);
                 if (lane < 8) s[at((lane & 1) * T, ((lane >> 1) & 1) * T, (lane >> 2) * T)] = corner;
@@ -647,13 +664,13 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
             }
             if constexpr (T >= 4) tile_top<T>(s, lane);
         }
-        __syncthreads();
+        cw.sync();
     }
-    if constexpr (!kGrid) prefetch_index(pf, a);
+    if constexpr (!kGrid) prefetch_index<kN>(pf, a, cw.tid);
     // 3. the remaining coarser levels on the even sub-array (a tile of T/2 cells)
-    if constexpr (T >= 8) tile_levels<S::G, S::H, 1, 31 - __builtin_clz(T)>(s);
+    if constexpr (T >= 8) tile_levels<S::G, S::H, 1, 31 - __builtin_clz(T), kN>(s, cw);
     // 4. the finest level, straight to HBM, while the next item's entries load
-    if constexpr (!kGrid) prefetch_values(pf, a);
+    if constexpr (!kGrid) prefetch_values<kN>(pf, a, cw.tid);
     float inv_scale = 1.f, offset = 0.f;
     if constexpr (!kGrid) {
         if (a.scale_offset) {
@@ -666,10 +683,11 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
     OutT* out = reinterpret_cast<OutT*>(a.out) + t.dense_off;
     const bool far_x = t.tx == mL - 1, far_y = t.ty == mL - 1, far_z = t.tz == mL - 1;
     if constexpr (T >= 2) {
-        finest_store<T, OutT, !kGrid>(s, flags, out, e, t.pitch, ox, oy, oz, far_x, far_y, far_z, inv_scale, offset);
+        finest_store<T, OutT, !kGrid, kN>(s, flags, out, e, t.pitch, ox, oy, oz, far_x, far_y, far_z, inv_scale,
+                                          offset, cw.tid);
     } else {
         // depth-0 block: its 8 root corners
-        for (uint32_t q = threadIdx.x; q < 8; q += kInterpThreads) {
+        for (uint32_t q = cw.tid; q < 8; q += kN) {
             const uint32_t x = q & 1, y = (q >> 1) & 1, z = q >> 2;
             Store<OutT>::put(out, ((uint64_t)(oz + z) * e + (oy + y)) * t.pitch + ox + x, s[at(x, y, z)],
                              inv_scale, offset);

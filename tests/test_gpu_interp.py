@@ -111,12 +111,13 @@ def test_batched_plan_bit_exact_with_oracle(ctx, tile):
     plan.close()
 
 
+@pytest.mark.parametrize("tile", [8, 16])
 @pytest.mark.parametrize("fmt", [_lib.BRICK_F16, _lib.BRICK_BF16])
-def test_batched_16bit_bricks_decode_within_quantization(ctx, fmt):
+def test_batched_16bit_bricks_decode_within_quantization(ctx, fmt, tile):
     import torch
     from revise_gb300.api import FramePlan
     w = workloads.small(seed=4, level=1, depths=(3, 4, 5), mask_fraction=0.1)
-    plan = FramePlan(ctx, w, fmt, tile_cells=16)
+    plan = FramePlan(ctx, w, fmt, tile_cells=tile)
     plan.interp(torch.from_numpy(w.sparse).cuda())
     torch.cuda.synchronize()
     dense = plan.dense()
