@@ -12,7 +12,8 @@
 // GB300 form: a cube at level L is self-contained -- every vertex inside it
 // (faces and edges included) depends only on the cube's 8 corners and on the
 // sparse nodes inside it -- so the grid is cut into tiles of 2^k cells, each
-// computed by one CTA in shared memory in a single launch:
+// computed by one CTA (one warp, for plans of tiles up to 8 cells) in shared
+// memory in a single launch:
 //   1. the tile's sparse nodes are placed into a NaN-filled shared tile;
 //   2. one warp walks the L = d - k coarse levels down from the block's root
 //      corners to the tile's 8 corners (27 points per level);
