@@ -469,7 +469,7 @@ __device__ __forceinline__ void finest_cube(const float* s, bool has, uint32_t c
 // The finest level of a tile, written straight to HBM: its H^3 2x2x2 cubes in
 // runs of Z along z, one run per thread (runs consecutive along x within a
 // warp), so that each cube after the first of a run takes its z = 0 face from
-// the one below; Z makes the runs about as many as the CTA's threads.
+// the one below; Z makes the runs about as many as the tile's threads (kN).
 template <uint32_t T, typename OutT, bool kPairs, uint32_t kN>
 __device__ __forceinline__ void finest_store(const float* s, const uint32_t* flags, OutT* out, uint32_t e,
                                              uint32_t pitch, uint32_t ox, uint32_t oy, uint32_t oz, bool far_x,
@@ -513,7 +513,7 @@ __device__ __forceinline__ void finest_store(const float* s, const uint32_t* fla
 // issued one phase of the current tile ahead of its use, so that the chain of
 // dependent global loads -- item and block, then entry positions and node
 // indices, then node values -- completes behind the current tile's work
-// instead of stalling the CTA at every tile.
+// instead of stalling the tile's threads at every tile.
 constexpr uint32_t kPrefetch = 2; // entries per thread held in registers
 struct Prefetch {
     uint32_t item;
@@ -653,7 +653,7 @@ __device__ __forceinline__ void run_tile(const TileArgs& a, float* s, float* des
     }
     cw.sync();
     // 2. single-grid form: tile corners from the coarse levels; then the tile cube's own
-    //    midpoints (its first level): warp 0, each level's 27 points in registers
+    //    midpoints (its first level): the first warp, each level's 27 points in registers
     if ((kGrid && L > 0) || T >= 4) {
         if (kN == 32 || cw.tid < 32) {
             const uint32_t lane = cw.tid & 31;
