@@ -260,7 +260,7 @@ template <uint32_t T> struct SplitTile {
     }
 };
 
-// Warp 0, T >= 4: the tile cube's 27 points (corners at 0 and T, midpoints at
+// The first warp of the tile's threads, T >= 4: the tile cube's 27 points (corners at 0 and T, midpoints at
 // T/2) from its corners and the sparse values already in the tile -- the
 // tile's first level, cube_level on its single cube, in registers.
 template <uint32_t T> __device__ __forceinline__ void tile_top(float* s, uint32_t lane)
